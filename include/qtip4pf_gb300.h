@@ -1,0 +1,194 @@
+/* qtip4pf_gb300 -- C ABI of the GB300 (sm_103a) force and ring-polymer
+ * propagation library for flexible qTIP4P/F water.
+ *
+ * Two tiers, both plain C (pointers and sizes; no C++ or torch types):
+ *
+ *  1. Per-call entries that take HOST arrays in the reference's layouts and
+ *     mirror one reference function each (copy in, compute on the GPU, copy
+ *     out, synchronise). Each declaration names the reference interface it
+ *     replaces (rayseashyn/qtip4pf_water, file:line).
+ *  2. A device-resident stepper: state lives in HBM, each MD step is one CUDA
+ *     graph replay, and estimators are read back on demand.
+ *
+ * Layouts (the reference's, indexing.h:6-24), per system:
+ *   positions q, momenta p, forces f   double[P][9N]  [bead][mol][O,H1,H2][x,y,z]
+ *   Verlet list                        int point[P][N], int list[P][list_size]
+ *   oxygen displacements               double[P][3N]
+ *   charges double[3N] (per site), masses double[9N] (per degree of freedom)
+ * Units: Hartree atomic units throughout (qtip4pfparams.h:43-61).
+ *
+ * Every entry returns a qtg_status (0 = success). On failure the message is
+ * available from qtg_last_error(ctx). No entry aborts the process. */
+#ifndef QTIP4PF_GB300_H
+#define QTIP4PF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct qtg_ctx qtg_ctx;
+
+typedef enum {
+    QTG_OK = 0,
+    QTG_ERR_ARG = 1,           /* bad argument or system index */
+    QTG_ERR_CUDA = 2,          /* a CUDA runtime call failed */
+    QTG_ERR_LIST_OVERFLOW = 3, /* a Verlet list needed more than list_size entries */
+    QTG_ERR_NONFINITE = 4,     /* NaN/Inf in forces or energies */
+    QTG_ERR_STATE = 5,         /* call made in the wrong state (e.g. no forces yet) */
+    QTG_ERR_NODEVICE = 6       /* no usable sm_103 device */
+} qtg_status;
+
+typedef enum {
+    QTG_FP64 = 0,  /* every force term in FP64 (parity mode) */
+    QTG_MIXED = 1  /* Ewald terms in FP32 with FP64 accumulation; LJ, intramolecular,
+                      integration, normal modes and thermostat in FP64 */
+} qtg_precision;
+
+typedef enum {
+    QTG_SUZUKI_CHIN = 0, /* fourth-order SC forces (forces.cpp:698-789); P even */
+    QTG_TROTTER = 1      /* second-order: every bead weight 1 (also P = 1) */
+} qtg_propagator;
+
+typedef enum {
+    QTG_THERMO_NONE = 0,   /* NVE */
+    QTG_THERMO_PILE_G = 1, /* centroid global rescale + mode Langevin (thermostat.cpp:64-133) */
+    QTG_THERMO_PILE_L = 2  /* centroid Langevin with time constant tau0 + mode Langevin */
+} qtg_thermostat;
+
+/* One independent system (replica). box in bohr; dt in fs. */
+typedef struct qtg_system_desc {
+    int n_mols;
+    int n_beads;
+    double box_bohr[3];
+    double temp_K;
+    double dt_fs;
+    double eps_ewald;  /* config.txt eps_ewald: acc = sqrt(-ln eps) (water.cpp:148) */
+    double eps_sc;     /* config.txt epsilon_sc (forces.cpp:754) */
+    int propagator;    /* qtg_propagator */
+    int thermostat;    /* qtg_thermostat */
+    double tau0_fs;    /* centroid time constant for QTG_THERMO_PILE_L */
+    uint64_t seed;     /* counter-based RNG key for this system */
+} qtg_system_desc;
+
+/* Derived per-system parameters, as the reference derives them
+ * (water.cpp:76-157, forces.cpp:574-584). */
+typedef struct qtg_system_info {
+    int n_mols, n_beads, n_dof, list_size, k_max, n_kvectors;
+    double kappa, rc, kc, dt, beta_n, omega_psq;
+} qtg_system_info;
+
+/* ---- context --------------------------------------------------------------- */
+/* Creates a context on the current CUDA device holding n_systems systems.
+ * All device memory is allocated here; no later call allocates. */
+qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precision, qtg_ctx **out);
+void qtg_destroy(qtg_ctx *ctx);
+const char *qtg_last_error(const qtg_ctx *ctx);
+const char *qtg_status_string(int status);
+/* Work is issued on this stream (a cudaStream_t passed as void*; NULL = the
+ * context's own stream). */
+qtg_status qtg_set_stream(qtg_ctx *ctx, void *cuda_stream);
+qtg_status qtg_system_info_get(const qtg_ctx *ctx, int sys, qtg_system_info *out);
+/* Number of this library's kernels launched since the context was created. */
+qtg_status qtg_kernel_launches(const qtg_ctx *ctx, uint64_t *out);
+/* Replace the default per-site charges / per-dof masses of one system. */
+qtg_status qtg_set_charges(qtg_ctx *ctx, int sys, const double *charge);
+qtg_status qtg_set_masses(qtg_ctx *ctx, int sys, const double *mass);
+
+/* ---- tier 1: per-call entries mirroring the reference ---------------------- */
+/* neighbour.cpp:12-62  void neighbour_list(pos, point, list, disp, bead)
+ * Bit-identical CSR list; the bead's disp slice is zeroed. */
+qtg_status qtg_neighbour_list(qtg_ctx *ctx, int sys, const double *pos, int *point, int *list,
+                              double *disp, int bead);
+/* forces.cpp:468-630  double get_forces_nospline(pos, f, charge, point, list, bead)
+ * Writes the bead's slice of f and the bead's potential energy. */
+qtg_status qtg_get_forces(qtg_ctx *ctx, int sys, const double *pos, double *f,
+                          const double *charge, const int *point, const int *list, int bead,
+                          double *energy);
+/* forces.cpp:180-448  double kwald(charge_pos, force, charge, k_max, kappa, k_cut_sq, bead)
+ * sites: the bead's charge sites (M, H1, H2); f_sites receives += k-space forces. */
+qtg_status qtg_kwald(qtg_ctx *ctx, int sys, const double *sites, double *f_sites,
+                     const double *charge, int bead, double *energy);
+/* forces.cpp:698-789  double force_eval_sc_nospline(pos, f, charge, mass, point, list,
+ *                                                  sc_pot, fphys) */
+qtg_status qtg_force_eval_sc(qtg_ctx *ctx, int sys, const double *pos, double *f,
+                             const double *charge, const double *mass, const int *point,
+                             const int *list, double *sc_pot, double *fphys, double *energy);
+/* Second-order assembly (no reference counterpart): f = fphys = -dV/dq per bead,
+ * *energy = sum_b V_b, *pot = sum_b V_b / P. */
+qtg_status qtg_force_eval_trotter(qtg_ctx *ctx, int sys, const double *pos, double *f,
+                                  const double *charge, const int *point, const int *list,
+                                  double *pot, double *energy);
+/* fourier.cpp:12-69  void ftransform(a, length, is_forwards)  (a: double[P][length]) */
+qtg_status qtg_ftransform(qtg_ctx *ctx, int sys, double *a, int length, int forwards);
+/* thermostat.cpp:64-133  double pile_g(p, mass, rng), on normal-mode momenta.
+ * noise = [R, g2, xi(mode 1..P-1, dof 0..9N-1)] supplied by the caller, or NULL to
+ * draw from the system's counter-based generator. *heat receives the return value. */
+qtg_status qtg_pile_g(qtg_ctx *ctx, int sys, double *p, const double *mass,
+                      const double *noise, double *heat);
+/* path_integrals.cpp:29-48  double get_kcv(q, f) */
+qtg_status qtg_get_kcv(qtg_ctx *ctx, int sys, const double *q, const double *f, double *out);
+/* path_integrals.cpp:55-81  double get_conserved(q, p, mass, energy); like the
+ * reference, q and p are round-tripped through the normal-mode transform in place. */
+qtg_status qtg_get_conserved(qtg_ctx *ctx, int sys, double *q, double *p, const double *mass,
+                             double energy, double *out);
+/* update.cpp:78-137  double update_trajectory_class_nospline(q, p, mass, f, charge,
+ *                                                           point, list, disp) */
+qtg_status qtg_update_class(qtg_ctx *ctx, int sys, double *q, double *p, const double *mass,
+                            double *f, const double *charge, int *point, int *list, double *disp,
+                            double *energy);
+/* update.cpp:271-401  double update_sc_nospline(q, p, mass, f, fphys, charge, point, list,
+ *                                               disp, rng, is_nvt, heat, sc_pot)
+ * The system's propagator decides the force assembly (SC or Trotter). noise as for
+ * qtg_pile_g (NULL = counter-based generator). *heat is updated in place. */
+qtg_status qtg_update_pimd(qtg_ctx *ctx, int sys, double *q, double *p, const double *mass,
+                           double *f, double *fphys, const double *charge, int *point,
+                           int *list, double *disp, int is_nvt, const double *noise,
+                           double *heat, double *pot, double *energy);
+
+/* ---- tier 2: device-resident stepping -------------------------------------- */
+/* Upload a system's positions and momenta (double[P][9N] each; p may be NULL = 0). */
+qtg_status qtg_set_state(qtg_ctx *ctx, int sys, const double *q, const double *p);
+/* Download state; any pointer may be NULL. f is the propagating force (SC or
+ * Trotter), fphys the physical force -dV/dq per bead. */
+qtg_status qtg_get_state(qtg_ctx *ctx, int sys, double *q, double *p, double *f, double *fphys,
+                         double *disp);
+/* Build every Verlet list and evaluate the initial forces of every system
+ * (simulation.cpp:838-874). Must precede qtg_run_steps. */
+qtg_status qtg_init_forces(qtg_ctx *ctx);
+/* Advance every system n_steps steps (each a CUDA graph replay), NVT if is_nvt.
+ * Estimators of every step are recorded on the device. Asynchronous on the
+ * context's stream: call qtg_sync to wait and collect device-side errors. */
+qtg_status qtg_run_steps(qtg_ctx *ctx, int n_steps, int is_nvt);
+qtg_status qtg_sync(qtg_ctx *ctx);
+/* Per-step estimator records of one system since the last reset, oldest first.
+ * Record layout (QTG_EST_FIELDS doubles): see QTG_EST_* indices. */
+#define QTG_EST_FIELDS 8
+#define QTG_EST_POT 0       /* potential estimator: SC sc_pot, Trotter sum V_b / P */
+#define QTG_EST_KCV 1       /* centroid-virial kinetic energy estimator */
+#define QTG_EST_CONSERVED 2 /* ring-polymer Hamiltonian + heat (path_integrals.cpp:55-81) */
+#define QTG_EST_HEAT 3      /* accumulated thermostat heat (update.cpp:325) */
+#define QTG_EST_KIN 4       /* bead-space kinetic energy sum p^2/2m */
+#define QTG_EST_VTOT 5      /* force-eval return value (SC tot_energy, Trotter sum V_b) */
+#define QTG_EST_REBUILDS 6  /* Verlet-list rebuilds performed this step (all beads) */
+#define QTG_EST_STEP 7      /* step index */
+qtg_status qtg_get_estimators(qtg_ctx *ctx, int sys, double *out, int max_records, int *n_records);
+qtg_status qtg_reset_estimators(qtg_ctx *ctx);
+
+/* ---- measurement helpers (no reference counterpart) ------------------------ */
+/* Average duration (ms, CUDA events on the context's stream) of `iters`
+ * back-to-back launches of one kernel of the force / step pipeline over every
+ * system, after one full force evaluation. name: "prep", "real", "ksk",
+ * "kforce", "combine", "lj", "rebuild", "ring", "end_step". Overwrites the
+ * context's forces and may move its state: call after the measured run. */
+qtg_status qtg_time_kernel(qtg_ctx *ctx, const char *name, int iters, double *avg_ms);
+/* FP32 fused-multiply-add throughput of the current device (TFLOP/s, 2 flops
+ * per FMA) from a dependent-chain kernel filling every SM. */
+qtg_status qtg_fp32_peak(double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

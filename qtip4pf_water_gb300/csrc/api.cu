@@ -1,0 +1,1348 @@
+// Host side of libqtipgpu: context, parameter derivation, job tables, the C ABI.
+//
+// All device memory is allocated in qtg_create; no later call allocates.
+// A context holds any number of independent systems (replicas) of uneven
+// size, laid out back to back in every array; each force-evaluation launch
+// covers a table of jobs (system, bead) so all replicas advance together.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/qtip4pf_gb300.h"
+#include "qtg_internal.h"
+
+using namespace qtg;
+
+namespace {
+
+// ---- qTIP4P/F constants (qtip4pfparams.h:41-133, same values and order) ----
+Consts make_consts() {
+    Consts K;
+    const double me = 9.10938356e-31, kb = 1.38064852e-23, Na = 6.0221409e23;
+    const double eh = 4.3597447222071e-18, kcal2au = 1.5936e-3;
+    const double mhgmol = 1.0080, mogmol = 15.9994, hbar_SI = 1.054571817e-34;
+    K.angs2bohr = 1.0 / 0.529177210903;
+    K.mo = 0.001 * mogmol / (Na * me);
+    K.mh = 0.001 * mhgmol / (Na * me);
+    K.K2au = kb / eh;
+    const double au2fs = hbar_SI * 1e15 / eh;
+    K.fs2au = 1.0 / au2fs;
+    K.r_cut = 9.0 * K.angs2bohr;
+    K.r_cut_sq = K.r_cut * K.r_cut;
+    K.r_skin = 1.30 * K.r_cut;
+    K.r_skin_sq = K.r_skin * K.r_skin;
+    K.gamma_vs = 0.73612;
+    K.epslj = 0.1852 * kcal2au;
+    const double sigmalj = 3.1589 * K.angs2bohr;
+    K.sigmalj6 = pow(sigmalj, 6.0);
+    K.sigmalj12 = K.sigmalj6 * K.sigmalj6;
+    K.e_cut = 4.0 * K.epslj * (pow((sigmalj / K.r_cut), 12.0) - pow((sigmalj / K.r_cut), 6.0));
+    K.roheq = 0.9419 * K.angs2bohr;
+    const double ar = 2.287 / K.angs2bohr;
+    K.ar2 = ar * ar;
+    K.ar3 = K.ar2 * ar;
+    K.ar4fac = 7.0 * K.ar3 * ar / 12.0;
+    K.Dr = 116.09 * kcal2au;
+    K.theta_eq = 107.4 * PI_REF / 180.0;
+    K.ktheta = 87.85 * kcal2au;
+    K.qo = -1.1128;
+    K.qh = -0.5 * K.qo;
+    return K;
+}
+
+// The k-vectors forces.cpp:251-445 visits, in its order.
+void enumerate_k(const SysDev &S, double kc_sq, std::vector<KVec> &out) {
+    double bk[3];
+    for (int d = 0; d < 3; ++d) bk[d] = 2.0 * PI_REF / S.box[d];
+    const double quart = 0.25 / (S.kappa * S.kappa);
+    const int km = S.k_max;
+    auto push = [&](int a, int b, int c, double ksq) {
+        KVec v;
+        v.kx = a;
+        v.ky = b;
+        v.kz = c;
+        v.pad = 0;
+        v.coef = S.k_pref * exp(-ksq * quart) / ksq * (a ? 2.0 : 1.0);
+        v.gx = 2.0 * v.coef * bk[0] * a;
+        v.gy = 2.0 * v.coef * bk[1] * b;
+        v.gz = 2.0 * v.coef * bk[2] * c;
+        out.push_back(v);
+    };
+    for (int kx = 0; kx <= km; ++kx) {
+        const double rx = bk[0] * kx;
+        double ksq = rx * rx;
+        if (ksq > 0.0 && ksq < kc_sq) push(kx, 0, 0, ksq);
+        for (int kz = 1; kz <= km; ++kz) {
+            const double rz = bk[2] * kz;
+            ksq = rx * rx + rz * rz;
+            if (ksq > kc_sq) break;
+            push(kx, 0, kz, ksq);
+            push(kx, 0, -kz, ksq);
+        }
+        for (int ky = 1; ky <= km; ++ky) {
+            const double ry = bk[1] * ky;
+            ksq = rx * rx + ry * ry;
+            if (ksq > kc_sq) break;
+            push(kx, ky, 0, ksq);
+            push(kx, -ky, 0, ksq);
+            for (int kz = 1; kz <= km; ++kz) {
+                const double rz = bk[2] * kz;
+                ksq = rx * rx + ry * ry + rz * rz;
+                if (ksq > kc_sq) break;
+                push(kx, ky, kz, ksq);
+                push(kx, ky, -kz, ksq);
+                push(kx, -ky, kz, ksq);
+                push(kx, -ky, -kz, ksq);
+            }
+        }
+    }
+}
+
+// Orthonormal bead -> normal-mode matrix in FFTW halfcomplex order with
+// fourier.cpp:39-51's scaling (sqrt(1/P) for k = 0 and k = P/2, sqrt(2/P) else).
+void nm_matrix(int P, std::vector<double> &C) {
+    C.assign((size_t)P * P, 0.0);
+    const double two_pi = 6.283185307179586476925286766559;
+    for (int b = 0; b < P; ++b) C[b] = sqrt(1.0 / P);
+    for (int k = 1; 2 * k < P; ++k)
+        for (int b = 0; b < P; ++b) {
+            const double ang = two_pi * (double)(((long)b * k) % P) / (double)P;
+            C[(size_t)k * P + b] = sqrt(2.0 / P) * cos(ang);
+            C[(size_t)(P - k) * P + b] = -sqrt(2.0 / P) * sin(ang);
+        }
+    if (P % 2 == 0 && P > 1)
+        for (int b = 0; b < P; ++b) C[(size_t)(P / 2) * P + b] = sqrt(1.0 / P) * ((b % 2 == 0) ? 1.0 : -1.0);
+}
+
+struct Table {  // a device job table plus its host copy
+    std::vector<Job> h;
+    Job *d = nullptr;
+};
+
+}  // namespace
+
+struct qtg_ctx {
+    int device = 0;
+    int precision = QTG_FP64;
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    std::string err;
+    Consts K;
+    std::vector<qtg_system_desc> desc;
+    std::vector<SysDev> sys_h;
+    std::vector<double> kc_sq;
+    std::vector<int> cw_begin, cw_count;  // column work ranges per system
+    SysDev *sys_d = nullptr;
+    int n_sys = 0;
+    size_t total_dof = 0, total_disp = 0, total_point = 0, total_list = 0, total_sites = 0;
+    size_t total_nm = 0, total_modes = 0, total_kvec = 0, total_phase = 0, total_slots = 0;
+    int max_mols = 0, max_kvec = 0, max_kmax = 0, max_p = 1, max_dof = 0;
+    bool any_sc = false, mixed = false;
+    // state
+    double *q = nullptr, *p = nullptr, *f = nullptr, *fphys = nullptr, *disp = nullptr;
+    int *point = nullptr, *list = nullptr;
+    double *charge = nullptr, *mass = nullptr;
+    double *qdisp = nullptr, *fdisp = nullptr, *fsr = nullptr, *dirv = nullptr, *sc_scale = nullptr;
+    double *stage = nullptr;  // per-call staging (total_dof doubles)
+    double *noise = nullptr;  // per-call noise (2 + (Pmax-1) * 9Nmax)
+    size_t noise_len = 0;
+    KVec *kvec = nullptr;
+    double *nm = nullptr;
+    ModeCoef *modes = nullptr;
+    // per-slot scratch
+    void *sites = nullptr, *tan_sites = nullptr, *phase = nullptr;
+    double *site_force = nullptr;
+    double2 *sk = nullptr, *dsk = nullptr;
+    double *energy = nullptr;      // per slot: energies of the base evaluations
+    double *energy_aux = nullptr;  // per slot: displaced / derivative evaluations
+    // job tables
+    Table base, fd, tan, fd_sc, tan_sc;
+    std::vector<int> fd_begin, fd_count, tan_begin, tan_count;  // per system
+    int *base_sys = nullptr, *base_bead = nullptr;  // (system, bead) of every base job
+    int *odd_sys = nullptr, *odd_bead = nullptr;    // odd beads of even-P systems
+    std::vector<int> odd_begin, odd_count;
+    int n_odd = 0;
+    int *sc_sys = nullptr, *sc_bead = nullptr;      // odd beads of SC systems (stepper)
+    int n_sc_odd = 0;
+    ColWork *colwork = nullptr;
+    int n_colwork = 0;
+    // run state
+    SysAcc *acc = nullptr;
+    SysRun *run = nullptr;
+    double *est = nullptr;
+    int max_records = 4096;
+    unsigned long long *step = nullptr, *records = nullptr;
+    unsigned *status = nullptr;
+    double *red_out = nullptr;  // small reduction output
+    bool forces_ready = false;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    unsigned long long graph_kernels[2] = {0, 0};
+    unsigned long long launches = 0;
+};
+
+namespace {
+
+qtg_status fail(qtg_ctx *c, qtg_status st, const std::string &msg) {
+    if (c) c->err = msg;
+    return st;
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(ctx, QTG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e == cudaSuccess) e = cudaMemset(*p, 0, n * sizeof(T));
+    return e;
+}
+
+EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, double *out, int mode, int sr_only) {
+    EvalArgs a;
+    memset(&a, 0, sizeof(a));
+    a.sys = c->sys_d;
+    a.jobs = jobs;
+    a.n_jobs = n_jobs;
+    a.max_mols = c->max_mols;
+    a.max_kvec = c->max_kvec;
+    a.max_kmax = c->max_kmax;
+    a.pos = pos;
+    a.out = out;
+    a.dir = c->dirv;
+    a.charge = c->charge;
+    a.point = c->point;
+    a.list = c->list;
+    a.kvec = c->kvec;
+    a.sites = c->sites;
+    a.site_force = c->site_force;
+    a.phase = c->phase;
+    a.sk = c->sk;
+    a.dsk = c->dsk;
+    a.tan_sites = c->tan_sites;
+    a.energy = c->energy;
+    a.status = c->status;
+    a.mode = mode;
+    a.sr_only = sr_only;
+    a.c = c->K;
+    return a;
+}
+
+EvalArgs aux_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, double *out, int mode, int sr_only) {
+    EvalArgs a = eval_args(c, jobs, n_jobs, pos, out, mode, sr_only);
+    a.energy = c->energy_aux;
+    return a;
+}
+
+void launch_eval(qtg_ctx *c, const EvalArgs &a) {
+    if (c->mixed) launch_eval_mixed(a, c->stream, &c->launches);
+    else launch_eval_fp64(a, c->stream, &c->launches);
+}
+
+RingArgs ring_args(qtg_ctx *c, int sys, int flags) {
+    RingArgs r;
+    memset(&r, 0, sizeof(r));
+    r.sys = c->sys_d;
+    if (sys < 0) {
+        r.work = c->colwork;
+        r.n_work = c->n_colwork;
+    } else {
+        r.work = c->colwork + c->cw_begin[sys];
+        r.n_work = c->cw_count[sys];
+    }
+    r.flags = flags;
+    r.q = c->q;
+    r.p = c->p;
+    r.f = c->f;
+    r.fphys = c->fphys;
+    r.disp = c->disp;
+    r.mass = c->mass;
+    r.nm = c->nm;
+    r.modes = c->modes;
+    r.run = c->run;
+    r.acc = c->acc;
+    r.step = c->step;
+    r.kcv_all_beads = -1;
+    r.max_p = c->max_p;
+    return r;
+}
+
+FinalizeArgs fin_args(qtg_ctx *c, int sys, int record, int draw_alpha) {
+    FinalizeArgs f;
+    memset(&f, 0, sizeof(f));
+    f.sys = c->sys_d;
+    f.n_sys = c->n_sys;
+    f.energy = c->energy;
+    f.acc = c->acc;
+    f.run = c->run;
+    f.est = c->est;
+    f.max_records = c->max_records;
+    f.step = c->step;
+    f.records = c->records;
+    f.status = c->status;
+    f.record = record;
+    f.draw_alpha = draw_alpha;
+    f.sys_begin = sys < 0 ? 0 : sys;
+    f.sys_end = sys < 0 ? c->n_sys : sys + 1;
+    return f;
+}
+
+ScArgs sc_args(qtg_ctx *c) {
+    ScArgs s;
+    memset(&s, 0, sizeof(s));
+    s.sys = c->sys_d;
+    s.q = c->q;
+    s.fphys = c->fphys;
+    s.mass = c->mass;
+    s.qdisp = c->qdisp;
+    s.dirv = c->dirv;
+    s.fdisp = c->fdisp;
+    s.fsr = c->fsr;
+    s.f = c->f;
+    s.sc_scale = c->sc_scale;
+    s.acc = c->acc;
+    s.mixed = c->mixed ? 1 : 0;
+    s.max_dof = c->max_dof;
+    return s;
+}
+
+ListArgs list_args(qtg_ctx *c, int first_job, int n_jobs, int force) {
+    ListArgs l;
+    memset(&l, 0, sizeof(l));
+    l.sys = c->sys_d;
+    l.job_sys = c->base_sys + first_job;
+    l.job_bead = c->base_bead + first_job;
+    l.n_jobs = n_jobs;
+    l.q = c->q;
+    l.disp = c->disp;
+    l.point = c->point;
+    l.list = c->list;
+    l.acc = c->acc;
+    l.status = c->status;
+    l.force_rebuild = force;
+    l.max_mols = c->max_mols;
+    return l;
+}
+
+// Forces of the given systems (sys < 0: all): physical forces into fphys, the
+// propagating force into f (SC assembly for SC systems or force_sc; copy for
+// Trotter). Positions are read from q.
+void enqueue_forces(qtg_ctx *c, int sys, bool force_sc) {
+    const int jb = sys < 0 ? 0 : c->sys_h[sys].job_base;
+    const int nj = sys < 0 ? (int)c->base.h.size() : c->sys_h[sys].n_beads;
+    launch_eval(c, eval_args(c, c->base.d + jb, nj, c->q, c->fphys, 0, 0));
+    // odd beads that need the Suzuki-Chin force gradient
+    const int *osys, *obead;
+    const Job *fdj, *tanj;
+    int n_odd, fdn, tn;
+    if (sys < 0) {
+        osys = c->sc_sys;
+        obead = c->sc_bead;
+        n_odd = c->n_sc_odd;
+        fdj = c->fd_sc.d;
+        fdn = (int)c->fd_sc.h.size();
+        tanj = c->tan_sc.d;
+        tn = (int)c->tan_sc.h.size();
+    } else {
+        const bool sc = force_sc || c->sys_h[sys].propagator == QTG_SUZUKI_CHIN;
+        osys = c->odd_sys + c->odd_begin[sys];
+        obead = c->odd_bead + c->odd_begin[sys];
+        n_odd = sc ? c->odd_count[sys] : 0;
+        fdj = c->fd.d + c->fd_begin[sys];
+        fdn = sc ? c->fd_count[sys] : 0;
+        tanj = c->tan.d + c->tan_begin[sys];
+        tn = sc ? c->tan_count[sys] : 0;
+    }
+    ScArgs sa = sc_args(c);
+    sa.force_sc = force_sc ? 1 : 0;
+    if (n_odd > 0) {
+        sa.job_sys = osys;
+        sa.job_bead = obead;
+        sa.n_jobs = n_odd;
+        launch_sc_prepare(sa, c->stream, &c->launches);
+        if (c->mixed) {
+            launch_eval(c, aux_args(c, tanj, tn, c->q, c->fdisp, 1, 0));
+            launch_eval(c, aux_args(c, fdj, fdn, c->qdisp, c->fsr, 0, 1));
+        } else {
+            launch_eval(c, aux_args(c, fdj, fdn, c->qdisp, c->fdisp, 0, 0));
+        }
+    }
+    sa.job_sys = c->base_sys + jb;
+    sa.job_bead = c->base_bead + jb;
+    sa.n_jobs = nj;
+    launch_sc_finish(sa, c->stream, &c->launches);
+}
+
+void enqueue_step(qtg_ctx *c, int sys, int nvt, int ext_noise, bool pile_g) {
+    RingArgs r = ring_args(c, sys, RF_KICK | RF_FWD | RF_CAYLEY | RF_BACK | RF_DISP | (nvt ? RF_THERMO : 0));
+    r.noise = ext_noise ? c->noise : nullptr;
+    r.pile_g = pile_g ? 1 : 0;
+    launch_ring(r, c->stream, &c->launches);
+    const int jb = sys < 0 ? 0 : c->sys_h[sys].job_base;
+    const int nj = sys < 0 ? (int)c->base.h.size() : c->sys_h[sys].n_beads;
+    launch_skin_rebuild(list_args(c, jb, nj, 0), c->stream, &c->launches);
+    enqueue_forces(c, sys, false);
+    RingArgs e = ring_args(c, sys, 0);
+    e.kick = 1;
+    launch_end_step(e, c->stream, &c->launches);
+    FinalizeArgs fa = fin_args(c, sys, 1, nvt);
+    fa.noise = nullptr;
+    fa.pile_g = pile_g ? 1 : 0;
+    launch_finalize(fa, c->stream, &c->launches);
+}
+
+qtg_status check_sys(qtg_ctx *ctx, int sys) {
+    if (!ctx) return QTG_ERR_ARG;
+    if (sys < 0 || sys >= ctx->n_sys) return fail(ctx, QTG_ERR_ARG, "system index out of range");
+    return QTG_OK;
+}
+
+qtg_status sync_status(qtg_ctx *ctx) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    unsigned st = 0;
+    CK(cudaMemcpy(&st, ctx->status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (st) {
+        CK(cudaMemset(ctx->status, 0, sizeof(unsigned)));
+        if (st & ST_LIST_OVERFLOW) return fail(ctx, QTG_ERR_LIST_OVERFLOW, "Verlet list exceeded list_size");
+        if (st & ST_NONFINITE) return fail(ctx, QTG_ERR_NONFINITE, "non-finite energy or force");
+        if (st & ST_GAMMA_LIMIT) return fail(ctx, QTG_ERR_NONFINITE, "gamma variate iteration limit reached");
+    }
+    return QTG_OK;
+}
+
+#define CKS(expr)                            \
+    do {                                     \
+        qtg_status s_ = (expr);              \
+        if (s_ != QTG_OK) return s_;         \
+    } while (0)
+
+cudaError_t up(qtg_ctx *c, void *dst, const void *src, size_t bytes) {
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+}
+cudaError_t down(qtg_ctx *c, void *dst, const void *src, size_t bytes) {
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
+}
+
+qtg_status refresh_sys(qtg_ctx *ctx, int sys) {
+    CK(cudaMemcpyAsync(ctx->sys_d + sys, &ctx->sys_h[sys], sizeof(SysDev), cudaMemcpyHostToDevice, ctx->stream));
+    return QTG_OK;
+}
+
+qtg_status upload_charges(qtg_ctx *ctx, int sys, const double *charge) {
+    SysDev &S = ctx->sys_h[sys];
+    double self = 0.0;
+    for (int i = 0; i < S.n_sites; ++i) self += 0.5 * S.ewald_pref * charge[i] * charge[i];
+    S.self_energy = self;
+    CK(up(ctx, ctx->charge + S.chg_off, charge, sizeof(double) * S.n_sites));
+    return refresh_sys(ctx, sys);
+}
+
+}  // namespace
+
+// ============================================================================
+extern "C" {
+
+const char *qtg_status_string(int s) {
+    switch (s) {
+        case QTG_OK: return "ok";
+        case QTG_ERR_ARG: return "invalid argument";
+        case QTG_ERR_CUDA: return "CUDA error";
+        case QTG_ERR_LIST_OVERFLOW: return "Verlet list overflow";
+        case QTG_ERR_NONFINITE: return "non-finite value";
+        case QTG_ERR_STATE: return "invalid state";
+        case QTG_ERR_NODEVICE: return "no sm_103 device";
+        default: return "unknown status";
+    }
+}
+
+const char *qtg_last_error(const qtg_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precision, qtg_ctx **out) {
+    if (!out || !systems || n_systems <= 0) return QTG_ERR_ARG;
+    *out = nullptr;
+    if (precision != QTG_FP64 && precision != QTG_MIXED) return QTG_ERR_ARG;
+    for (int s = 0; s < n_systems; ++s) {
+        const qtg_system_desc &d = systems[s];
+        if (d.n_mols < 2 || d.n_beads < 1 || d.n_beads > 128) return QTG_ERR_ARG;
+        if (d.n_beads > 1 && (d.n_beads % 2) && d.propagator == QTG_SUZUKI_CHIN) return QTG_ERR_ARG;
+        if (!(d.box_bohr[0] > 0 && d.box_bohr[1] > 0 && d.box_bohr[2] > 0)) return QTG_ERR_ARG;
+        if (!(d.temp_K > 0) || !(d.dt_fs > 0) || !(d.eps_ewald > 0 && d.eps_ewald < 1)) return QTG_ERR_ARG;
+        if (d.propagator != QTG_SUZUKI_CHIN && d.propagator != QTG_TROTTER) return QTG_ERR_ARG;
+        if (d.thermostat < 0 || d.thermostat > 2) return QTG_ERR_ARG;
+        if (d.thermostat == QTG_THERMO_PILE_L && !(d.tau0_fs > 0)) return QTG_ERR_ARG;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return QTG_ERR_NODEVICE;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return QTG_ERR_NODEVICE;
+    if (prop.major != 10 || prop.minor != 3) return QTG_ERR_NODEVICE;
+
+    qtg_ctx *ctx = new qtg_ctx();
+    ctx->device = dev;
+    ctx->precision = precision;
+    ctx->mixed = precision == QTG_MIXED;
+    ctx->K = make_consts();
+    ctx->n_sys = n_systems;
+    ctx->desc.assign(systems, systems + n_systems);
+    const Consts &K = ctx->K;
+    std::vector<KVec> kall;
+    std::vector<double> nm_all;
+    std::vector<ModeCoef> mode_all;
+    std::vector<double> chg_all, mass_all;
+    long long q_off = 0, d_off = 0, pt_off = 0, ls_off = 0, chg_off = 0, mass_off = 0;
+    long long nm_off = 0, mode_off = 0;
+    int job_base = 0;
+    for (int s = 0; s < n_systems; ++s) {
+        const qtg_system_desc &d = systems[s];
+        SysDev S;
+        memset(&S, 0, sizeof(S));
+        const int N = d.n_mols, P = d.n_beads;
+        S.n_mols = N;
+        S.n_beads = P;
+        S.n_sites = 3 * N;
+        S.n_dof = 9 * N;
+        S.propagator = d.propagator;
+        S.thermostat = d.thermostat;
+        S.job_base = job_base;
+        S.cols_per_block = 256 / P;
+        S.seed = d.seed;
+        for (int k = 0; k < 3; ++k) {
+            S.box[k] = d.box_bohr[k];
+            S.inv_box[k] = 1.0 / d.box_bohr[k];
+            S.boxf[k] = (float)S.box[k];
+            S.inv_boxf[k] = (float)S.inv_box[k];
+        }
+        // water.cpp:76-157 with the box given directly
+        S.beta = 1.0 / (K.K2au * d.temp_K);
+        S.beta_n = S.beta / P;
+        const double omega_p = 1.0 / S.beta_n;
+        S.omega_psq = omega_p * omega_p;
+        S.dt = d.dt_fs * K.fs2au;
+        S.halfdt = 0.5 * S.dt;
+        S.eps_sc = d.eps_sc;
+        const double vol = S.box[0] * S.box[1] * S.box[2];
+        const double rho_ox = N / vol;
+        S.list_size = (int)std::round(4.0 * K.r_skin * K.r_skin * K.r_skin * N * rho_ox);
+        const double acc = sqrt(-log(d.eps_ewald));
+        const double rho = (3 * N) / vol;
+        const double min_box = std::min(std::min(S.box[0], S.box[1]), S.box[2]);
+        const double max_box = std::max(std::max(S.box[0], S.box[1]), S.box[2]);
+        S.k_pref = 2.0 * PI_REF / vol;
+        // forces.cpp:574-584
+        double kappa = 2.6 * pow(rho / vol, 1.0 / 6.0);
+        double rc = acc / kappa;
+        if (rc > 0.5 * min_box) {
+            rc = 0.5 * min_box;
+            kappa = acc / rc;
+        }
+        S.kappa = kappa;
+        S.rc_sq = rc * rc;
+        const double kc = 2.0 * acc * kappa;
+        S.k_max = (int)(kc * max_box / (2.0 * PI_REF));
+        S.ewald_pref = 2.0 * kappa / sqrt(PI_REF);
+        S.kappaf = (float)kappa;
+        S.kappa_sqf = (float)(kappa * kappa);
+        S.rc_sqf = (float)S.rc_sq;
+        S.ewald_preff = (float)S.ewald_pref;
+        S.r_cut_sq = K.r_cut_sq;
+        S.r_skin_sq = K.r_skin_sq;
+        S.skin_margin = K.r_skin - K.r_cut;
+        S.c1_centroid = d.thermostat == QTG_THERMO_PILE_L ? exp(-S.dt / (d.tau0_fs * K.fs2au)) : 0.0;
+        std::vector<KVec> kv;
+        enumerate_k(S, kc * kc, kv);
+        S.n_kvec = (int)kv.size();
+        S.kvec_off = (int)kall.size();
+        kall.insert(kall.end(), kv.begin(), kv.end());
+        ctx->kc_sq.push_back(kc * kc);
+        S.q_off = q_off;
+        S.d_off = d_off;
+        S.pt_off = pt_off;
+        S.ls_off = ls_off;
+        S.chg_off = chg_off;
+        S.mass_off = mass_off;
+        S.nm_off = nm_off;
+        S.mode_off = mode_off;
+        q_off += (long long)P * 9 * N;
+        d_off += (long long)P * 3 * N;
+        pt_off += (long long)P * N;
+        ls_off += (long long)P * S.list_size;
+        chg_off += 3 * N;
+        mass_off += 9 * N;
+        nm_off += (long long)P * P;
+        mode_off += P;
+        job_base += P;
+        std::vector<double> C;
+        nm_matrix(P, C);
+        nm_all.insert(nm_all.end(), C.begin(), C.end());
+        const double piovern = PI_REF / P;
+        const double pref = 2.0 / S.beta_n, pref_sq = pref * pref, gpref = 4.0 / S.beta_n;
+        for (int k = 0; k < P; ++k) {
+            ModeCoef mc;
+            const double sn = sin(k * piovern);
+            mc.w2 = pref_sq * sn * sn;
+            mc.scale = 1.0 / sqrt(1.0 + 0.25 * mc.w2 * S.dt * S.dt);
+            const double gk = gpref * sin(k * PI_REF / P);
+            mc.c1 = exp(-S.dt * gk);
+            mc.c2 = sqrt(1.0 - mc.c1 * mc.c1);
+            mode_all.push_back(mc);
+        }
+        for (int m = 0; m < N; ++m) {
+            chg_all.push_back(K.qo);
+            chg_all.push_back(K.qh);
+            chg_all.push_back(K.qh);
+            for (int a = 0; a < 3; ++a)
+                for (int k = 0; k < 3; ++k) mass_all.push_back(a == 0 ? K.mo : K.mh);
+        }
+        double self = 0.0;
+        for (int i = 0; i < 3 * N; ++i) self += 0.5 * S.ewald_pref * chg_all[S.chg_off + i] * chg_all[S.chg_off + i];
+        S.self_energy = self;
+        ctx->sys_h.push_back(S);
+        ctx->max_mols = std::max(ctx->max_mols, N);
+        ctx->max_kvec = std::max(ctx->max_kvec, S.n_kvec);
+        ctx->max_kmax = std::max(ctx->max_kmax, S.k_max);
+        ctx->max_p = std::max(ctx->max_p, P);
+        ctx->max_dof = std::max(ctx->max_dof, 9 * N);
+        if (d.propagator == QTG_SUZUKI_CHIN && P > 1) ctx->any_sc = true;
+    }
+    ctx->total_dof = (size_t)q_off;
+    ctx->total_disp = (size_t)d_off;
+    ctx->total_point = (size_t)pt_off;
+    ctx->total_list = (size_t)ls_off;
+    ctx->total_nm = (size_t)nm_off;
+    ctx->total_modes = (size_t)mode_off;
+    ctx->total_kvec = kall.size();
+
+    // scratch slots: one per base job (bead), sized for its system
+    std::vector<long long> slot_site, slot_phase, slot_sk;
+    long long so = 0, po = 0, ko = 0;
+    for (int s = 0; s < n_systems; ++s) {
+        const SysDev &S = ctx->sys_h[s];
+        for (int b = 0; b < S.n_beads; ++b) {
+            slot_site.push_back(so);
+            slot_phase.push_back(po);
+            slot_sk.push_back(ko);
+            so += S.n_sites;
+            po += (long long)3 * (S.k_max + 1) * S.n_sites;
+            ko += S.n_kvec;
+        }
+    }
+    ctx->total_slots = slot_site.size();
+    ctx->total_sites = (size_t)so;
+    ctx->total_phase = (size_t)po;
+    auto mkjob = [&](int s, int b, int slot, int mode, long long pos_off) {
+        Job j;
+        j.sys = s;
+        j.bead = b;
+        j.slot = slot;
+        j.mode = mode;
+        j.pos_off = pos_off;
+        j.out_off = pos_off;
+        j.site_off = slot_site[slot];
+        j.phase_off = slot_phase[slot];
+        j.sk_off = slot_sk[slot];
+        return j;
+    };
+    std::vector<int> bsys, bbead, osys, obead, scs, scb;
+    for (int s = 0; s < n_systems; ++s) {
+        const SysDev &S = ctx->sys_h[s];
+        ctx->fd_begin.push_back((int)ctx->fd.h.size());
+        ctx->tan_begin.push_back((int)ctx->tan.h.size());
+        ctx->odd_begin.push_back((int)osys.size());
+        for (int b = 0; b < S.n_beads; ++b) {
+            ctx->base.h.push_back(mkjob(s, b, S.job_base + b, 0, S.q_off + (long long)b * S.n_dof));
+            bsys.push_back(s);
+            bbead.push_back(b);
+        }
+        if (S.n_beads % 2 == 0) {
+            for (int b = 1; b < S.n_beads; b += 2) {
+                ctx->fd.h.push_back(mkjob(s, b, S.job_base + b, 0, S.q_off + (long long)b * S.n_dof));
+                ctx->fd.h.push_back(mkjob(s, b, S.job_base + b - 1, 0, S.q_off + (long long)(b - 1) * S.n_dof));
+                ctx->tan.h.push_back(mkjob(s, b, S.job_base + b, 1, S.q_off + (long long)b * S.n_dof));
+                osys.push_back(s);
+                obead.push_back(b);
+                if (S.propagator == QTG_SUZUKI_CHIN) {
+                    scs.push_back(s);
+                    scb.push_back(b);
+                    ctx->fd_sc.h.push_back(ctx->fd.h[ctx->fd.h.size() - 2]);
+                    ctx->fd_sc.h.push_back(ctx->fd.h[ctx->fd.h.size() - 1]);
+                    ctx->tan_sc.h.push_back(ctx->tan.h.back());
+                }
+            }
+        }
+        ctx->fd_count.push_back((int)ctx->fd.h.size() - ctx->fd_begin[s]);
+        ctx->tan_count.push_back((int)ctx->tan.h.size() - ctx->tan_begin[s]);
+        ctx->odd_count.push_back((int)osys.size() - ctx->odd_begin[s]);
+    }
+    ctx->n_odd = (int)osys.size();
+    ctx->n_sc_odd = (int)scs.size();
+    std::vector<ColWork> cw;
+    for (int s = 0; s < n_systems; ++s) {
+        const SysDev &S = ctx->sys_h[s];
+        ctx->cw_begin.push_back((int)cw.size());
+        for (int c0 = 0; c0 < S.n_dof; c0 += S.cols_per_block) {
+            ColWork w;
+            w.sys = s;
+            w.col0 = c0;
+            w.ncols = std::min(S.cols_per_block, S.n_dof - c0);
+            w.pad = 0;
+            cw.push_back(w);
+        }
+        ctx->cw_count.push_back((int)cw.size() - ctx->cw_begin[s]);
+    }
+    ctx->n_colwork = (int)cw.size();
+    ctx->noise_len = 2 + (size_t)(ctx->max_p - 1) * ctx->max_dof;
+
+    init_force_kernel_attributes();
+    init_list_kernel_attributes();
+    init_propagate_kernel_attributes();
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+    ctx->stream = ctx->own_stream;
+#define AL(ptr, n)                                  \
+    if (e == cudaSuccess) e = dalloc(&(ptr), (n));
+    AL(ctx->sys_d, n_systems);
+    AL(ctx->q, ctx->total_dof);
+    AL(ctx->p, ctx->total_dof);
+    AL(ctx->f, ctx->total_dof);
+    AL(ctx->fphys, ctx->total_dof);
+    AL(ctx->qdisp, ctx->total_dof);
+    AL(ctx->fdisp, ctx->total_dof);
+    AL(ctx->fsr, ctx->total_dof);
+    AL(ctx->dirv, ctx->total_dof);
+    AL(ctx->stage, ctx->total_dof);
+    AL(ctx->disp, ctx->total_disp);
+    AL(ctx->point, ctx->total_point);
+    AL(ctx->list, ctx->total_list);
+    AL(ctx->charge, chg_all.size());
+    AL(ctx->mass, mass_all.size());
+    AL(ctx->sc_scale, ctx->total_slots);
+    AL(ctx->noise, ctx->noise_len);
+    AL(ctx->kvec, kall.size());
+    AL(ctx->nm, nm_all.size());
+    AL(ctx->modes, mode_all.size());
+    {
+        // sized for the FP64 element types: 4 doubles per site, 2 per phase entry
+        double *tmp = nullptr;
+        AL(tmp, 4 * ctx->total_sites);
+        ctx->sites = tmp;
+        tmp = nullptr;
+        AL(tmp, 4 * ctx->total_sites);
+        ctx->tan_sites = tmp;
+        tmp = nullptr;
+        AL(tmp, 2 * ctx->total_phase);
+        ctx->phase = tmp;
+    }
+    AL(ctx->site_force, 3 * ctx->total_sites);
+    AL(ctx->sk, (size_t)ko);
+    AL(ctx->dsk, (size_t)ko);
+    AL(ctx->energy, ctx->total_slots);
+    AL(ctx->energy_aux, ctx->total_slots);
+    AL(ctx->base.d, ctx->base.h.size());
+    AL(ctx->fd.d, ctx->fd.h.size());
+    AL(ctx->tan.d, ctx->tan.h.size());
+    AL(ctx->fd_sc.d, ctx->fd_sc.h.size());
+    AL(ctx->tan_sc.d, ctx->tan_sc.h.size());
+    AL(ctx->base_sys, bsys.size());
+    AL(ctx->base_bead, bbead.size());
+    AL(ctx->odd_sys, osys.size());
+    AL(ctx->odd_bead, obead.size());
+    AL(ctx->sc_sys, scs.size());
+    AL(ctx->sc_bead, scb.size());
+    AL(ctx->colwork, cw.size());
+    AL(ctx->acc, n_systems);
+    AL(ctx->run, n_systems);
+    AL(ctx->est, (size_t)ctx->max_records * n_systems * 8);
+    AL(ctx->step, 1);
+    AL(ctx->records, 1);
+    AL(ctx->status, 1);
+    AL(ctx->red_out, 8);
+#undef AL
+    auto cp = [&](void *dst, const void *src, size_t bytes) {
+        if (e == cudaSuccess && bytes) e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    };
+    cp(ctx->sys_d, ctx->sys_h.data(), sizeof(SysDev) * n_systems);
+    cp(ctx->charge, chg_all.data(), sizeof(double) * chg_all.size());
+    cp(ctx->mass, mass_all.data(), sizeof(double) * mass_all.size());
+    cp(ctx->kvec, kall.data(), sizeof(KVec) * kall.size());
+    cp(ctx->nm, nm_all.data(), sizeof(double) * nm_all.size());
+    cp(ctx->modes, mode_all.data(), sizeof(ModeCoef) * mode_all.size());
+    cp(ctx->base.d, ctx->base.h.data(), sizeof(Job) * ctx->base.h.size());
+    cp(ctx->fd.d, ctx->fd.h.data(), sizeof(Job) * ctx->fd.h.size());
+    cp(ctx->tan.d, ctx->tan.h.data(), sizeof(Job) * ctx->tan.h.size());
+    cp(ctx->fd_sc.d, ctx->fd_sc.h.data(), sizeof(Job) * ctx->fd_sc.h.size());
+    cp(ctx->tan_sc.d, ctx->tan_sc.h.data(), sizeof(Job) * ctx->tan_sc.h.size());
+    cp(ctx->base_sys, bsys.data(), sizeof(int) * bsys.size());
+    cp(ctx->base_bead, bbead.data(), sizeof(int) * bbead.size());
+    cp(ctx->odd_sys, osys.data(), sizeof(int) * osys.size());
+    cp(ctx->odd_bead, obead.data(), sizeof(int) * obead.size());
+    cp(ctx->sc_sys, scs.data(), sizeof(int) * scs.size());
+    cp(ctx->sc_bead, scb.data(), sizeof(int) * scb.size());
+    cp(ctx->colwork, cw.data(), sizeof(ColWork) * cw.size());
+    if (e == cudaSuccess) {
+        std::vector<SysRun> runs(n_systems);
+        for (auto &r : runs) {
+            r.heat = 0.0;
+            r.alpha = 1.0;
+            r.pad[0] = r.pad[1] = 0.0;
+        }
+        cp(ctx->run, runs.data(), sizeof(SysRun) * n_systems);
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        ctx->err = std::string("allocation/upload failed: ") + cudaGetErrorString(e);
+        qtg_destroy(ctx);
+        return QTG_ERR_CUDA;
+    }
+    *out = ctx;
+    return QTG_OK;
+}
+
+void qtg_destroy(qtg_ctx *ctx) {
+    if (!ctx) return;
+    for (int i = 0; i < 2; ++i)
+        if (ctx->graph[i]) cudaGraphExecDestroy(ctx->graph[i]);
+    void *ptrs[] = {ctx->sys_d, ctx->q, ctx->p, ctx->f, ctx->fphys, ctx->qdisp, ctx->fdisp, ctx->fsr,
+                    ctx->dirv, ctx->stage, ctx->disp, ctx->point, ctx->list, ctx->charge, ctx->mass,
+                    ctx->sc_scale, ctx->noise, ctx->kvec, ctx->nm, ctx->modes, ctx->sites, ctx->tan_sites,
+                    ctx->phase, ctx->site_force, ctx->sk, ctx->dsk, ctx->energy, ctx->energy_aux,
+                    ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
+                    ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
+                    ctx->status, ctx->red_out};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+qtg_status qtg_set_stream(qtg_ctx *ctx, void *stream) {
+    if (!ctx) return QTG_ERR_ARG;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return QTG_OK;
+}
+
+qtg_status qtg_system_info_get(const qtg_ctx *ctx, int sys, qtg_system_info *out) {
+    if (!ctx || !out || sys < 0 || sys >= ctx->n_sys) return QTG_ERR_ARG;
+    const SysDev &S = ctx->sys_h[sys];
+    out->n_mols = S.n_mols;
+    out->n_beads = S.n_beads;
+    out->n_dof = S.n_dof;
+    out->list_size = S.list_size;
+    out->k_max = S.k_max;
+    out->n_kvectors = S.n_kvec;
+    out->kappa = S.kappa;
+    out->rc = sqrt(S.rc_sq);
+    out->kc = sqrt(ctx->kc_sq[sys]);
+    out->dt = S.dt;
+    out->beta_n = S.beta_n;
+    out->omega_psq = S.omega_psq;
+    return QTG_OK;
+}
+
+qtg_status qtg_kernel_launches(const qtg_ctx *ctx, uint64_t *out) {
+    if (!ctx || !out) return QTG_ERR_ARG;
+    *out = ctx->launches;
+    return QTG_OK;
+}
+
+qtg_status qtg_set_charges(qtg_ctx *ctx, int sys, const double *charge) {
+    CKS(check_sys(ctx, sys));
+    if (!charge) return fail(ctx, QTG_ERR_ARG, "null charge array");
+    CKS(upload_charges(ctx, sys, charge));
+    return sync_status(ctx);
+}
+
+qtg_status qtg_set_masses(qtg_ctx *ctx, int sys, const double *mass) {
+    CKS(check_sys(ctx, sys));
+    if (!mass) return fail(ctx, QTG_ERR_ARG, "null mass array");
+    const SysDev &S = ctx->sys_h[sys];
+    CK(up(ctx, ctx->mass + S.mass_off, mass, sizeof(double) * S.n_dof));
+    return sync_status(ctx);
+}
+
+// ---- tier 1 ------------------------------------------------------------------------
+
+qtg_status qtg_neighbour_list(qtg_ctx *ctx, int sys, const double *pos, int *point, int *list, double *disp,
+                              int bead) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    if (!pos || !point || !list || !disp || bead < 0 || bead >= S.n_beads) return fail(ctx, QTG_ERR_ARG, "bad argument");
+    const size_t nd = S.n_dof;
+    CK(up(ctx, ctx->q + S.q_off + bead * nd, pos + bead * nd, sizeof(double) * nd));
+    launch_skin_rebuild(list_args(ctx, S.job_base + bead, 1, 1), ctx->stream, &ctx->launches);
+    CK(down(ctx, point + (size_t)bead * S.n_mols, ctx->point + S.pt_off + (size_t)bead * S.n_mols, sizeof(int) * S.n_mols));
+    CK(down(ctx, list + (size_t)bead * S.list_size, ctx->list + S.ls_off + (size_t)bead * S.list_size,
+            sizeof(int) * S.list_size));
+    CK(down(ctx, disp + (size_t)bead * 3 * S.n_mols, ctx->disp + S.d_off + (size_t)bead * 3 * S.n_mols,
+            sizeof(double) * 3 * S.n_mols));
+    CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
+    return sync_status(ctx);
+}
+
+static qtg_status upload_lists(qtg_ctx *ctx, int sys, const int *point, const int *list, int bead_lo, int bead_hi) {
+    const SysDev &S = ctx->sys_h[sys];
+    const int nb = bead_hi - bead_lo;
+    CK(up(ctx, ctx->point + S.pt_off + (size_t)bead_lo * S.n_mols, point + (size_t)bead_lo * S.n_mols,
+          sizeof(int) * S.n_mols * nb));
+    CK(up(ctx, ctx->list + S.ls_off + (size_t)bead_lo * S.list_size, list + (size_t)bead_lo * S.list_size,
+          sizeof(int) * (size_t)S.list_size * nb));
+    return QTG_OK;
+}
+
+qtg_status qtg_get_forces(qtg_ctx *ctx, int sys, const double *pos, double *f, const double *charge,
+                          const int *point, const int *list, int bead, double *energy) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    if (!pos || !f || !point || !list || bead < 0 || bead >= S.n_beads) return fail(ctx, QTG_ERR_ARG, "bad argument");
+    const size_t nd = S.n_dof;
+    if (charge) CKS(upload_charges(ctx, sys, charge));
+    CK(up(ctx, ctx->q + S.q_off + bead * nd, pos + bead * nd, sizeof(double) * nd));
+    CKS(upload_lists(ctx, sys, point, list, bead, bead + 1));
+    const int jb = S.job_base + bead;
+    launch_eval(ctx, eval_args(ctx, ctx->base.d + jb, 1, ctx->q, ctx->fphys, 0, 0));
+    CK(down(ctx, f + bead * nd, ctx->fphys + S.q_off + bead * nd, sizeof(double) * nd));
+    double e = 0.0;
+    CK(down(ctx, &e, ctx->energy + jb, sizeof(double)));
+    CKS(sync_status(ctx));
+    if (energy) *energy = e;
+    return QTG_OK;
+}
+
+qtg_status qtg_kwald(qtg_ctx *ctx, int sys, const double *sites, double *f_sites, const double *charge, int bead,
+                     double *energy) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    if (!sites || !f_sites || bead < 0 || bead >= S.n_beads) return fail(ctx, QTG_ERR_ARG, "bad argument");
+    const size_t nd = S.n_dof;
+    if (charge) CKS(upload_charges(ctx, sys, charge));
+    CK(up(ctx, ctx->stage + S.q_off + bead * nd, sites + bead * nd, sizeof(double) * nd));
+    const int jb = S.job_base + bead;
+    const Job &J = ctx->base.h[jb];
+    CK(up(ctx, ctx->site_force + 3 * J.site_off, f_sites + bead * nd, sizeof(double) * nd));
+    EvalArgs a = eval_args(ctx, ctx->base.d + jb, 1, ctx->stage, ctx->fphys, 0, 0);
+    a.sites_are_input = 1;
+    a.skip_short_range = 1;
+    launch_kwald_only(a, ctx->mixed, ctx->stream, &ctx->launches);
+    CK(down(ctx, f_sites + bead * nd, ctx->site_force + 3 * J.site_off, sizeof(double) * nd));
+    double e = 0.0;
+    CK(down(ctx, &e, ctx->energy + jb, sizeof(double)));
+    CKS(sync_status(ctx));
+    if (energy) *energy = e;
+    return QTG_OK;
+}
+
+static qtg_status read_energies(qtg_ctx *ctx, int sys, double *vsum, double *veven, double *sc_extra) {
+    const SysDev &S = ctx->sys_h[sys];
+    std::vector<double> e(S.n_beads);
+    SysAcc acc;
+    CK(down(ctx, e.data(), ctx->energy + S.job_base, sizeof(double) * S.n_beads));
+    CK(down(ctx, &acc, ctx->acc + sys, sizeof(SysAcc)));
+    CKS(sync_status(ctx));
+    CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
+    double vs = 0.0, ve = 0.0;
+    for (int b = 0; b < S.n_beads; ++b) {
+        vs += e[b];
+        if (b % 2 == 0) ve += e[b];
+    }
+    *vsum = vs;
+    *veven = ve;
+    *sc_extra = acc.sc_extra;
+    return QTG_OK;
+}
+
+qtg_status qtg_force_eval_sc(qtg_ctx *ctx, int sys, const double *pos, double *f, const double *charge,
+                             const double *mass, const int *point, const int *list, double *sc_pot, double *fphys,
+                             double *energy) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    if (!pos || !f || !point || !list || !fphys || S.n_beads % 2) return fail(ctx, QTG_ERR_ARG, "bad argument");
+    const size_t nt = (size_t)S.n_beads * S.n_dof;
+    if (charge) CKS(upload_charges(ctx, sys, charge));
+    if (mass) CK(up(ctx, ctx->mass + S.mass_off, mass, sizeof(double) * S.n_dof));
+    CK(up(ctx, ctx->q + S.q_off, pos, sizeof(double) * nt));
+    CKS(upload_lists(ctx, sys, point, list, 0, S.n_beads));
+    CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
+    enqueue_forces(ctx, sys, true);
+    CK(down(ctx, f, ctx->f + S.q_off, sizeof(double) * nt));
+    CK(down(ctx, fphys, ctx->fphys + S.q_off, sizeof(double) * nt));
+    double vs, ve, extra;
+    CKS(read_energies(ctx, sys, &vs, &ve, &extra));
+    if (sc_pot) *sc_pot = 2.0 * ve / S.n_beads;
+    if (energy) *energy = (2.0 * ve + 4.0 * (vs - ve) + extra) / 3.0;
+    return QTG_OK;
+}
+
+qtg_status qtg_force_eval_trotter(qtg_ctx *ctx, int sys, const double *pos, double *f, const double *charge,
+                                  const int *point, const int *list, double *pot, double *energy) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    if (!pos || !f || !point || !list) return fail(ctx, QTG_ERR_ARG, "bad argument");
+    const size_t nt = (size_t)S.n_beads * S.n_dof;
+    if (charge) CKS(upload_charges(ctx, sys, charge));
+    CK(up(ctx, ctx->q + S.q_off, pos, sizeof(double) * nt));
+    CKS(upload_lists(ctx, sys, point, list, 0, S.n_beads));
+    launch_eval(ctx, eval_args(ctx, ctx->base.d + S.job_base, S.n_beads, ctx->q, ctx->fphys, 0, 0));
+    CK(down(ctx, f, ctx->fphys + S.q_off, sizeof(double) * nt));
+    double vs, ve, extra;
+    CKS(read_energies(ctx, sys, &vs, &ve, &extra));
+    if (pot) *pot = vs / S.n_beads;
+    if (energy) *energy = vs;
+    return QTG_OK;
+}
+
+qtg_status qtg_ftransform(qtg_ctx *ctx, int sys, double *a, int length, int forwards) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    if (!a || length <= 0 || length > S.n_dof) return fail(ctx, QTG_ERR_ARG, "bad argument");
+    const size_t nt = (size_t)S.n_beads * length;
+    double *buf = ctx->stage + S.q_off;
+    CK(up(ctx, buf, a, sizeof(double) * nt));
+    launch_transform(ctx->sys_d, sys, S.n_beads, ctx->nm + S.nm_off, buf, length, forwards, ctx->stream,
+                     &ctx->launches);
+    CK(down(ctx, a, buf, sizeof(double) * nt));
+    return sync_status(ctx);
+}
+
+qtg_status qtg_pile_g(qtg_ctx *ctx, int sys, double *p, const double *mass, const double *noise, double *heat) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    if (!p) return fail(ctx, QTG_ERR_ARG, "bad argument");
+    const size_t nt = (size_t)S.n_beads * S.n_dof;
+    if (mass) CK(up(ctx, ctx->mass + S.mass_off, mass, sizeof(double) * S.n_dof));
+    CK(up(ctx, ctx->p + S.q_off, p, sizeof(double) * nt));
+    if (noise) CK(up(ctx, ctx->noise, noise, sizeof(double) * (2 + (size_t)(S.n_beads - 1) * S.n_dof)));
+    CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
+    CK(cudaMemsetAsync(&ctx->run[sys].heat, 0, sizeof(double), ctx->stream));
+    RingArgs r = ring_args(ctx, sys, RF_THERMO);
+    r.pile_g = 1;
+    r.noise = noise ? ctx->noise : nullptr;
+    launch_centroid_ke(r, ctx->stream, &ctx->launches);
+    FinalizeArgs fa = fin_args(ctx, sys, 0, 1);
+    fa.pile_g = 1;
+    fa.noise = noise ? ctx->noise : nullptr;
+    launch_finalize(fa, ctx->stream, &ctx->launches);
+    launch_ring(r, ctx->stream, &ctx->launches);
+    CK(down(ctx, p, ctx->p + S.q_off, sizeof(double) * nt));
+    double h = 0.0;
+    CK(down(ctx, &h, &ctx->run[sys].heat, sizeof(double)));
+    CKS(sync_status(ctx));
+    if (heat) *heat = -h;
+    return QTG_OK;
+}
+
+qtg_status qtg_get_kcv(qtg_ctx *ctx, int sys, const double *q, const double *f, double *out) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    if (!q || !f || !out) return fail(ctx, QTG_ERR_ARG, "bad argument");
+    const size_t nt = (size_t)S.n_beads * S.n_dof;
+    CK(up(ctx, ctx->q + S.q_off, q, sizeof(double) * nt));
+    CK(up(ctx, ctx->fphys + S.q_off, f, sizeof(double) * nt));
+    CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
+    RingArgs e = ring_args(ctx, sys, 0);
+    e.kick = 0;
+    e.kcv_all_beads = 0;  // even beads only, as path_integrals.cpp:37-44
+    e.f = ctx->fphys;
+    launch_end_step(e, ctx->stream, &ctx->launches);
+    SysAcc acc;
+    CK(down(ctx, &acc, ctx->acc + sys, sizeof(SysAcc)));
+    CKS(sync_status(ctx));
+    CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
+    *out = 0.5 * S.n_dof / S.beta + acc.kcv_tq / S.n_beads;
+    return sync_status(ctx);
+}
+
+qtg_status qtg_get_conserved(qtg_ctx *ctx, int sys, double *q, double *p, const double *mass, double energy,
+                             double *out) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    if (!q || !p || !out) return fail(ctx, QTG_ERR_ARG, "bad argument");
+    const size_t nt = (size_t)S.n_beads * S.n_dof;
+    if (mass) CK(up(ctx, ctx->mass + S.mass_off, mass, sizeof(double) * S.n_dof));
+    CK(up(ctx, ctx->q + S.q_off, q, sizeof(double) * nt));
+    CK(up(ctx, ctx->p + S.q_off, p, sizeof(double) * nt));
+    CK(cudaMemsetAsync(ctx->red_out, 0, 2 * sizeof(double), ctx->stream));
+    launch_transform(ctx->sys_d, sys, S.n_beads, ctx->nm + S.nm_off, ctx->q + S.q_off, S.n_dof, 1, ctx->stream,
+                     &ctx->launches);
+    launch_transform(ctx->sys_d, sys, S.n_beads, ctx->nm + S.nm_off, ctx->p + S.q_off, S.n_dof, 1, ctx->stream,
+                     &ctx->launches);
+    launch_nm_energy(ctx->sys_d, sys, S.n_beads, S.n_dof, ctx->q, ctx->p, ctx->mass, ctx->modes, ctx->red_out,
+                     ctx->stream, &ctx->launches);
+    launch_transform(ctx->sys_d, sys, S.n_beads, ctx->nm + S.nm_off, ctx->q + S.q_off, S.n_dof, 0, ctx->stream,
+                     &ctx->launches);
+    launch_transform(ctx->sys_d, sys, S.n_beads, ctx->nm + S.nm_off, ctx->p + S.q_off, S.n_dof, 0, ctx->stream,
+                     &ctx->launches);
+    double r[2];
+    CK(down(ctx, r, ctx->red_out, 2 * sizeof(double)));
+    CK(down(ctx, q, ctx->q + S.q_off, sizeof(double) * nt));
+    CK(down(ctx, p, ctx->p + S.q_off, sizeof(double) * nt));
+    CKS(sync_status(ctx));
+    *out = energy + r[0] + r[1];
+    return QTG_OK;
+}
+
+static qtg_status upload_dynamic(qtg_ctx *ctx, int sys, const double *q, const double *p, const double *mass,
+                                 const double *f, const double *fphys, const double *charge, const int *point,
+                                 const int *list, const double *disp) {
+    const SysDev &S = ctx->sys_h[sys];
+    const size_t nt = (size_t)S.n_beads * S.n_dof;
+    if (charge) CKS(upload_charges(ctx, sys, charge));
+    if (mass) CK(up(ctx, ctx->mass + S.mass_off, mass, sizeof(double) * S.n_dof));
+    CK(up(ctx, ctx->q + S.q_off, q, sizeof(double) * nt));
+    CK(up(ctx, ctx->p + S.q_off, p, sizeof(double) * nt));
+    CK(up(ctx, ctx->f + S.q_off, f, sizeof(double) * nt));
+    CK(up(ctx, ctx->fphys + S.q_off, fphys ? fphys : f, sizeof(double) * nt));
+    CK(up(ctx, ctx->disp + S.d_off, disp, sizeof(double) * S.n_beads * 3 * S.n_mols));
+    return upload_lists(ctx, sys, point, list, 0, S.n_beads);
+}
+
+static qtg_status download_dynamic(qtg_ctx *ctx, int sys, double *q, double *p, double *f, double *fphys, int *point,
+                                   int *list, double *disp) {
+    const SysDev &S = ctx->sys_h[sys];
+    const size_t nt = (size_t)S.n_beads * S.n_dof;
+    CK(down(ctx, q, ctx->q + S.q_off, sizeof(double) * nt));
+    CK(down(ctx, p, ctx->p + S.q_off, sizeof(double) * nt));
+    CK(down(ctx, f, ctx->f + S.q_off, sizeof(double) * nt));
+    if (fphys) CK(down(ctx, fphys, ctx->fphys + S.q_off, sizeof(double) * nt));
+    CK(down(ctx, disp, ctx->disp + S.d_off, sizeof(double) * S.n_beads * 3 * S.n_mols));
+    CK(down(ctx, point, ctx->point + S.pt_off, sizeof(int) * S.n_beads * S.n_mols));
+    CK(down(ctx, list, ctx->list + S.ls_off, sizeof(int) * (size_t)S.n_beads * S.list_size));
+    return QTG_OK;
+}
+
+qtg_status qtg_update_class(qtg_ctx *ctx, int sys, double *q, double *p, const double *mass, double *f,
+                            const double *charge, int *point, int *list, double *disp, double *energy) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    if (S.n_beads != 1 || !q || !p || !f || !point || !list || !disp) return fail(ctx, QTG_ERR_ARG, "bad argument");
+    CKS(upload_dynamic(ctx, sys, q, p, mass, f, nullptr, charge, point, list, disp));
+    CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
+    launch_ring(ring_args(ctx, sys, RF_KICK | RF_VV | RF_DISP), ctx->stream, &ctx->launches);
+    launch_skin_rebuild(list_args(ctx, S.job_base, 1, 0), ctx->stream, &ctx->launches);
+    launch_eval(ctx, eval_args(ctx, ctx->base.d + S.job_base, 1, ctx->q, ctx->fphys, 0, 0));
+    // P = 1: the propagating force is the physical force
+    CK(cudaMemcpyAsync(ctx->f + S.q_off, ctx->fphys + S.q_off, sizeof(double) * S.n_dof, cudaMemcpyDeviceToDevice,
+                       ctx->stream));
+    RingArgs e = ring_args(ctx, sys, 0);
+    e.kick = 1;
+    launch_end_step(e, ctx->stream, &ctx->launches);
+    CKS(download_dynamic(ctx, sys, q, p, f, nullptr, point, list, disp));
+    double en = 0.0;
+    CK(down(ctx, &en, ctx->energy + S.job_base, sizeof(double)));
+    CKS(sync_status(ctx));
+    CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
+    if (energy) *energy = en;
+    return sync_status(ctx);
+}
+
+qtg_status qtg_update_pimd(qtg_ctx *ctx, int sys, double *q, double *p, const double *mass, double *f, double *fphys,
+                           const double *charge, int *point, int *list, double *disp, int is_nvt, const double *noise,
+                           double *heat, double *pot, double *energy) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    if (!q || !p || !f || !fphys || !point || !list || !disp) return fail(ctx, QTG_ERR_ARG, "bad argument");
+    CKS(upload_dynamic(ctx, sys, q, p, mass, f, fphys, charge, point, list, disp));
+    if (noise) CK(up(ctx, ctx->noise, noise, sizeof(double) * (2 + (size_t)(S.n_beads - 1) * S.n_dof)));
+    const double h0 = heat ? *heat : 0.0;
+    CK(up(ctx, &ctx->run[sys].heat, &h0, sizeof(double)));
+    CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
+    if (is_nvt) {
+        // centroid kinetic energy after the opening kick, then the centroid draw
+        RingArgs e = ring_args(ctx, sys, 0);
+        e.kick = 0;
+        launch_end_step(e, ctx->stream, &ctx->launches);
+        FinalizeArgs fa = fin_args(ctx, sys, 0, 1);
+        fa.pile_g = 1;
+        fa.noise = noise ? ctx->noise : nullptr;
+        launch_finalize(fa, ctx->stream, &ctx->launches);
+    }
+    RingArgs r = ring_args(ctx, sys, RF_KICK | RF_FWD | RF_CAYLEY | RF_BACK | RF_DISP | (is_nvt ? RF_THERMO : 0));
+    r.noise = noise ? ctx->noise : nullptr;
+    r.pile_g = 1;
+    launch_ring(r, ctx->stream, &ctx->launches);
+    launch_skin_rebuild(list_args(ctx, S.job_base, S.n_beads, 0), ctx->stream, &ctx->launches);
+    CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
+    enqueue_forces(ctx, sys, false);
+    RingArgs e = ring_args(ctx, sys, 0);
+    e.kick = 1;
+    launch_end_step(e, ctx->stream, &ctx->launches);
+    CKS(download_dynamic(ctx, sys, q, p, f, fphys, point, list, disp));
+    double h = 0.0;
+    CK(down(ctx, &h, &ctx->run[sys].heat, sizeof(double)));
+    double vs, ve, extra;
+    CKS(read_energies(ctx, sys, &vs, &ve, &extra));
+    if (heat) *heat = h;
+    if (S.propagator == QTG_SUZUKI_CHIN) {
+        if (pot) *pot = 2.0 * ve / S.n_beads;
+        if (energy) *energy = (2.0 * ve + 4.0 * (vs - ve) + extra) / 3.0;
+    } else {
+        if (pot) *pot = vs / S.n_beads;
+        if (energy) *energy = vs;
+    }
+    return QTG_OK;
+}
+
+// ---- tier 2 ------------------------------------------------------------------------
+
+qtg_status qtg_set_state(qtg_ctx *ctx, int sys, const double *q, const double *p) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    if (!q) return fail(ctx, QTG_ERR_ARG, "null positions");
+    const size_t nt = (size_t)S.n_beads * S.n_dof;
+    CK(up(ctx, ctx->q + S.q_off, q, sizeof(double) * nt));
+    if (p) CK(up(ctx, ctx->p + S.q_off, p, sizeof(double) * nt));
+    else CK(cudaMemsetAsync(ctx->p + S.q_off, 0, sizeof(double) * nt, ctx->stream));
+    ctx->forces_ready = false;
+    return sync_status(ctx);
+}
+
+qtg_status qtg_get_state(qtg_ctx *ctx, int sys, double *q, double *p, double *f, double *fphys, double *disp) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    const size_t nt = (size_t)S.n_beads * S.n_dof;
+    if (q) CK(down(ctx, q, ctx->q + S.q_off, sizeof(double) * nt));
+    if (p) CK(down(ctx, p, ctx->p + S.q_off, sizeof(double) * nt));
+    if (f) CK(down(ctx, f, ctx->f + S.q_off, sizeof(double) * nt));
+    if (fphys) CK(down(ctx, fphys, ctx->fphys + S.q_off, sizeof(double) * nt));
+    if (disp) CK(down(ctx, disp, ctx->disp + S.d_off, sizeof(double) * S.n_beads * 3 * S.n_mols));
+    return sync_status(ctx);
+}
+
+qtg_status qtg_init_forces(qtg_ctx *ctx) {
+    if (!ctx) return QTG_ERR_ARG;
+    CK(cudaMemsetAsync(ctx->disp, 0, sizeof(double) * ctx->total_disp, ctx->stream));
+    CK(cudaMemsetAsync(ctx->acc, 0, sizeof(SysAcc) * ctx->n_sys, ctx->stream));
+    launch_skin_rebuild(list_args(ctx, 0, (int)ctx->base.h.size(), 1), ctx->stream, &ctx->launches);
+    CK(cudaMemsetAsync(ctx->acc, 0, sizeof(SysAcc) * ctx->n_sys, ctx->stream));
+    enqueue_forces(ctx, -1, false);
+    RingArgs e = ring_args(ctx, -1, 0);
+    e.kick = 0;
+    launch_end_step(e, ctx->stream, &ctx->launches);
+    launch_finalize(fin_args(ctx, -1, 1, 1), ctx->stream, &ctx->launches);
+    CKS(sync_status(ctx));
+    ctx->forces_ready = true;
+    return QTG_OK;
+}
+
+qtg_status qtg_run_steps(qtg_ctx *ctx, int n_steps, int is_nvt) {
+    if (!ctx || n_steps < 0) return QTG_ERR_ARG;
+    if (!ctx->forces_ready) return fail(ctx, QTG_ERR_STATE, "qtg_init_forces must precede qtg_run_steps");
+    const int g = is_nvt ? 1 : 0;
+    if (!ctx->graph[g]) {
+        cudaGraph_t graph;
+        unsigned long long before = ctx->launches;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_step(ctx, -1, is_nvt, 0, false);
+        cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+        if (e != cudaSuccess) return fail(ctx, QTG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        ctx->graph_kernels[g] = ctx->launches - before;
+        ctx->launches = before;
+        e = cudaGraphInstantiate(&ctx->graph[g], graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(ctx, QTG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+    for (int i = 0; i < n_steps; ++i) {
+        CK(cudaGraphLaunch(ctx->graph[g], ctx->stream));
+        ctx->launches += ctx->graph_kernels[g];
+    }
+    return QTG_OK;
+}
+
+qtg_status qtg_sync(qtg_ctx *ctx) {
+    if (!ctx) return QTG_ERR_ARG;
+    return sync_status(ctx);
+}
+
+qtg_status qtg_get_estimators(qtg_ctx *ctx, int sys, double *out, int max_records, int *n_records) {
+    CKS(check_sys(ctx, sys));
+    if (!out || max_records < 0 || !n_records) return fail(ctx, QTG_ERR_ARG, "bad argument");
+    unsigned long long nrec = 0;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(&nrec, ctx->records, sizeof(nrec), cudaMemcpyDeviceToHost));
+    const unsigned long long avail = std::min<unsigned long long>(nrec, (unsigned long long)ctx->max_records);
+    const unsigned long long n = std::min<unsigned long long>(avail, (unsigned long long)max_records);
+    std::vector<double> all((size_t)ctx->max_records * ctx->n_sys * 8);
+    CK(cudaMemcpy(all.data(), ctx->est, sizeof(double) * all.size(), cudaMemcpyDeviceToHost));
+    for (unsigned long long i = 0; i < n; ++i) {
+        const unsigned long long r = nrec - n + i;
+        const double *src = all.data() + ((size_t)(r % ctx->max_records) * ctx->n_sys + sys) * 8;
+        memcpy(out + i * 8, src, 8 * sizeof(double));
+    }
+    *n_records = (int)n;
+    return QTG_OK;
+}
+
+qtg_status qtg_time_kernel(qtg_ctx *ctx, const char *name, int iters, double *avg_ms) {
+    if (!ctx || !name || iters <= 0 || !avg_ms) return QTG_ERR_ARG;
+    const std::string n(name);
+    const bool ewald = n == "prep" || n == "real" || n == "ksk" || n == "kforce" || n == "combine" || n == "lj";
+    if (!ewald && n != "rebuild" && n != "ring" && n != "end_step") return fail(ctx, QTG_ERR_ARG, "unknown kernel name");
+    const int nj = (int)ctx->base.h.size();
+    const EvalArgs a = eval_args(ctx, ctx->base.d, nj, ctx->q, ctx->fphys, 0, 0);
+    launch_eval(ctx, a);  // fills every scratch array the single kernels read
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    RingArgs r = ring_args(ctx, -1, RF_KICK | RF_FWD | RF_CAYLEY | RF_BACK | RF_DISP);
+    RingArgs es = ring_args(ctx, -1, 0);
+    es.kick = 0;
+    for (int pass = 0; pass < 2; ++pass) {  // pass 0 warms up
+        CK(cudaEventRecord(e0, ctx->stream));
+        for (int i = 0; i < (pass ? iters : 1); ++i) {
+            if (ewald) launch_ewald_kernel(a, ctx->mixed, name, ctx->stream);
+            else if (n == "rebuild") launch_skin_rebuild(list_args(ctx, 0, nj, 1), ctx->stream, nullptr);
+            else if (n == "ring") launch_ring(r, ctx->stream, nullptr);
+            else launch_end_step(es, ctx->stream, nullptr);
+        }
+        CK(cudaEventRecord(e1, ctx->stream));
+        CK(cudaEventSynchronize(e1));
+    }
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CK(cudaMemsetAsync(ctx->acc, 0, sizeof(SysAcc) * ctx->n_sys, ctx->stream));
+    *avg_ms = (double)ms / iters;
+    ctx->forces_ready = false;
+    return sync_status(ctx);
+}
+
+qtg_status qtg_fp32_peak(double *tflops) {
+    if (!tflops) return QTG_ERR_ARG;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return QTG_ERR_NODEVICE;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return QTG_ERR_NODEVICE;
+    float *out = nullptr;
+    if (cudaMalloc(&out, sizeof(float)) != cudaSuccess) return QTG_ERR_CUDA;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = sms * 8, iters = 1 << 16;
+    launch_fp32_probe(out, blocks, 1024, nullptr);
+    cudaEventRecord(e0, nullptr);
+    launch_fp32_probe(out, blocks, iters, nullptr);
+    cudaEventRecord(e1, nullptr);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (e != cudaSuccess || ms <= 0.f) return QTG_ERR_CUDA;
+    const double flops = 2.0 * 8.0 * (double)iters * blocks * 256.0;
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    return QTG_OK;
+}
+
+qtg_status qtg_reset_estimators(qtg_ctx *ctx) {
+    if (!ctx) return QTG_ERR_ARG;
+    CK(cudaMemsetAsync(ctx->records, 0, sizeof(unsigned long long), ctx->stream));
+    return sync_status(ctx);
+}
+
+}  // extern "C"

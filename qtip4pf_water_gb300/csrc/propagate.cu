@@ -1,0 +1,483 @@
+// Ring-polymer propagation on GB300 (replaces update.cpp:78-137 / :271-401,
+// fourier.cpp:12-69, thermostat.cpp:12-133 and the reductions of
+// path_integrals.cpp:29-81). All arithmetic here is FP64.
+//
+// A block owns cols_per_block degree-of-freedom columns of one system and all
+// P beads of each: thread (k, c) holds bead / normal mode k of column c. The
+// orthonormal bead <-> normal-mode matrix (fourier.cpp's FFTW halfcomplex order
+// and scaling) is staged in shared memory and applied as a batched P x P
+// matrix product on the column tile, so the B kick, forward transform, the two
+// sqrt-Cayley half steps, the O step and the backward transform of a step are
+// one kernel with one read and one write of q and p.
+#include <math.h>
+
+#include "qtg_internal.h"
+
+namespace qtg {
+
+namespace {
+
+__device__ __forceinline__ void philox_key(const SysDev &S, int sys, uint32_t tag, uint32_t *k0,
+                                           uint32_t *k1) {
+    *k0 = (uint32_t)S.seed ^ ((uint32_t)sys * 0x85EBCA6Bu);
+    *k1 = (uint32_t)(S.seed >> 32) ^ (tag * 0xC2B2AE35u);
+}
+
+// Standard normal from one Philox block, Box-Muller in FP32 (thermostat noise).
+__device__ __forceinline__ double normal_f32(const Philox4 &r) {
+    float u1 = ((float)(r.v[0] >> 8) + 0.5f) * (1.0f / 16777216.0f);
+    float u2 = ((float)(r.v[1] >> 8) + 0.5f) * (1.0f / 16777216.0f);
+    float s, c;
+    sincospif(2.0f * u2, &s, &c);
+    return (double)(sqrtf(-2.0f * logf(u1)) * c);
+}
+
+__global__ void __launch_bounds__(256) k_ring(RingArgs a) {
+    const ColWork W = a.work[blockIdx.x];
+    const SysDev &S = a.sys[W.sys];
+    const int P = S.n_beads, C = S.cols_per_block;
+    const int k = threadIdx.x / C, c = threadIdx.x - k * C;
+    const bool act = (k < P) && (c < W.ncols);
+    const int col = W.col0 + c;
+    const int flags = a.flags;
+    extern __shared__ double sh[];
+    double *Cm = sh;
+    double *Xq = Cm + P * P;
+    double *Xp = Xq + P * C;
+    __shared__ double red[8];
+    if (flags & (RF_FWD | RF_BACK))
+        for (int t = threadIdx.x; t < P * P; t += blockDim.x) Cm[t] = a.nm[S.nm_off + t];
+    const long long at = S.q_off + (long long)k * S.n_dof + col;
+    double qb = 0.0, pb = 0.0;
+    const double m = act ? a.mass[S.mass_off + col] : 1.0;
+    if (act) {
+        qb = a.q[at];
+        pb = a.p[at];
+        if (flags & RF_KICK) pb += S.halfdt * a.f[at];
+    }
+    const double q_old = qb;
+    double yq = qb, yp = pb;
+    if (flags & RF_FWD) {
+        if (k < P) {
+            Xq[k * C + c] = qb;
+            Xp[k * C + c] = pb;
+        }
+        __syncthreads();
+        if (act) {
+            double sq = 0.0, sp = 0.0;
+            const double *row = Cm + k * P;
+            for (int b = 0; b < P; ++b) {
+                sq += row[b] * Xq[b * C + c];
+                sp += row[b] * Xp[b * C + c];
+            }
+            yq = sq;
+            yp = sp;
+        }
+        __syncthreads();
+    }
+    double heat = 0.0;
+    if (act) {
+        if (flags & RF_VV) {
+            // update.cpp:87-91
+            const double dq = yp * S.dt / m;
+            if ((flags & RF_DISP) && (col % 9) < 3) a.disp[S.d_off + 3 * (col / 9) + (col % 9)] += dq;
+            yq += dq;
+        }
+        const ModeCoef mc = a.modes[S.mode_off + k];
+        if (flags & RF_CAYLEY) {
+            // update.cpp:301-320
+            double t = S.halfdt * yp / m + yq;
+            t *= mc.scale;
+            yp = yp - S.halfdt * mc.w2 * yq * m;
+            yp *= mc.scale;
+            yq = t;
+        }
+        if ((flags & RF_THERMO) && (S.thermostat != 0 || a.pile_g)) {
+            const double before = 0.5 * yp * yp / m;
+            if (k == 0 && (S.thermostat == 1 || a.pile_g)) {
+                yp *= a.run[W.sys].alpha;  // PILE-G centroid (thermostat.cpp:88-104)
+            } else {
+                double c1 = mc.c1, c2 = mc.c2;
+                if (k == 0) {  // PILE-L centroid
+                    c1 = S.c1_centroid;
+                    c2 = sqrt(1.0 - c1 * c1);
+                }
+                double xi;
+                if (a.noise && k > 0) {
+                    xi = a.noise[2 + (size_t)(k - 1) * S.n_dof + col];
+                } else {
+                    uint32_t k0, k1;
+                    philox_key(S, W.sys, RNG_MODES, &k0, &k1);
+                    const unsigned long long st = *a.step;
+                    xi = normal_f32(philox4x32_10((uint32_t)col, (uint32_t)k, (uint32_t)st,
+                                                  (uint32_t)(st >> 32), k0, k1));
+                }
+                yp = c1 * yp + sqrt(m / S.beta_n) * c2 * xi;  // thermostat.cpp:131-136
+            }
+            heat = 0.5 * yp * yp / m - before;
+        }
+        if (flags & RF_CAYLEY) {
+            double t = S.halfdt * yp / m + yq;
+            t *= mc.scale;
+            yp = yp - S.halfdt * mc.w2 * yq * m;
+            yp *= mc.scale;
+            yq = t;
+        }
+    }
+    double qn = yq, pn = yp;
+    if (flags & RF_BACK) {
+        if (k < P) {
+            Xq[k * C + c] = yq;
+            Xp[k * C + c] = yp;
+        }
+        __syncthreads();
+        if (act) {
+            double sq = 0.0, sp = 0.0;
+            for (int j = 0; j < P; ++j) {
+                const double cj = Cm[j * P + k];
+                sq += cj * Xq[j * C + c];
+                sp += cj * Xp[j * C + c];
+            }
+            qn = sq;
+            pn = sp;
+        }
+    }
+    if (act) {
+        a.q[at] = qn;
+        a.p[at] = pn;
+        if ((flags & RF_DISP) && !(flags & RF_VV) && (col % 9) < 3)
+            a.disp[S.d_off + (long long)k * 3 * S.n_mols + 3 * (col / 9) + (col % 9)] += qn - q_old;
+    }
+    if (flags & RF_THERMO) {
+        double t = block_sum(heat, red);
+        if (threadIdx.x == 0) atomicAdd(&a.run[W.sys].heat, t);
+    }
+}
+
+// Closing kick and the per-step estimator partial sums (bead space).
+__global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
+    const ColWork W = a.work[blockIdx.x];
+    const SysDev &S = a.sys[W.sys];
+    const int P = S.n_beads, C = S.cols_per_block;
+    const int b = threadIdx.x / C, c = threadIdx.x - b * C;
+    const bool act = (b < P) && (c < W.ncols);
+    const int col = W.col0 + c;
+    extern __shared__ double sh[];
+    double *Xq = sh;
+    double *Xp = Xq + P * C;
+    __shared__ double red[8];
+    const long long at = S.q_off + (long long)b * S.n_dof + col;
+    double qb = 0.0, pb = 0.0, fb = 0.0, fpb = 0.0;
+    const double m = act ? a.mass[S.mass_off + col] : 1.0;
+    if (act) {
+        qb = a.q[at];
+        pb = a.p[at];
+        fb = a.f[at];
+        fpb = a.fphys[at];
+        if (a.kick) {
+            pb += S.halfdt * fb;  // update.cpp:391-397
+            a.p[at] = pb;
+        }
+        Xq[b * C + c] = qb;
+        Xp[b * C + c] = pb + S.halfdt * fb;
+    }
+    __syncthreads();
+    double kin = 0.0, spring = 0.0, tq = 0.0, k0 = 0.0;
+    if (act) {
+        kin = 0.5 * pb * pb / m;
+        const double qn = Xq[((b + 1) % P) * C + c];
+        const double dq = qb - qn;
+        spring = 0.5 * m * S.omega_psq * dq * dq;
+        const int all = a.kcv_all_beads < 0 ? (S.propagator == 1) : a.kcv_all_beads;
+        if (all || (b % 2 == 0)) {
+            double qc = 0.0;
+            for (int j = 0; j < P; ++j) qc += Xq[j * C + c];
+            qc /= (double)P;
+            tq = -(qb - qc) * fpb;
+        }
+        if (b == 0) {
+            double s = 0.0;
+            for (int j = 0; j < P; ++j) s += Xp[j * C + c];
+            const double p0 = sqrt(1.0 / P) * s;
+            k0 = 0.5 * p0 * p0 / m;
+        }
+    }
+    double t0 = block_sum(kin, red);
+    double t1 = block_sum(spring, red);
+    double t2 = block_sum(tq, red);
+    double t3 = block_sum(k0, red);
+    if (threadIdx.x == 0) {
+        SysAcc *ac = &a.acc[W.sys];
+        atomicAdd(&ac->kin, t0);
+        atomicAdd(&ac->spring, t1);
+        atomicAdd(&ac->kcv_tq, t2);
+        atomicAdd(&ac->k0, t3);
+    }
+}
+
+// Centroid normal-mode kinetic energy of normal-mode momenta (row 0 of p).
+__global__ void k_centroid_ke(RingArgs a) {
+    const ColWork W = a.work[blockIdx.x];
+    const SysDev &S = a.sys[W.sys];
+    __shared__ double red[8];
+    double e = 0.0;
+    for (int c = threadIdx.x; c < W.ncols; c += blockDim.x) {
+        const int col = W.col0 + c;
+        const double pv = a.p[S.q_off + col];
+        e += 0.5 * pv * pv / a.mass[S.mass_off + col];
+    }
+    double t = block_sum(e, red);
+    if (threadIdx.x == 0) atomicAdd(&a.acc[W.sys].k0, t);
+}
+
+// Gamma(shape) by Marsaglia & Tsang, "A simple method for generating gamma
+// variables" (ACM TOMS 26, 2000), for shape >= 1, with a bounded loop.
+__device__ double gamma_mt(double shape, const SysDev &S, int sys, unsigned long long st, bool *ok) {
+    const double d = shape - 1.0 / 3.0, cc = 1.0 / sqrt(9.0 * d);
+    uint32_t k0, k1;
+    philox_key(S, sys, RNG_GAMMA, &k0, &k1);
+    for (uint32_t it = 0; it < 64; ++it) {
+        const double x = normal2(philox4x32_10(2 * it, 0u, (uint32_t)st, (uint32_t)(st >> 32), k0, k1)).x;
+        double v = 1.0 + cc * x;
+        if (v <= 0.0) continue;
+        v = v * v * v;
+        const Philox4 r = philox4x32_10(2 * it + 1, 0u, (uint32_t)st, (uint32_t)(st >> 32), k0, k1);
+        const double u = u01_from(r.v[0], r.v[1]);
+        if (u < 1.0 - 0.0331 * x * x * x * x) return d * v;
+        if (log(u) < 0.5 * x * x + d * (1.0 - v + log(v))) return d * v;
+    }
+    *ok = false;
+    return shape;
+}
+
+__global__ void k_finalize(FinalizeArgs a) {
+    const unsigned long long st = *a.step;
+    const unsigned long long rec = *a.records;
+    for (int s = a.sys_begin + threadIdx.x; s < a.sys_end; s += blockDim.x) {
+        const SysDev &S = a.sys[s];
+        SysAcc *ac = &a.acc[s];
+        SysRun *run = &a.run[s];
+        const int P = S.n_beads;
+        if (a.record) {
+            double vsum = 0.0, veven = 0.0;
+            for (int b = 0; b < P; ++b) {
+                const double e = a.energy[S.job_base + b];
+                vsum += e;
+                if (b % 2 == 0) veven += e;
+            }
+            double vtot, pot, kcv;
+            const double half_nd_beta = 0.5 * S.n_dof / S.beta;
+            if (S.propagator == 0) {  // Suzuki-Chin (forces.cpp:724-781, path_integrals.cpp:29-48)
+                vtot = (2.0 * veven + 4.0 * (vsum - veven) + ac->sc_extra) / 3.0;
+                pot = 2.0 * veven / P;
+                kcv = half_nd_beta + ac->kcv_tq / P;
+            } else {
+                vtot = vsum;
+                pot = vsum / P;
+                kcv = half_nd_beta + ac->kcv_tq / (2.0 * P);
+            }
+            const double cons = vtot + ac->kin + ac->spring + run->heat;
+            double *o = a.est + ((size_t)(rec % (unsigned long long)a.max_records) * a.n_sys + s) * 8;
+            o[0] = pot;
+            o[1] = kcv;
+            o[2] = cons;
+            o[3] = run->heat;
+            o[4] = ac->kin;
+            o[5] = vtot;
+            o[6] = ac->rebuilds;
+            o[7] = (double)st;
+            if (!isfinite(cons) || !isfinite(vtot)) atomicOr(a.status, (unsigned)ST_NONFINITE);
+        }
+        if (a.draw_alpha && (S.thermostat == 1 || a.pile_g)) {
+            double R, g2;
+            if (a.noise && s == 0) {
+                R = a.noise[0];
+                g2 = a.noise[1];
+            } else {
+                uint32_t k0, k1;
+                philox_key(S, s, RNG_CENTROID, &k0, &k1);
+                R = normal2(philox4x32_10(0u, 0u, (uint32_t)st, (uint32_t)(st >> 32), k0, k1)).x;
+                // g2 ~ chi^2 with (n_dof - 1) degrees of freedom: both branches of
+                // thermostat.cpp:102-110 draw exactly this distribution
+                bool ok = true;
+                g2 = 2.0 * gamma_mt(0.5 * (S.n_dof - 1), S, s, st, &ok);
+                if (!ok) atomicOr(a.status, (unsigned)ST_GAMMA_LIMIT);
+            }
+            run->alpha = sqrt((R * R + g2) / (2.0 * S.beta_n * ac->k0));
+        }
+        ac->kin = ac->spring = ac->kcv_tq = ac->k0 = ac->sc_extra = ac->rebuilds = 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (a.record) *a.records = rec + 1;
+        *a.step = st + 1;
+    }
+}
+
+// ---- Suzuki-Chin assembly (forces.cpp:724-775) -----------------------------------
+__global__ void __launch_bounds__(256) k_sc_prepare(ScArgs a) {
+    const int sid = a.job_sys[blockIdx.x], b = a.job_bead[blockIdx.x];
+    const SysDev &S = a.sys[sid];
+    const int nd = S.n_dof, P = S.n_beads;
+    const double *fp = a.fphys + S.q_off + (size_t)b * nd;
+    const double *mass = a.mass + S.mass_off;
+    __shared__ double red[8];
+    __shared__ double scl_sh;
+    double fsq = 0.0, dl = 0.0;
+    for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+        const double f = fp[i], m = mass[i];
+        fsq += f * f / m;
+        const double t = f / m;
+        dl += t * t;
+    }
+    fsq = block_sum(fsq, red);
+    dl = block_sum(dl, red);
+    if (threadIdx.x == 0) {
+        double delta = dl / (S.n_sites * P);
+        delta = 1.0 / sqrt(delta);
+        const double scl = S.eps_sc * delta;
+        scl_sh = scl;
+        a.sc_scale[S.job_base + b] = scl;
+        atomicAdd(&a.acc[sid].sc_extra, fsq / (3.0 * S.omega_psq));
+    }
+    __syncthreads();
+    const double scl = scl_sh;
+    const double *qb = a.q + S.q_off + (size_t)b * nd;
+    double *qp = a.qdisp + S.q_off + (size_t)b * nd;
+    double *qm = a.qdisp + S.q_off + (size_t)(b - 1) * nd;
+    for (int i = threadIdx.x; i < nd; i += blockDim.x) {
+        const double dq = scl * fp[i] / mass[i];
+        qp[i] = qb[i] + dq;
+        qm[i] = qb[i] - dq;
+        if (a.mixed) a.dirv[S.q_off + (size_t)b * nd + i] = fp[i] / mass[i];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_sc_finish(ScArgs a) {
+    const int sid = a.job_sys[blockIdx.y], b = a.job_bead[blockIdx.y];
+    const SysDev &S = a.sys[sid];
+    const int nd = S.n_dof;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nd) return;
+    const size_t at = S.q_off + (size_t)b * nd + i;
+    const double fp = a.fphys[at];
+    double f;
+    if (S.propagator == 1 && !a.force_sc) {
+        f = fp;  // second-order assembly: every bead weight 1
+    } else if (b % 2 == 0) {
+        f = 2.0 * fp / 3.0;
+    } else {
+        const double scl = a.sc_scale[S.job_base + b];
+        const double fscale = 1.0 / (9.0 * S.omega_psq * scl);
+        const size_t am = at - nd;
+        double diff;
+        if (a.mixed) diff = 2.0 * scl * a.fdisp[at] + (a.fsr[at] - a.fsr[am]);
+        else diff = a.fdisp[at] - a.fdisp[am];
+        f = 4.0 * fp / 3.0;
+        f -= fscale * diff;
+    }
+    a.f[at] = f;
+}
+
+// Plain bead <-> normal-mode transform of an arbitrary-length array (tier-1 ftransform).
+__global__ void __launch_bounds__(256) k_transform(int P, int C, const double *nm, double *x, int length,
+                                                   int forwards) {
+    const int k = threadIdx.x / C, c = threadIdx.x - k * C;
+    const int col = blockIdx.x * C + c;
+    const bool act = (k < P) && (col < length);
+    extern __shared__ double sh[];
+    double *Cm = sh;
+    double *X = Cm + P * P;
+    for (int t = threadIdx.x; t < P * P; t += blockDim.x) Cm[t] = nm[t];
+    if (k < P) X[k * C + c] = act ? x[(size_t)k * length + col] : 0.0;
+    __syncthreads();
+    if (!act) return;
+    double s = 0.0;
+    if (forwards)
+        for (int b = 0; b < P; ++b) s += Cm[k * P + b] * X[b * C + c];
+    else
+        for (int j = 0; j < P; ++j) s += Cm[j * P + k] * X[j * C + c];
+    x[(size_t)k * length + col] = s;
+}
+
+__global__ void __launch_bounds__(256) k_nm_energy(const SysDev *sys, int sysi, int P, int n_dof,
+                                                   const double *q, const double *p, const double *mass,
+                                                   const ModeCoef *modes, double *out) {
+    const SysDev &S = sys[sysi];
+    __shared__ double red[8];
+    double kin = 0.0, spr = 0.0;
+    const size_t total = (size_t)P * n_dof;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(t / n_dof), j = (int)(t - (size_t)k * n_dof);
+        const double m = mass[S.mass_off + j], pv = p[S.q_off + t], qv = q[S.q_off + t];
+        kin += 0.5 * pv * pv / m;
+        spr += 0.5 * modes[S.mode_off + k].w2 * m * qv * qv;
+    }
+    kin = block_sum(kin, red);
+    spr = block_sum(spr, red);
+    if (threadIdx.x == 0) {
+        atomicAdd(&out[0], kin);
+        atomicAdd(&out[1], spr);
+    }
+}
+
+}  // namespace
+
+void init_propagate_kernel_attributes() {
+    cudaFuncSetAttribute(k_ring, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+void launch_nm_energy(const SysDev *sys, int sysi, int P, int n_dof, const double *q, const double *p,
+                      const double *mass, const ModeCoef *modes, double *out, cudaStream_t s,
+                      unsigned long long *n) {
+    k_nm_energy<<<64, 256, 0, s>>>(sys, sysi, P, n_dof, q, p, mass, modes, out);
+    if (n) ++*n;
+}
+
+void launch_ring(const RingArgs &a, cudaStream_t s, unsigned long long *n) {
+    if (a.n_work <= 0) return;
+    // shared memory: P^2 + 2 P C doubles, with P C <= 256
+    size_t smem = (size_t)(a.max_p * a.max_p + 2 * 256) * sizeof(double);
+    k_ring<<<a.n_work, 256, smem, s>>>(a);
+    if (n) ++*n;
+}
+
+void launch_end_step(const RingArgs &a, cudaStream_t s, unsigned long long *n) {
+    if (a.n_work <= 0) return;
+    k_end_step<<<a.n_work, 256, 2 * 256 * sizeof(double), s>>>(a);
+    if (n) ++*n;
+}
+
+void launch_centroid_ke(const RingArgs &a, cudaStream_t s, unsigned long long *n) {
+    if (a.n_work <= 0) return;
+    k_centroid_ke<<<a.n_work, 256, 0, s>>>(a);
+    if (n) ++*n;
+}
+
+void launch_finalize(const FinalizeArgs &a, cudaStream_t s, unsigned long long *n) {
+    k_finalize<<<1, 64, 0, s>>>(a);
+    if (n) ++*n;
+}
+
+void launch_sc_prepare(const ScArgs &a, cudaStream_t s, unsigned long long *n) {
+    if (a.n_jobs <= 0) return;
+    k_sc_prepare<<<a.n_jobs, 256, 0, s>>>(a);
+    if (n) ++*n;
+}
+
+void launch_sc_finish(const ScArgs &a, cudaStream_t s, unsigned long long *n) {
+    if (a.n_jobs <= 0) return;
+    k_sc_finish<<<dim3((a.max_dof + 255) / 256, a.n_jobs), 256, 0, s>>>(a);
+    if (n) ++*n;
+}
+
+void launch_transform(const SysDev *, int, int P, const double *nm_sys, double *x, int length, int forwards,
+                      cudaStream_t s, unsigned long long *n) {
+    const int C = P >= 256 ? 1 : 256 / P;
+    const size_t smem = (size_t)(P * P + P * C) * sizeof(double);
+    k_transform<<<(length + C - 1) / C, 256, smem, s>>>(P, C, nm_sys, x, length, forwards);
+    if (n) ++*n;
+}
+
+}  // namespace qtg

@@ -1,0 +1,333 @@
+// Internal definitions shared by the CUDA translation units of libqtipgpu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace qtg {
+
+// The reference's truncated pi (qtip4pfparams.h:45). It enters theta_eq,
+// sqrt(pi), 2 pi / L and sin(k pi / P), so FP64 parity needs the same value.
+constexpr double PI_REF = 3.14159265359;
+
+// qTIP4P/F parameters in atomic units, derived on the host exactly as
+// qtip4pfparams.h:41-133 derives them (same constants, same operation order).
+struct Consts {
+    double angs2bohr, fs2au, K2au, mo, mh;
+    double r_cut, r_cut_sq, r_skin, r_skin_sq;
+    double gamma_vs, epslj, sigmalj6, sigmalj12, e_cut;
+    double roheq, ar2, ar3, ar4fac, Dr, theta_eq, ktheta, qo, qh;
+};
+
+// Per-system constants (one per replica), resident in device memory.
+struct SysDev {
+    int n_mols, n_beads, n_sites, n_dof, list_size, k_max, n_kvec, kvec_off;
+    int propagator, thermostat, job_base, cols_per_block;
+    long long nm_off;   // doubles: P x P bead->normal-mode matrix C (y = C x)
+    long long mode_off; // ModeCoef entries: P per system
+    long long q_off;    // doubles: system block [P][9N] in q/p/f/fphys/aux arrays
+    long long d_off;    // doubles: [P][3N] block in disp
+    long long pt_off;   // ints: [P][N] block in point
+    long long ls_off;   // ints: [P][list_size] block in list
+    long long chg_off;  // doubles: [3N] in charge
+    long long mass_off; // doubles: [9N] in mass
+    double box[3], inv_box[3];
+    double kappa, rc_sq, ewald_pref, k_pref, self_energy;
+    double r_cut_sq, r_skin_sq, skin_margin;
+    double beta, beta_n, omega_psq, dt, halfdt, eps_sc, c1_centroid;
+    float boxf[3], inv_boxf[3];
+    float kappaf, rc_sqf, ewald_preff, kappa_sqf;
+    unsigned long long seed;
+};
+
+// Per normal mode k of a system: free ring-polymer frequency and the
+// sqrt-Cayley / PILE coefficients (update.cpp:301-320, thermostat.cpp:117-123).
+struct ModeCoef {
+    double w2;     // omega_k^2 = (2 / beta_P hbar)^2 sin^2(k pi / P)
+    double scale;  // 1 / sqrt(1 + omega_k^2 dt^2 / 4)
+    double c1;     // exp(-dt gamma_k), gamma_k = (4 / beta_P hbar) sin(k pi / P)
+    double c2;     // sqrt(1 - c1^2)
+};
+
+// One reciprocal-lattice vector k = 2 pi (kx/Lx, ky/Ly, kz/Lz) of the set
+// forces.cpp:251-445 visits, with c_k = (2 pi / V) exp(-k^2/4 kappa^2) / k^2
+// (doubled for kx > 0) and g = 2 c_k k.
+struct KVec {
+    int kx, ky, kz, pad;
+    double coef, gx, gy, gz;
+};
+
+// One force evaluation ("job"): one configuration of one system.
+struct Job {
+    int sys;   // system index
+    int bead;  // bead whose Verlet list (point/list slice) the LJ term uses
+    int slot;  // scratch slot (per-job scratch arrays are indexed by slot)
+    int mode;  // 0 = forces; 1 = directional derivative of the Ewald forces
+    long long pos_off;  // doubles: the job's 9N positions, relative to the position base
+    long long out_off;  // doubles: the job's 9N forces, relative to the output base
+    long long site_off; // elements: 3N sites in the site scratch (per slot)
+    long long phase_off;// complex elements: phase table (3 * (kmax+1) * 3N) per slot
+    long long sk_off;   // complex elements: S(k) per slot
+};
+
+// Per-system, per-step accumulators (zeroed by the step-finalize kernel).
+struct SysAcc {
+    double kin;      // sum_b p^2 / 2m after the closing kick
+    double spring;   // sum_b 1/2 m w_P^2 (q_b - q_{b+1})^2
+    double kcv_tq;   // -sum (q_b - qbar) . fphys_b over the estimator's beads
+    double k0;       // centroid normal-mode kinetic energy entering the next O step
+    double sc_extra; // SC: sum over odd beads of fsq / (3 w_P^2)
+    double rebuilds; // Verlet lists rebuilt this step
+    double pad[2];
+};
+
+// Per-system persistent thermostat / RNG state.
+struct SysRun {
+    double heat;   // accumulated thermostat heat (update.cpp:325)
+    double alpha;  // centroid rescale factor for the next O step (PILE-G)
+    double pad[2];
+};
+
+// Status word written by kernels (bit flags), read by the host after a sync.
+enum StatusBits : unsigned {
+    ST_LIST_OVERFLOW = 1u,
+    ST_NONFINITE = 2u,
+    ST_GAMMA_LIMIT = 4u,
+};
+
+// ---- device helpers ---------------------------------------------------------
+#ifdef __CUDACC__
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum; every thread must call it. `sh` needs blockDim.x/32 doubles.
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (w == 0) {
+        t = (lane < nw) ? sh[lane] : 0.0;
+        t = warp_sum(t);
+    }
+    return t;  // valid in warp 0 (lane 0)
+}
+
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror & Shaw,
+// "Parallel random numbers: as easy as 1, 2, 3", SC'11): ten rounds of
+// (hi,lo) = M * x multiplications with a Weyl-sequence key schedule.
+struct Philox4 {
+    uint32_t v[4];
+};
+
+__device__ __forceinline__ Philox4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                 uint32_t k0, uint32_t k1) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(M0, c0), lo0 = M0 * c0;
+        uint32_t hi1 = __umulhi(M1, c2), lo1 = M1 * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+        k0 += W0;
+        k1 += W1;
+    }
+    Philox4 o;
+    o.v[0] = c0;
+    o.v[1] = c1;
+    o.v[2] = c2;
+    o.v[3] = c3;
+    return o;
+}
+
+// Uniform double in (0, 1) from two 32-bit words (53 significant bits).
+__device__ __forceinline__ double u01_from(uint32_t a, uint32_t b) {
+    unsigned long long x = ((unsigned long long)a << 21) ^ (unsigned long long)(b >> 11);
+    x &= ((1ull << 53) - 1ull);
+    return ((double)x + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+// Two standard normals (Box-Muller) from one Philox block.
+__device__ __forceinline__ double2 normal2(const Philox4 &r) {
+    double u1 = u01_from(r.v[0], r.v[1]);
+    double u2 = u01_from(r.v[2], r.v[3]);
+    double rad = sqrt(-2.0 * log(u1));
+    double s, c;
+    sincospi(2.0 * u2, &s, &c);
+    return make_double2(rad * c, rad * s);
+}
+
+// RNG stream tags (third counter word's high byte) keep draws independent.
+enum RngTag : uint32_t { RNG_MODES = 1u, RNG_CENTROID = 2u, RNG_GAMMA = 3u };
+
+#endif  // __CUDACC__
+
+// ---- launch interface between translation units ----------------------------
+
+// Column work item of the normal-mode / propagation kernels: a block handles
+// cols_per_block dof columns of one system (all beads of each column).
+struct ColWork {
+    int sys, col0, ncols, pad;
+};
+
+enum RingFlags : int {
+    RF_KICK = 1,    // p += dt/2 f before the transform
+    RF_FWD = 2,     // bead -> normal-mode transform of q, p
+    RF_CAYLEY = 4,  // sqrt-Cayley free ring-polymer half steps around the O step
+    RF_THERMO = 8,  // O step (PILE-G centroid rescale or PILE-L / mode Langevin)
+    RF_BACK = 16,   // normal-mode -> bead transform
+    RF_DISP = 32,   // track oxygen displacements in bead space
+    RF_VV = 64,     // classical velocity-Verlet drift q += dt p / m (P = 1)
+};
+
+struct RingArgs {
+    const SysDev *sys;
+    const ColWork *work;
+    int n_work;
+    int flags;
+    double *q, *p;
+    const double *f;
+    double *disp;
+    const double *mass;
+    const double *nm;        // bead -> normal-mode matrices
+    const ModeCoef *modes;
+    SysRun *run;
+    SysAcc *acc;
+    const double *noise;     // optional caller noise [R, g2, xi(mode 1..P-1, dof)] (one system)
+    const unsigned long long *step;
+    const double *fphys;     // end step: physical forces for the virial estimator
+    int kick;                // end step: 1 = apply the closing kick, 0 = estimators only
+    int kcv_all_beads;       // end step: -1 = by propagator, 0 = even beads, 1 = all beads
+    int max_p;               // largest bead count (shared-memory sizing)
+    int pile_g;              // 1: O step is PILE-G whatever the system's thermostat
+};
+
+struct FinalizeArgs {
+    const SysDev *sys;
+    int n_sys;
+    const double *energy;    // base-job energies (job_base + bead)
+    SysAcc *acc;
+    SysRun *run;
+    double *est;             // ring buffer [max_records][n_sys][8]
+    int max_records;
+    unsigned long long *step;
+    unsigned long long *records;
+    unsigned *status;
+    const double *noise;     // optional caller noise for the centroid draw (system 0 only)
+    int record;              // 1: write an estimator record and count a step
+    int draw_alpha;          // 1: draw the next PILE-G centroid factor
+    int sys_begin, sys_end;  // systems handled
+    int pile_g;              // 1: draw alpha whatever the system's thermostat
+};
+
+struct ScArgs {
+    const SysDev *sys;
+    const int *job_sys, *job_bead;  // odd beads (prepare) or all base jobs (finish)
+    int n_jobs;
+    const double *q, *fphys, *mass;
+    double *qdisp;      // displaced positions (q + d at bead b, q - d at bead b-1)
+    double *dirv;       // direction f/m at bead b (mixed mode)
+    const double *fdisp;   // FP64: F(q+d) at b, F(q-d) at b-1; mixed: dF_ewald at b
+    const double *fsr;     // mixed: short-range F(q+d) at b, F(q-d) at b-1
+    double *f;
+    double *sc_scale;   // per base job: s (the finite-difference step scale)
+    SysAcc *acc;
+    int mixed;
+    int max_dof;
+    int force_sc;       // finish: 1 = Suzuki-Chin assembly whatever the propagator
+};
+
+struct ReduceArgs {   // tier-1 estimators
+    const SysDev *sys;
+    int sysi;
+    const double *q, *p, *f, *mass, *nm;
+    double *out;      // out[0..]
+    int trotter;
+};
+
+// propagate.cu
+void launch_ring(const RingArgs &a, cudaStream_t s, unsigned long long *n);
+void launch_end_step(const RingArgs &a, cudaStream_t s, unsigned long long *n);
+void launch_finalize(const FinalizeArgs &a, cudaStream_t s, unsigned long long *n);
+void launch_sc_prepare(const ScArgs &a, cudaStream_t s, unsigned long long *n);
+void launch_sc_finish(const ScArgs &a, cudaStream_t s, unsigned long long *n);
+void launch_transform(const SysDev *sys, int sysi, int P, const double *nm_sys, double *a, int length,
+                      int forwards, cudaStream_t s, unsigned long long *n);
+void launch_centroid_ke(const RingArgs &a, cudaStream_t s, unsigned long long *n);
+// sum_k sum_j (p_kj^2 / 2 m_j + m_j w_k^2 q_kj^2 / 2) of normal-mode arrays -> out[0], out[1]
+void launch_nm_energy(const SysDev *sys, int sysi, int P, int n_dof, const double *q, const double *p,
+                      const double *mass, const ModeCoef *modes, double *out, cudaStream_t s,
+                      unsigned long long *n);
+
+struct EvalArgs {
+    const SysDev *sys;     // device array
+    const Job *jobs;       // device array, n_jobs entries
+    int n_jobs;
+    int max_mols;          // largest N over the jobs' systems (grid sizing)
+    int max_kvec;          // largest k-vector count
+    int max_kmax;
+    const double *pos;     // position base (jobs' pos_off are relative to it)
+    double *out;           // force output base
+    const double *dir;     // tangent direction base (mode 1 jobs), same offsets as pos
+    const double *charge;
+    const int *point, *list;
+    const KVec *kvec;
+    void *sites;           // float4 or double4 per site, per slot
+    double *site_force;    // double[3] per site, per slot
+    void *phase;           // float2 or double2, per slot
+    double2 *sk;           // S(k), per slot
+    double2 *dsk;          // d S(k) along the tangent direction, per slot
+    void *tan_sites;       // tangent of the site positions (mode 1), per slot
+    double *energy;        // per job
+    unsigned *status;
+    int sites_are_input;   // 1: positions are charge sites (M,H1,H2) -> kwald only
+    int skip_short_range;  // 1: no LJ / intramolecular terms (kwald only)
+    int sr_only;           // 1: only the FP64 short-range terms (LJ, intramolecular,
+                           //    same-molecule Ewald); site forces are ignored
+    int mode;              // 0 = forces, 1 = directional derivative of the Ewald forces
+    Consts c;
+};
+
+// forces.cu: individual Ewald kernels (for timing)
+void launch_ewald_kernel(const EvalArgs &a, bool mixed, const char *name, cudaStream_t s);
+void launch_fp32_probe(float *out, int blocks, int iters, cudaStream_t s);
+
+// forces.cu
+void launch_eval_fp64(const EvalArgs &a, cudaStream_t s, unsigned long long *launches);
+void launch_eval_mixed(const EvalArgs &a, cudaStream_t s, unsigned long long *launches);
+void launch_kwald_only(const EvalArgs &a, bool mixed, cudaStream_t s, unsigned long long *launches);
+
+// one-time kernel attribute set-up (shared-memory limits); called at context creation
+void init_force_kernel_attributes();
+void init_list_kernel_attributes();
+void init_propagate_kernel_attributes();
+
+// neighbour.cu
+struct ListArgs {
+    const SysDev *sys;
+    const int *job_sys, *job_bead;  // one (system, bead) per block
+    int n_jobs;
+    const double *q;
+    double *disp;
+    int *point, *list;
+    SysAcc *acc;
+    unsigned *status;
+    int force_rebuild;  // 1: rebuild unconditionally (initial build / per-call API)
+    int max_mols;
+};
+void launch_skin_rebuild(const ListArgs &a, cudaStream_t s, unsigned long long *launches);
+
+}  // namespace qtg
