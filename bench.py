@@ -153,17 +153,20 @@ def time_device_steps(s, steps, warmup, flush):
     """Per-step CUDA-event timing of graph replays; L2 flushed before each step (not timed)."""
     import torch
 
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: torch's default stream is the legacy NULL stream, which the
+    # library would replace by its own non-blocking stream
+    stream = torch.cuda.Stream()
     s.ctx.set_stream(stream.cuda_stream)
     s.ctx.run_steps(warmup, is_nvt=True)
     torch.cuda.synchronize()
     launches0 = s.ctx.kernel_launches()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    for k in range(steps):
-        flush.zero_()
-        ev[k][0].record(stream)
-        s.ctx.run_steps(1, is_nvt=True)
-        ev[k][1].record(stream)
+    with torch.cuda.stream(stream):
+        for k in range(steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            s.ctx.run_steps(1, is_nvt=True)
+            ev[k][1].record(stream)
     torch.cuda.synchronize()
     s.ctx.sync()
     ms = [a.elapsed_time(b) for a, b in ev]

@@ -154,9 +154,10 @@ struct qtg_ctx {
     double *nm = nullptr;
     ModeCoef *modes = nullptr;
     // per-slot scratch
-    void *sites = nullptr, *tan_sites = nullptr, *phase = nullptr;
-    double *site_force = nullptr;
-    double2 *sk = nullptr, *dsk = nullptr;
+    void *sites = nullptr, *tan_sites = nullptr, *phase = nullptr, *opos = nullptr;
+    double *part = nullptr;           // [MAX_PART][total_sites][3]
+    double2 *skp = nullptr, *dskp = nullptr;  // [MAX_SC][total_k]
+    size_t total_k = 0;
     double *energy = nullptr;      // per slot: energies of the base evaluations
     double *energy_aux = nullptr;  // per slot: displaced / derivative evaluations
     // job tables
@@ -223,11 +224,14 @@ EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, d
     a.list = c->list;
     a.kvec = c->kvec;
     a.sites = c->sites;
-    a.site_force = c->site_force;
+    a.opos = c->opos;
     a.phase = c->phase;
-    a.sk = c->sk;
-    a.dsk = c->dsk;
     a.tan_sites = c->tan_sites;
+    a.part = c->part;
+    a.total_sites = (long long)c->total_sites;
+    a.skp = c->skp;
+    a.dskp = c->dskp;
+    a.total_k = (long long)c->total_k;
     a.energy = c->energy;
     a.status = c->status;
     a.mode = mode;
@@ -637,6 +641,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     ctx->total_slots = slot_site.size();
     ctx->total_sites = (size_t)so;
     ctx->total_phase = (size_t)po;
+    ctx->total_k = (size_t)ko;
     auto mkjob = [&](int s, int b, int slot, int mode, long long pos_off) {
         Job j;
         j.sys = s;
@@ -739,9 +744,14 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         AL(tmp, 2 * ctx->total_phase);
         ctx->phase = tmp;
     }
-    AL(ctx->site_force, 3 * ctx->total_sites);
-    AL(ctx->sk, (size_t)ko);
-    AL(ctx->dsk, (size_t)ko);
+    {
+        double *tmp = nullptr;
+        AL(tmp, 4 * (ctx->total_sites / 3));
+        ctx->opos = tmp;
+    }
+    AL(ctx->part, (size_t)MAX_PART * 3 * ctx->total_sites);
+    AL(ctx->skp, (size_t)MAX_SC * ctx->total_k);
+    AL(ctx->dskp, (size_t)MAX_SC * ctx->total_k);
     AL(ctx->energy, ctx->total_slots);
     AL(ctx->energy_aux, ctx->total_slots);
     AL(ctx->base.d, ctx->base.h.size());
@@ -811,7 +821,7 @@ void qtg_destroy(qtg_ctx *ctx) {
     void *ptrs[] = {ctx->sys_d, ctx->q, ctx->p, ctx->f, ctx->fphys, ctx->qdisp, ctx->fdisp, ctx->fsr,
                     ctx->dirv, ctx->stage, ctx->disp, ctx->point, ctx->list, ctx->charge, ctx->mass,
                     ctx->sc_scale, ctx->noise, ctx->kvec, ctx->nm, ctx->modes, ctx->sites, ctx->tan_sites,
-                    ctx->phase, ctx->site_force, ctx->sk, ctx->dsk, ctx->energy, ctx->energy_aux,
+                    ctx->phase, ctx->opos, ctx->part, ctx->skp, ctx->dskp, ctx->energy, ctx->energy_aux,
                     ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
                     ctx->status, ctx->red_out};
@@ -921,15 +931,14 @@ qtg_status qtg_kwald(qtg_ctx *ctx, int sys, const double *sites, double *f_sites
     if (!sites || !f_sites || bead < 0 || bead >= S.n_beads) return fail(ctx, QTG_ERR_ARG, "bad argument");
     const size_t nd = S.n_dof;
     if (charge) CKS(upload_charges(ctx, sys, charge));
-    CK(up(ctx, ctx->stage + S.q_off + bead * nd, sites + bead * nd, sizeof(double) * nd));
+    // sites in qdisp, the caller's site forces in stage (the k-space forces are added)
+    CK(up(ctx, ctx->qdisp + S.q_off + bead * nd, sites + bead * nd, sizeof(double) * nd));
+    CK(up(ctx, ctx->stage + S.q_off + bead * nd, f_sites + bead * nd, sizeof(double) * nd));
     const int jb = S.job_base + bead;
-    const Job &J = ctx->base.h[jb];
-    CK(up(ctx, ctx->site_force + 3 * J.site_off, f_sites + bead * nd, sizeof(double) * nd));
-    EvalArgs a = eval_args(ctx, ctx->base.d + jb, 1, ctx->stage, ctx->fphys, 0, 0);
+    EvalArgs a = eval_args(ctx, ctx->base.d + jb, 1, ctx->qdisp, ctx->stage, 0, 0);
     a.sites_are_input = 1;
-    a.skip_short_range = 1;
     launch_kwald_only(a, ctx->mixed, ctx->stream, &ctx->launches);
-    CK(down(ctx, f_sites + bead * nd, ctx->site_force + 3 * J.site_off, sizeof(double) * nd));
+    CK(down(ctx, f_sites + bead * nd, ctx->stage + S.q_off + bead * nd, sizeof(double) * nd));
     double e = 0.0;
     CK(down(ctx, &e, ctx->energy + jb, sizeof(double)));
     CKS(sync_status(ctx));

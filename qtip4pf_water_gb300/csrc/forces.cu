@@ -2,26 +2,31 @@
 //
 // A launch evaluates a batch of "jobs" (one configuration of one system each;
 // all beads of all replicas at once). Per job:
-//   k_prep     charge sites (M, H1, H2) wrapped into the box, charges, and the
-//              per-site phase tables exp(i 2 pi m s_d), m = 0..k_max, d = x,y,z
-//              (charge folded into the x factor);
-//   k_real     real-space Ewald between sites of different molecules, j-sites
-//              tiled through shared memory, every i-site owned by one thread
-//              (no atomics, deterministic);
-//   k_ksk      structure factors S(k) = sum_i q_i exp(i k.r_i), one thread per
-//              k-vector, site chunks staged in shared memory; chunk partial sums
-//              are promoted to FP64 (compensated accumulation);
-//   k_kforce   reciprocal-space site forces, one thread per site, k-vector
-//              chunks (k, 2 c_k k, S(k)) broadcast from shared memory;
-//   k_combine  FP64 per molecule: same-molecule real-space pairs (erfc - 1),
-//              quartic-Morse bonds, HOH angle, M-site chain rule;
-//   k_lj       FP64 O-O Lennard-Jones over the CSR Verlet list.
-// The Ewald kernels are templated on the arithmetic type: double for the
-// parity mode, float (FP64 accumulation across tiles/chunks) for the mixed mode.
-// Mode-1 jobs compute the directional derivative of the intermolecular Ewald
-// forces along a per-dof direction (used by the Suzuki-Chin force gradient).
+//   k_prep     charge sites (M, H1, H2) wrapped into the box with their charges,
+//              wrapped oxygen positions, and per-site phase tables
+//              exp(i 2 pi m s_d), m = 0..k_max, d = x,y,z (complex recursion from
+//              exp(i 2 pi s_d), charge folded into the x factor);
+//   k_real     real-space Ewald between sites of different molecules; grid =
+//              (i-site tiles) x (j-chunks) x jobs, j-sites staged through shared
+//              memory, each thread owns one i-site and writes one partial force
+//              per j-chunk (no atomics, deterministic);
+//   k_ksk      structure factors S(k) = sum_i q_i exp(i k.r_i); grid = (k tiles)
+//              x (site chunks) x jobs, one thread per k-vector, site chunks staged
+//              in shared memory, 32-site partial sums promoted to FP64;
+//   k_kforce   reciprocal-space site forces; grid = (i-site tiles) x (k-chunks)
+//              x jobs, (k, 2 c_k k, S(k)) broadcast from shared memory, S(k)
+//              summed over the site-chunk partials in fixed order;
+//   k_combine  per molecule: partial site forces summed in fixed order, same-
+//              molecule real-space pairs (erfc - 1), quartic-Morse bonds, HOH
+//              angle (FP64 difference vectors), M-site chain rule;
+//   k_lj       O-O Lennard-Jones over the CSR Verlet list, one warp per row.
+// The kernels are templated on the arithmetic type: double for the parity
+// mode, float (FP64 accumulation across tiles/chunks/planes) for the mixed
+// mode. Mode-1 jobs compute the directional derivative of the intermolecular
+// Ewald forces along a per-dof direction (the Suzuki-Chin force gradient).
 #include <math.h>
 
+#include <algorithm>
 #include <string>
 
 #include "qtg_internal.h"
@@ -45,6 +50,8 @@ __device__ __forceinline__ float f_rint(float x) { return rintf(x); }
 __device__ __forceinline__ double f_rint(double x) { return rint(x); }
 __device__ __forceinline__ float f_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double f_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float f_acos(float x) { return acosf(x); }
+__device__ __forceinline__ double f_acos(double x) { return acos(x); }
 __device__ __forceinline__ void f_sincospi(float t, float *s, float *c) { sincospif(t, s, c); }
 __device__ __forceinline__ void f_sincospi(double t, double *s, double *c) { sincospi(t, s, c); }
 
@@ -54,6 +61,8 @@ template <> __device__ __forceinline__ double sys_box<double>(const SysDev &S, i
 template <typename R> __device__ __forceinline__ R sys_ibox(const SysDev &S, int d);
 template <> __device__ __forceinline__ float sys_ibox<float>(const SysDev &S, int d) { return S.inv_boxf[d]; }
 template <> __device__ __forceinline__ double sys_ibox<double>(const SysDev &S, int d) { return S.inv_box[d]; }
+
+__device__ __forceinline__ int chunk_lo(int n, int c, int nc) { return (int)(((long long)n * c) / nc); }
 
 // ---- k_prep -------------------------------------------------------------------
 template <typename R>
@@ -81,46 +90,67 @@ __global__ void __launch_bounds__(128) k_prep(EvalArgs a) {
             for (int d = 0; d < 3; ++d)
                 u[d] = g * v[9 * mol + d] + 0.5 * (1.0 - g) * (v[9 * mol + 3 + d] + v[9 * mol + 6 + d]);
         }
+        // wrapped oxygen position for the Lennard-Jones kernel
+        V4<R> o;
+        double w[3];
+        for (int d = 0; d < 3; ++d) {
+            const double t = q[9 * mol + d] * S.inv_box[d];
+            w[d] = (t - floor(t)) * S.box[d];
+        }
+        o.x = (R)w[0];
+        o.y = (R)w[1];
+        o.z = (R)w[2];
+        o.w = (R)0;
+        reinterpret_cast<V4<R> *>(a.opos)[J.site_off / 3 + mol] = o;
     }
     const double chg = a.charge[S.chg_off + s];
     double frac[3];
     for (int d = 0; d < 3; ++d) {
-        double t = x[d] * S.inv_box[d];
+        const double t = x[d] * S.inv_box[d];
         frac[d] = t - floor(t);
     }
-    V4<R> *sites = reinterpret_cast<V4<R> *>(a.sites) + J.site_off;
     V4<R> sv;
     sv.x = (R)(frac[0] * S.box[0]);
     sv.y = (R)(frac[1] * S.box[1]);
     sv.z = (R)(frac[2] * S.box[2]);
     sv.w = (R)chg;
-    sites[s] = sv;
+    reinterpret_cast<V4<R> *>(a.sites)[J.site_off + s] = sv;
     if (J.mode == 1) {
-        V4<R> *tan = reinterpret_cast<V4<R> *>(a.tan_sites) + J.site_off;
         V4<R> tv;
         tv.x = (R)u[0];
         tv.y = (R)u[1];
         tv.z = (R)u[2];
         tv.w = (R)0;
-        tan[s] = tv;
+        reinterpret_cast<V4<R> *>(a.tan_sites)[J.site_off + s] = tv;
     }
-    // phase table exp(i 2 pi m frac_d), layout [(d * (kmax+1) + m) * ns + s]
+    // phase table exp(i 2 pi m frac_d), layout [(d * (kmax+1) + m) * ns + s], by
+    // complex recursion from exp(i 2 pi frac_d) (as forces.cpp:233-240 does),
+    // reseeded every 4 powers from a directly evaluated phase whose argument
+    // 2 m frac_d is reduced in FP64, so rounding does not accumulate with m
     const int km1 = S.k_max + 1;
     V2<R> *ph = reinterpret_cast<V2<R> *>(a.phase) + J.phase_off;
     for (int d = 0; d < 3; ++d) {
-        for (int m = 0; m < km1; ++m) {
-            double t = 2.0 * m * frac[d];
+        R s1, c1;
+        {
+            double t = 2.0 * frac[d];
             t -= 2.0 * floor(0.5 * t + 0.5);  // in [-1, 1)
-            R sn, cs;
-            f_sincospi((R)t, &sn, &cs);
-            if (d == 0) {
-                cs = (R)(cs * chg);
-                sn = (R)(sn * chg);
+            f_sincospi((R)t, &s1, &c1);
+        }
+        const R qd = (d == 0) ? (R)chg : (R)1;
+        R cr = (R)1, ci = (R)0;
+        for (int m = 0; m < km1; ++m) {
+            if (m > 0 && (m & 3) == 0) {
+                double t = 2.0 * m * frac[d];
+                t -= 2.0 * floor(0.5 * t + 0.5);
+                f_sincospi((R)t, &ci, &cr);
             }
             V2<R> e;
-            e.x = cs;
-            e.y = sn;
+            e.x = cr * qd;
+            e.y = ci * qd;
             ph[(size_t)(d * km1 + m) * ns + s] = e;
+            const R nr = cr * c1 - ci * s1;
+            ci = cr * s1 + ci * c1;
+            cr = nr;
         }
     }
 }
@@ -130,13 +160,14 @@ constexpr int RT = 128;
 
 template <typename R, int MODE>
 __global__ void __launch_bounds__(RT) k_real(EvalArgs a) {
-    const int jb = blockIdx.y;
+    const int rj = blockIdx.y, jb = blockIdx.z;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
     const int ns = S.n_sites;
     if (blockIdx.x * RT >= ns) return;
     const int i = blockIdx.x * RT + threadIdx.x;
     const bool act = i < ns;
+    const int j0 = chunk_lo(ns, rj, a.n_rj), j1 = chunk_lo(ns, rj + 1, a.n_rj);
     const V4<R> *sites = reinterpret_cast<const V4<R> *>(a.sites) + J.site_off;
     const V4<R> *tans = reinterpret_cast<const V4<R> *>(a.tan_sites) + J.site_off;
     __shared__ V4<R> sj[RT];
@@ -154,19 +185,18 @@ __global__ void __launch_bounds__(RT) k_real(EvalArgs a) {
     }
     const int mi = i / 3;
     double Fx = 0.0, Fy = 0.0, Fz = 0.0, E = 0.0;
-    for (int t0 = 0; t0 < ns; t0 += RT) {
+    for (int t0 = j0; t0 < j1; t0 += RT) {
         __syncthreads();
-        if (t0 + threadIdx.x < ns) {
+        if (t0 + threadIdx.x < j1) {
             sj[threadIdx.x] = sites[t0 + threadIdx.x];
             if (MODE == 1) uj[threadIdx.x] = tans[t0 + threadIdx.x];
         }
         __syncthreads();
-        const int nj = min(RT, ns - t0);
+        const int nj = min(RT, j1 - t0);
         R fx = 0, fy = 0, fz = 0, e = 0;
         if (act) {
             for (int jj = 0; jj < nj; ++jj) {
-                const int j = t0 + jj;
-                if (j / 3 == mi) continue;
+                if ((t0 + jj) / 3 == mi) continue;
                 const V4<R> b = sj[jj];
                 R dx = si.x - b.x, dy = si.y - b.y, dz = si.z - b.z;
                 dx -= L0 * f_rint(dx * I0);
@@ -207,13 +237,13 @@ __global__ void __launch_bounds__(RT) k_real(EvalArgs a) {
         E += (double)e;
     }
     if (act) {
-        double *fs = a.site_force + 3 * (J.site_off + i);
+        double *fs = a.part + 3 * ((size_t)rj * a.total_sites + J.site_off + i);
         fs[0] = Fx;
         fs[1] = Fy;
         fs[2] = Fz;
     }
     if (MODE == 0) {
-        double t = block_sum(0.5 * E, red);
+        const double t = block_sum(0.5 * E, red);
         if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
     }
 }
@@ -224,18 +254,18 @@ constexpr int CH = 32;   // sites per shared-memory chunk
 
 template <typename R, int MODE>
 __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
-    const int jb = blockIdx.y;
+    const int sc = blockIdx.y, jb = blockIdx.z;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
     const int nk = S.n_kvec, ns = S.n_sites, km1 = S.k_max + 1;
     if (blockIdx.x * KT >= nk) return;
     const int t = blockIdx.x * KT + threadIdx.x;
     const bool act = t < nk;
+    const int s0 = chunk_lo(ns, sc, a.n_sc), s1 = chunk_lo(ns, sc + 1, a.n_sc);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // 16-byte elements first so every array stays aligned for vector access
-    V4<R> *ush = reinterpret_cast<V4<R> *>(smem_raw);                 // [CH] (mode 1)
-    V2<R> *tab = reinterpret_cast<V2<R> *>(ush + CH);                 // [3*km1][CH+1]
-    __shared__ double red[KT / 32];
+    V4<R> *ush = reinterpret_cast<V4<R> *>(smem_raw);  // [CH] (mode 1)
+    V2<R> *tab = reinterpret_cast<V2<R> *>(ush + CH);  // [3*km1][CH+1]
     KVec kv;
     kv.kx = kv.ky = kv.kz = 0;
     kv.coef = 0.0;
@@ -249,22 +279,22 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
     const V4<R> *tans = reinterpret_cast<const V4<R> *>(a.tan_sites) + J.site_off;
     double Sr = 0.0, Si = 0.0, dSr = 0.0, dSi = 0.0;
     const int rows = 3 * km1;
-    for (int c0 = 0; c0 < ns; c0 += CH) {
+    for (int c0 = s0; c0 < s1; c0 += CH) {
         __syncthreads();
         for (int idx = threadIdx.x; idx < rows * CH; idx += KT) {
             const int row = idx / CH, c = idx - row * CH, s = c0 + c;
             V2<R> v;
             v.x = v.y = (R)0;
-            if (s < ns) v = ph[(size_t)row * ns + s];
+            if (s < s1) v = ph[(size_t)row * ns + s];
             tab[row * (CH + 1) + c] = v;
         }
         if (MODE == 1 && threadIdx.x < CH) {
             V4<R> z;
             z.x = z.y = z.z = z.w = (R)0;
-            ush[threadIdx.x] = (c0 + threadIdx.x < ns) ? tans[c0 + threadIdx.x] : z;
+            ush[threadIdx.x] = (c0 + threadIdx.x < s1) ? tans[c0 + threadIdx.x] : z;
         }
         __syncthreads();
-        const int nc = min(CH, ns - c0);
+        const int nc = min(CH, s1 - c0);
         R sr = 0, si = 0, dsr = 0, dsi = 0;
         const V2<R> *X = tab + ax * (CH + 1);
         const V2<R> *Y = tab + (km1 + ay) * (CH + 1);
@@ -291,13 +321,9 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
         }
     }
     if (act) {
-        a.sk[J.sk_off + t] = make_double2(Sr, Si);
-        if (MODE == 1) a.dsk[J.sk_off + t] = make_double2(dSr, dSi);
-    }
-    if (MODE == 0) {
-        double e = act ? kv.coef * (Sr * Sr + Si * Si) : 0.0;
-        double tot = block_sum(e, red);
-        if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], tot);
+        const size_t at = (size_t)sc * a.total_k + J.sk_off + t;
+        a.skp[at] = make_double2(Sr, Si);
+        if (MODE == 1) a.dskp[at] = make_double2(dSr, dSi);
     }
 }
 
@@ -307,20 +333,22 @@ constexpr int KC = 128;  // k-vectors per shared-memory chunk
 
 template <typename R, int MODE>
 __global__ void __launch_bounds__(FT) k_kforce(EvalArgs a) {
-    const int jb = blockIdx.y;
+    const int kc = blockIdx.y, jb = blockIdx.z;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
     const int nk = S.n_kvec, ns = S.n_sites, km1 = S.k_max + 1;
     if (blockIdx.x * FT >= ns) return;
     const int i = blockIdx.x * FT + threadIdx.x;
     const bool act = i < ns;
+    const int k0 = chunk_lo(nk, kc, a.n_kc), k1 = chunk_lo(nk, kc + 1, a.n_kc);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // 16-byte elements first so every array stays aligned for vector access
-    int4 *kk = reinterpret_cast<int4 *>(smem_raw);      // [KC]
-    V4<R> *gg = reinterpret_cast<V4<R> *>(kk + KC);     // [KC]
-    V2<R> *ss = reinterpret_cast<V2<R> *>(gg + KC);     // [KC]
-    V2<R> *ds = ss + KC;                                // [KC]
-    V2<R> *myph = ds + KC;                              // [3*km1][FT]
+    int4 *kk = reinterpret_cast<int4 *>(smem_raw);   // [KC]
+    V4<R> *gg = reinterpret_cast<V4<R> *>(kk + KC);  // [KC]
+    V2<R> *ss = reinterpret_cast<V2<R> *>(gg + KC);  // [KC]
+    V2<R> *ds = ss + KC;                             // [KC]
+    V2<R> *myph = ds + KC;                           // [3*km1][FT]
+    __shared__ double red[FT / 32];
     const V2<R> *ph = reinterpret_cast<const V2<R> *>(a.phase) + J.phase_off;
     for (int row = 0; row < 3 * km1; ++row) {
         V2<R> v;
@@ -333,12 +361,13 @@ __global__ void __launch_bounds__(FT) k_kforce(EvalArgs a) {
     if (MODE == 1 && act) ui = reinterpret_cast<const V4<R> *>(a.tan_sites)[J.site_off + i];
     const R b0 = (R)(2.0 * PI_REF * S.inv_box[0]), b1 = (R)(2.0 * PI_REF * S.inv_box[1]),
             b2 = (R)(2.0 * PI_REF * S.inv_box[2]);
-    double Fx = 0.0, Fy = 0.0, Fz = 0.0;
-    for (int k0 = 0; k0 < nk; k0 += KC) {
+    const bool do_energy = (MODE == 0) && blockIdx.x == 0;
+    double Fx = 0.0, Fy = 0.0, Fz = 0.0, E = 0.0;
+    for (int c0 = k0; c0 < k1; c0 += KC) {
         __syncthreads();
         for (int idx = threadIdx.x; idx < KC; idx += FT) {
-            const int k = k0 + idx;
-            if (k < nk) {
+            const int k = c0 + idx;
+            if (k < k1) {
                 const KVec v = a.kvec[S.kvec_off + k];
                 kk[idx] = make_int4(v.kx, abs(v.ky), abs(v.kz), (v.ky < 0 ? 1 : 0) | (v.kz < 0 ? 2 : 0));
                 V4<R> g;
@@ -347,22 +376,33 @@ __global__ void __launch_bounds__(FT) k_kforce(EvalArgs a) {
                 g.z = (R)v.gz;
                 g.w = (R)0;
                 gg[idx] = g;
-                const double2 sk = a.sk[J.sk_off + k];
+                double sr = 0.0, si = 0.0, dr = 0.0, di = 0.0;
+                for (int sc = 0; sc < a.n_sc; ++sc) {
+                    const size_t at = (size_t)sc * a.total_k + J.sk_off + k;
+                    const double2 p = a.skp[at];
+                    sr += p.x;
+                    si += p.y;
+                    if (MODE == 1) {
+                        const double2 d = a.dskp[at];
+                        dr += d.x;
+                        di += d.y;
+                    }
+                }
+                if (do_energy) E += v.coef * (sr * sr + si * si);
                 V2<R> s2;
-                s2.x = (R)sk.x;
-                s2.y = (R)sk.y;
+                s2.x = (R)sr;
+                s2.y = (R)si;
                 ss[idx] = s2;
                 if (MODE == 1) {
-                    const double2 d = a.dsk[J.sk_off + k];
                     V2<R> d2;
-                    d2.x = (R)d.x;
-                    d2.y = (R)d.y;
+                    d2.x = (R)dr;
+                    d2.y = (R)di;
                     ds[idx] = d2;
                 }
             }
         }
         __syncthreads();
-        const int nc = min(KC, nk - k0);
+        const int nc = min(KC, k1 - c0);
         R fx = 0, fy = 0, fz = 0;
         for (int c = 0; c < nc; ++c) {
             const int4 k = kk[c];
@@ -390,38 +430,45 @@ __global__ void __launch_bounds__(FT) k_kforce(EvalArgs a) {
         Fz += (double)fz;
     }
     if (act) {
-        double *fs = a.site_force + 3 * (J.site_off + i);
-        fs[0] += Fx;
-        fs[1] += Fy;
-        fs[2] += Fz;
+        double *fs = a.part + 3 * ((size_t)(a.n_rj + kc) * a.total_sites + J.site_off + i);
+        fs[0] = Fx;
+        fs[1] = Fy;
+        fs[2] = Fz;
+    }
+    if (do_energy) {
+        const double t = block_sum(E, red);
+        if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
     }
 }
 
-// ---- k_combine: FP64 short-range terms and the M-site chain rule ------------------
+// ---- k_combine: partial sums, short-range terms and the M-site chain rule ---------
 
 __device__ __forceinline__ void min_image3(double *r, const SysDev &S) {
     for (int d = 0; d < 3; ++d) r[d] -= S.box[d] * round(r[d] / S.box[d]);
 }
 
-// same-molecule real-space pair with erfc - 1 (forces.cpp:141-177)
-__device__ __forceinline__ double ewald_same_mol(const double *ri, const double *rj, double qiqj,
-                                                 const SysDev &S, double *fi, double *fj) {
-    double r[3];
-    for (int d = 0; d < 3; ++d) r[d] = ri[d] - rj[d];
-    min_image3(r, S);
-    const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
-    if (!(r2 < S.rc_sq)) return 0.0;
-    const double rl = sqrt(r2), inv = 1.0 / rl;
-    const double ec = erfc(S.kappa * rl) - 1.0;
-    const double e = qiqj * inv * ec;
-    const double ff = (e + qiqj * S.ewald_pref * exp(-(S.kappa * S.kappa) * r2)) * inv * inv;
+// same-molecule real-space pair with erfc - 1 (forces.cpp:141-177); the
+// difference vector is formed in FP64, the pair term in R
+template <typename R>
+__device__ __forceinline__ double ewald_same_mol(const double *ri, const double *rj, double qiqj, const SysDev &S,
+                                                 double *fi, double *fj) {
+    double rd[3];
+    for (int d = 0; d < 3; ++d) rd[d] = ri[d] - rj[d];
+    min_image3(rd, S);
+    const double r2d = rd[0] * rd[0] + rd[1] * rd[1] + rd[2] * rd[2];
+    if (!(r2d < S.rc_sq)) return 0.0;
+    const R r2 = (R)r2d, rl = f_sqrt(r2), inv = (R)1 / rl, kap = (R)S.kappa;
+    const R ec = f_erfc(kap * rl) - (R)1;
+    const R e = (R)qiqj * inv * ec;
+    const R ff = (e + (R)qiqj * (R)S.ewald_pref * f_exp(-(kap * kap) * r2)) * inv * inv;
     for (int d = 0; d < 3; ++d) {
-        fi[d] += ff * r[d];
-        fj[d] -= ff * r[d];
+        fi[d] += (double)(ff * (R)rd[d]);
+        fj[d] -= (double)(ff * (R)rd[d]);
     }
-    return e;
+    return (double)e;
 }
 
+template <typename R>
 __global__ void __launch_bounds__(128) k_combine(EvalArgs a) {
     const int jb = blockIdx.y;
     const Job J = a.jobs[jb];
@@ -435,11 +482,13 @@ __global__ void __launch_bounds__(128) k_combine(EvalArgs a) {
         const double *q = a.pos + J.pos_off + 9 * m;
         double *f = a.out + J.out_off + 9 * m;
         double fs[9];
-        if (a.sr_only) {
-            for (int k = 0; k < 9; ++k) fs[k] = 0.0;
-        } else {
-            const double *sf = a.site_force + 3 * (J.site_off + 3 * m);
-            for (int k = 0; k < 9; ++k) fs[k] = sf[k];
+        for (int k = 0; k < 9; ++k) fs[k] = 0.0;
+        if (!a.sr_only) {
+            const int np = a.n_rj + a.n_kc;
+            for (int p = 0; p < np; ++p) {
+                const double *sf = a.part + 3 * ((size_t)p * a.total_sites + J.site_off + 3 * m);
+                for (int k = 0; k < 9; ++k) fs[k] += sf[k];
+            }
         }
         double fa[9];
         for (int k = 0; k < 9; ++k) fa[k] = 0.0;
@@ -453,44 +502,51 @@ __global__ void __launch_bounds__(128) k_combine(EvalArgs a) {
                 site[3 + d] = q[3 + d];
                 site[6 + d] = q[6 + d];
             }
-            e += ewald_same_mol(site, site + 3, chg[0] * chg[1], S, fs, fs + 3);
-            e += ewald_same_mol(site, site + 6, chg[0] * chg[2], S, fs, fs + 6);
-            e += ewald_same_mol(site + 3, site + 6, chg[1] * chg[2], S, fs + 3, fs + 6);
-            // quartic Morse bonds (forces.cpp:65-93, :519-551)
-            double ra[3], rb[3];
+            e += ewald_same_mol<R>(site, site + 3, chg[0] * chg[1], S, fs, fs + 3);
+            e += ewald_same_mol<R>(site, site + 6, chg[0] * chg[2], S, fs, fs + 6);
+            e += ewald_same_mol<R>(site + 3, site + 6, chg[1] * chg[2], S, fs + 3, fs + 6);
+            // quartic Morse bonds (forces.cpp:65-93, :519-551); FP64 bond vectors
+            double rad[3], rbd[3];
             for (int d = 0; d < 3; ++d) {
-                ra[d] = q[d] - q[3 + d];
-                rb[d] = q[d] - q[6 + d];
+                rad[d] = q[d] - q[3 + d];
+                rbd[d] = q[d] - q[6 + d];
             }
-            min_image3(ra, S);
-            min_image3(rb, S);
-            const double la = sqrt(ra[0] * ra[0] + ra[1] * ra[1] + ra[2] * ra[2]);
-            const double lb = sqrt(rb[0] * rb[0] + rb[1] * rb[1] + rb[2] * rb[2]);
+            min_image3(rad, S);
+            min_image3(rbd, S);
+            R ra[3], rb[3];
+            for (int d = 0; d < 3; ++d) {
+                ra[d] = (R)rad[d];
+                rb[d] = (R)rbd[d];
+            }
+            const double lad = sqrt(rad[0] * rad[0] + rad[1] * rad[1] + rad[2] * rad[2]);
+            const double lbd = sqrt(rbd[0] * rbd[0] + rbd[1] * rbd[1] + rbd[2] * rbd[2]);
+            const R la = (R)lad, lb = (R)lbd;
+            const R ar2 = (R)C.ar2, ar3 = (R)C.ar3, ar4 = (R)C.ar4fac, Dr = (R)C.Dr;
             for (int bnd = 0; bnd < 2; ++bnd) {
-                const double *r = bnd ? rb : ra;
-                const double rl = bnd ? lb : la;
-                const double x = rl - C.roheq, x2 = x * x, x3 = x2 * x, x4 = x2 * x2;
-                e += C.Dr * (C.ar2 * x2 - C.ar3 * x3 + C.ar4fac * x4);
-                const double gg = (2.0 * C.ar2 * x - 3.0 * C.ar3 * x2 + 4.0 * C.ar4fac * x3) * C.Dr / rl;
+                const R *r = bnd ? rb : ra;
+                const R rl = bnd ? lb : la;
+                const R x = (R)((bnd ? lbd : lad) - C.roheq), x2 = x * x, x3 = x2 * x, x4 = x2 * x2;
+                e += (double)(Dr * (ar2 * x2 - ar3 * x3 + ar4 * x4));
+                const R gg = ((R)2 * ar2 * x - (R)3 * ar3 * x2 + (R)4 * ar4 * x3) * Dr / rl;
                 for (int d = 0; d < 3; ++d) {
-                    fa[d] -= gg * r[d];
-                    fa[3 + 3 * bnd + d] += gg * r[d];
+                    fa[d] -= (double)(gg * r[d]);
+                    fa[3 + 3 * bnd + d] += (double)(gg * r[d]);
                 }
             }
             // harmonic HOH angle (forces.cpp:96-138)
             {
-                const double dot = ra[0] * rb[0] + ra[1] * rb[1] + ra[2] * rb[2];
-                const double ia = 1.0 / la, ib = 1.0 / lb, iab = ia * ib;
-                const double c = dot * iab;
-                const double dacos = 1.0 / sqrt(1.0 - c * c);
-                const double ca = dot * ia * ia * iab, cb = dot * ib * ib * iab;
-                const double dth = acos(c) - C.theta_eq;
-                e += 0.5 * C.ktheta * dth * dth;
-                const double gp = C.ktheta * dth * dacos;
+                const R dot = ra[0] * rb[0] + ra[1] * rb[1] + ra[2] * rb[2];
+                const R ia = (R)1 / la, ib = (R)1 / lb, iab = ia * ib;
+                const R c = dot * iab;
+                const R dacos = (R)1 / f_sqrt((R)1 - c * c);
+                const R ca = dot * ia * ia * iab, cb = dot * ib * ib * iab;
+                const R dth = f_acos(c) - (R)C.theta_eq;
+                e += 0.5 * C.ktheta * (double)dth * (double)dth;
+                const R gp = (R)C.ktheta * dth * dacos;
                 for (int d = 0; d < 3; ++d) {
-                    fa[d] += gp * (iab * (ra[d] + rb[d]) - ca * ra[d] - cb * rb[d]);
-                    fa[3 + d] -= gp * (iab * rb[d] - ca * ra[d]);
-                    fa[6 + d] -= gp * (iab * ra[d] - cb * rb[d]);
+                    fa[d] += (double)(gp * (iab * (ra[d] + rb[d]) - ca * ra[d] - cb * rb[d]));
+                    fa[3 + d] -= (double)(gp * (iab * rb[d] - ca * ra[d]));
+                    fa[6 + d] -= (double)(gp * (iab * ra[d] - cb * rb[d]));
                 }
             }
         }
@@ -504,65 +560,155 @@ __global__ void __launch_bounds__(128) k_combine(EvalArgs a) {
     }
     if (J.mode == 0) {
         if (m == 0 && !a.sr_only) e -= S.self_energy;
-        double t = block_sum(e, red);
+        const double t = block_sum(e, red);
         if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
     }
 }
 
 // ---- k_lj: O-O Lennard-Jones over the Verlet list (forces.cpp:489-515) -----------
+// One warp per CSR row; lanes over the row's entries. The pair's displacement
+// and the cutoff decision r^2 < r_cut^2 must be the reference's (FP64,
+// x - L*round(x/L) with a true division and round-half-away-from-zero, each
+// operation rounded): a pair whose working-precision r^2 lies within a
+// relative band around r_cut^2, or whose separation is within rounding of
+// half a box in some dimension (where the two images tie and the rounding rule
+// picks the sign), is recomputed with exactly that arithmetic.
+__device__ __forceinline__ double lj_exact_disp(const double *qi, const double *qj, const SysDev &S, double *r) {
+    double r2 = 0.0;
+    for (int d = 0; d < 3; ++d) {
+        double x = __dsub_rn(qi[d], qj[d]);
+        x = __dsub_rn(x, __dmul_rn(S.box[d], round(__ddiv_rn(x, S.box[d]))));
+        r[d] = x;
+        r2 = (d == 0) ? __dmul_rn(x, x) : __dadd_rn(r2, __dmul_rn(x, x));
+    }
+    return r2;
+}
+
+template <typename R>
 __global__ void __launch_bounds__(128) k_lj(EvalArgs a) {
     const int jb = blockIdx.y;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
     const int N = S.n_mols;
-    if (blockIdx.x * blockDim.x >= N) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (blockIdx.x * 4 >= N) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int i = blockIdx.x * 4 + w;
     __shared__ double red[4];
     double e = 0.0;
+    const Consts &C = a.c;
+    const double rc2 = C.r_cut_sq;
+    const double band = sizeof(R) == 4 ? 1e-5 : 1e-12;
+    const R tie = sizeof(R) == 4 ? (R)1e-5 : (R)1e-12;
     if (i < N - 1) {
         const double *q = a.pos + J.pos_off;
         double *f = a.out + J.out_off;
         const int *pt = a.point + S.pt_off + (size_t)J.bead * N;
         const int *ls = a.list + S.ls_off + (size_t)J.bead * S.list_size;
-        const Consts &C = a.c;
-        double fi[3] = {0.0, 0.0, 0.0};
         // a row outside [0, list_size] (overflowed or caller-corrupted list) or an index
-        // outside [0, N) is skipped and flagged instead of being read out of bounds
+        // outside (i, N) is skipped and flagged instead of being read out of bounds
         int n0 = pt[i], n1 = pt[i + 1];
         if (n0 < 0 || n1 > S.list_size || n0 > n1) {
-            atomicOr(a.status, (unsigned)ST_LIST_OVERFLOW);
+            if (lane == 0) atomicOr(a.status, (unsigned)ST_LIST_OVERFLOW);
             n0 = max(0, min(n0, S.list_size));
             n1 = max(n0, min(n1, S.list_size));
         }
-        for (int n = n0; n < n1; ++n) {
+        R xi[3];
+        const V4<R> *opos = reinterpret_cast<const V4<R> *>(a.opos) + J.site_off / 3;
+        if (sizeof(R) == 4) {
+            const V4<R> o = opos[i];
+            xi[0] = o.x;
+            xi[1] = o.y;
+            xi[2] = o.z;
+        } else {
+            for (int d = 0; d < 3; ++d) xi[d] = (R)q[9 * i + d];
+        }
+        const R s6c = (R)C.sigmalj6, s12c = (R)C.sigmalj12, eps4 = (R)(4.0 * C.epslj), eps24 = (R)(24.0 * C.epslj);
+        R fi0 = 0, fi1 = 0, fi2 = 0, el = 0;
+        for (int n = n0 + lane; n < n1; n += 32) {
             const int j = ls[n];
             if (j <= i || j >= N) {
                 atomicOr(a.status, (unsigned)ST_LIST_OVERFLOW);
                 continue;
             }
-            double r[3];
-            for (int d = 0; d < 3; ++d) {
-                double x = __dsub_rn(q[9 * i + d], q[9 * j + d]);
-                r[d] = __dsub_rn(x, __dmul_rn(S.box[d], round(__ddiv_rn(x, S.box[d]))));
+            R r[3];
+            if (sizeof(R) == 4) {
+                const V4<R> o = opos[j];
+                r[0] = xi[0] - o.x;
+                r[1] = xi[1] - o.y;
+                r[2] = xi[2] - o.z;
+            } else {
+                for (int d = 0; d < 3; ++d) r[d] = xi[d] - (R)q[9 * j + d];
             }
-            const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(r[0], r[0]), __dmul_rn(r[1], r[1])),
-                                        __dmul_rn(r[2], r[2]));
-            if (r2 < C.r_cut_sq) {
-                const double i2 = 1.0 / r2, i6 = i2 * i2 * i2;
-                const double s6 = i6 * C.sigmalj6, s12 = i6 * i6 * C.sigmalj12;
-                const double en = s12 - s6;
-                e += en * 4.0 * C.epslj - C.e_cut;
-                const double ff = (en + s12) * 24.0 * C.epslj * i2;
-                for (int d = 0; d < 3; ++d) {
-                    fi[d] += ff * r[d];
-                    atomicAdd(&f[9 * j + d], -ff * r[d]);
-                }
+            bool exact = false;
+            for (int d = 0; d < 3; ++d) {
+                const R t = r[d] * sys_ibox<R>(S, d);
+                const R fr = fabs(t - trunc(t));
+                if (fabs(fr - (R)0.5) < tie) exact = true;
+                r[d] -= sys_box<R>(S, d) * f_rint(t);
+            }
+            R r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+            if (exact || fabs((double)r2 - rc2) <= band * rc2) {
+                double rd[3];
+                const double r2d = lj_exact_disp(q + 9 * i, q + 9 * j, S, rd);
+                for (int d = 0; d < 3; ++d) r[d] = (R)rd[d];
+                r2 = (R)r2d;
+                exact = r2d < rc2;
+            } else {
+                exact = r2 < (R)rc2;
+            }
+            if (exact) {
+                const R i2 = (R)1 / r2, i6 = i2 * i2 * i2;
+                const R s6 = i6 * s6c, s12 = i6 * i6 * s12c;
+                const R en = s12 - s6;
+                el += en * eps4 - (R)C.e_cut;
+                const R ff = (en + s12) * eps24 * i2;
+                fi0 += ff * r[0];
+                fi1 += ff * r[1];
+                fi2 += ff * r[2];
+                atomicAdd(&f[9 * j], -(double)(ff * r[0]));
+                atomicAdd(&f[9 * j + 1], -(double)(ff * r[1]));
+                atomicAdd(&f[9 * j + 2], -(double)(ff * r[2]));
             }
         }
-        for (int d = 0; d < 3; ++d) atomicAdd(&f[9 * i + d], fi[d]);
+        const double d0 = warp_sum((double)fi0), d1 = warp_sum((double)fi1), d2 = warp_sum((double)fi2);
+        e = warp_sum((double)el);
+        if (lane == 0) {
+            atomicAdd(&f[9 * i], d0);
+            atomicAdd(&f[9 * i + 1], d1);
+            atomicAdd(&f[9 * i + 2], d2);
+        } else {
+            e = 0.0;
+        }
     }
-    double t = block_sum(e, red);
+    const double t = block_sum(e, red);
     if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
+}
+
+// site-force output of the reciprocal-space-only path: out += sum of the k-chunk planes
+__global__ void k_sum_parts(EvalArgs a) {
+    const Job J = a.jobs[blockIdx.y];
+    const SysDev &S = a.sys[J.sys];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * S.n_sites) return;
+    double v = 0.0;
+    for (int p = 0; p < a.n_rj + a.n_kc; ++p) v += a.part[3 * ((size_t)p * a.total_sites + J.site_off) + t];
+    a.out[J.out_off + t] += v;
+}
+
+// FP32 FMA throughput probe: 8 independent dependent chains per thread.
+__global__ void __launch_bounds__(256) k_fp32_probe(float *out, int iters) {
+    float v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = 1.0f + 1e-7f * (threadIdx.x + k);
+    const float b = 0.9999999f, c = 1e-7f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = fmaf(v[k], b, c);
+    }
+    float t = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) t += v[k];
+    if (t == 12345.f) out[0] = t;  // keeps the chains live
 }
 
 template <typename R>
@@ -583,48 +729,37 @@ void set_attrs() {
     cudaFuncSetAttribute(k_kforce<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
 }
 
-template <typename R>
-void launch_ewald(const EvalArgs &a, cudaStream_t s, unsigned long long *n) {
-    const int ns = 3 * a.max_mols;
-    dim3 gs((ns + 127) / 128, a.n_jobs);
-    dim3 gk((a.max_kvec + KT - 1) / KT, a.n_jobs);
-    k_prep<R><<<gs, 128, 0, s>>>(a);
-    if (a.mode == 0) {
-        k_real<R, 0><<<dim3((ns + RT - 1) / RT, a.n_jobs), RT, 0, s>>>(a);
-        k_ksk<R, 0><<<gk, KT, ksk_smem<R>(a.max_kmax), s>>>(a);
-        k_kforce<R, 0><<<dim3((ns + FT - 1) / FT, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
-    } else {
-        k_real<R, 1><<<dim3((ns + RT - 1) / RT, a.n_jobs), RT, 0, s>>>(a);
-        k_ksk<R, 1><<<gk, KT, ksk_smem<R>(a.max_kmax), s>>>(a);
-        k_kforce<R, 1><<<dim3((ns + FT - 1) / FT, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
-    }
-    if (n) *n += 4;
+// Chunk counts so that each force kernel launches enough blocks to fill the GPU.
+int chunks_for(long long base_blocks, int maxc) {
+    const long long want = 4LL * 152;
+    const int c = (int)((want + base_blocks - 1) / std::max(1LL, base_blocks));
+    return std::max(1, std::min(c, maxc));
 }
 
-void launch_short_range(const EvalArgs &a, cudaStream_t s, unsigned long long *n) {
-    dim3 gm((a.max_mols + 127) / 128, a.n_jobs);
-    k_combine<<<gm, 128, 0, s>>>(a);
-    if (n) *n += 1;
+template <typename R>
+void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n) {
+    const int ns = 3 * a.max_mols;
+    const int tiles = (ns + RT - 1) / RT, ktiles = (a.max_kvec + KT - 1) / KT;
+    a.n_rj = chunks_for((long long)tiles * a.n_jobs, MAX_RJ);
+    a.n_sc = chunks_for((long long)ktiles * a.n_jobs, MAX_SC);
+    a.n_kc = chunks_for((long long)tiles * a.n_jobs, MAX_KC);
+    k_prep<R><<<dim3((ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
     if (a.mode == 0) {
-        k_lj<<<gm, 128, 0, s>>>(a);
+        k_real<R, 0><<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
+        k_ksk<R, 0><<<dim3(ktiles, a.n_sc, a.n_jobs), KT, ksk_smem<R>(a.max_kmax), s>>>(a);
+        k_kforce<R, 0><<<dim3(tiles, a.n_kc, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
+    } else {
+        k_real<R, 1><<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
+        k_ksk<R, 1><<<dim3(ktiles, a.n_sc, a.n_jobs), KT, ksk_smem<R>(a.max_kmax), s>>>(a);
+        k_kforce<R, 1><<<dim3(tiles, a.n_kc, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
+    }
+    const dim3 gm((a.max_mols + 127) / 128, a.n_jobs);
+    k_combine<R><<<gm, 128, 0, s>>>(a);
+    if (n) *n += 5;
+    if (a.mode == 0) {
+        k_lj<R><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
         if (n) *n += 1;
     }
-}
-
-// FP32 FMA throughput probe: 8 independent dependent chains per thread.
-__global__ void __launch_bounds__(256) k_fp32_probe(float *out, int iters) {
-    float a[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) a[k] = 1.0f + 1e-7f * (threadIdx.x + k);
-    const float b = 0.9999999f, c = 1e-7f;
-    for (int i = 0; i < iters; ++i) {
-#pragma unroll
-        for (int k = 0; k < 8; ++k) a[k] = fmaf(a[k], b, c);
-    }
-    float t = 0.f;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) t += a[k];
-    if (t == 12345.f) out[0] = t;  // keeps the chains live
 }
 
 }  // namespace
@@ -633,11 +768,16 @@ void launch_fp32_probe(float *out, int blocks, int iters, cudaStream_t s) {
     k_fp32_probe<<<blocks, 256, 0, s>>>(out, iters);
 }
 
-void launch_ewald_kernel(const EvalArgs &a, bool mixed, const char *name, cudaStream_t s) {
+void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaStream_t s) {
+    EvalArgs a = a0;
     const int ns = 3 * a.max_mols;
-    const dim3 gs((ns + 127) / 128, a.n_jobs), gr((ns + RT - 1) / RT, a.n_jobs);
-    const dim3 gk((a.max_kvec + KT - 1) / KT, a.n_jobs), gf((ns + FT - 1) / FT, a.n_jobs);
-    const dim3 gm((a.max_mols + 127) / 128, a.n_jobs);
+    const int tiles = (ns + RT - 1) / RT, ktiles = (a.max_kvec + KT - 1) / KT;
+    a.n_rj = chunks_for((long long)tiles * a.n_jobs, MAX_RJ);
+    a.n_sc = chunks_for((long long)ktiles * a.n_jobs, MAX_SC);
+    a.n_kc = chunks_for((long long)tiles * a.n_jobs, MAX_KC);
+    const dim3 gs((ns + 127) / 128, a.n_jobs), gr(tiles, a.n_rj, a.n_jobs);
+    const dim3 gk(ktiles, a.n_sc, a.n_jobs), gf(tiles, a.n_kc, a.n_jobs);
+    const dim3 gm((a.max_mols + 127) / 128, a.n_jobs), gl((a.max_mols + 3) / 4, a.n_jobs);
     const std::string n(name);
     if (n == "prep") {
         if (mixed) k_prep<float><<<gs, 128, 0, s>>>(a);
@@ -652,9 +792,11 @@ void launch_ewald_kernel(const EvalArgs &a, bool mixed, const char *name, cudaSt
         if (mixed) k_kforce<float, 0><<<gf, FT, kforce_smem<float>(a.max_kmax), s>>>(a);
         else k_kforce<double, 0><<<gf, FT, kforce_smem<double>(a.max_kmax), s>>>(a);
     } else if (n == "combine") {
-        k_combine<<<gm, 128, 0, s>>>(a);
+        if (mixed) k_combine<float><<<gm, 128, 0, s>>>(a);
+        else k_combine<double><<<gm, 128, 0, s>>>(a);
     } else if (n == "lj") {
-        k_lj<<<gm, 128, 0, s>>>(a);
+        if (mixed) k_lj<float><<<gl, 128, 0, s>>>(a);
+        else k_lj<double><<<gl, 128, 0, s>>>(a);
     }
 }
 
@@ -665,24 +807,37 @@ void init_force_kernel_attributes() {
 
 void launch_eval_fp64(const EvalArgs &a, cudaStream_t s, unsigned long long *n) {
     if (a.n_jobs <= 0) return;
-    if (!a.sr_only) launch_ewald<double>(a, s, n);
-    launch_short_range(a, s, n);
+    if (!a.sr_only) {
+        launch_ewald<double>(a, s, n);
+        return;
+    }
+    // short-range terms only (FP64): LJ reads the raw positions, no preparation pass
+    const dim3 gm((a.max_mols + 127) / 128, a.n_jobs);
+    k_combine<double><<<gm, 128, 0, s>>>(a);
+    k_lj<double><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
+    if (n) *n += 2;
 }
 
 void launch_eval_mixed(const EvalArgs &a, cudaStream_t s, unsigned long long *n) {
     if (a.n_jobs <= 0) return;
-    if (!a.sr_only) launch_ewald<float>(a, s, n);
-    launch_short_range(a, s, n);
+    if (a.sr_only) {
+        launch_eval_fp64(a, s, n);  // the finite-difference short-range terms stay FP64
+        return;
+    }
+    launch_ewald<float>(a, s, n);
 }
 
-// Reciprocal space only, on caller-supplied charge sites; site forces are
-// accumulated into a.site_force (which the caller pre-loads).
-void launch_kwald_only(const EvalArgs &a, bool mixed, cudaStream_t s, unsigned long long *n) {
-    if (a.n_jobs <= 0) return;
+// Reciprocal space only, on caller-supplied charge sites: out (site forces,
+// 9N per job) += k-space forces.
+void launch_kwald_only(const EvalArgs &a0, bool mixed, cudaStream_t s, unsigned long long *n) {
+    if (a0.n_jobs <= 0) return;
+    EvalArgs a = a0;
     const int ns = 3 * a.max_mols;
-    dim3 gs((ns + 127) / 128, a.n_jobs);
-    dim3 gk((a.max_kvec + KT - 1) / KT, a.n_jobs);
-    dim3 gf((ns + FT - 1) / FT, a.n_jobs);
+    const int tiles = (ns + FT - 1) / FT, ktiles = (a.max_kvec + KT - 1) / KT;
+    a.n_rj = 0;
+    a.n_sc = chunks_for((long long)ktiles * a.n_jobs, MAX_SC);
+    a.n_kc = chunks_for((long long)tiles * a.n_jobs, MAX_KC);
+    const dim3 gs((ns + 127) / 128, a.n_jobs), gk(ktiles, a.n_sc, a.n_jobs), gf(tiles, a.n_kc, a.n_jobs);
     if (mixed) {
         k_prep<float><<<gs, 128, 0, s>>>(a);
         k_ksk<float, 0><<<gk, KT, ksk_smem<float>(a.max_kmax), s>>>(a);
@@ -692,7 +847,8 @@ void launch_kwald_only(const EvalArgs &a, bool mixed, cudaStream_t s, unsigned l
         k_ksk<double, 0><<<gk, KT, ksk_smem<double>(a.max_kmax), s>>>(a);
         k_kforce<double, 0><<<gf, FT, kforce_smem<double>(a.max_kmax), s>>>(a);
     }
-    if (n) *n += 3;
+    k_sum_parts<<<dim3((3 * ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
+    if (n) *n += 4;
 }
 
 }  // namespace qtg

@@ -272,6 +272,12 @@ void launch_nm_energy(const SysDev *sys, int sysi, int P, int n_dof, const doubl
                       const double *mass, const ModeCoef *modes, double *out, cudaStream_t s,
                       unsigned long long *n);
 
+// Chunking limits of the force kernels' second grid dimension.
+constexpr int MAX_RJ = 8;    // real-space j-chunks
+constexpr int MAX_KC = 8;    // reciprocal-space k-chunks
+constexpr int MAX_SC = 8;    // structure-factor site chunks
+constexpr int MAX_PART = MAX_RJ + MAX_KC + 1;  // partial site-force planes
+
 struct EvalArgs {
     const SysDev *sys;     // device array
     const Job *jobs;       // device array, n_jobs entries
@@ -285,18 +291,21 @@ struct EvalArgs {
     const double *charge;
     const int *point, *list;
     const KVec *kvec;
-    void *sites;           // float4 or double4 per site, per slot
-    double *site_force;    // double[3] per site, per slot
-    void *phase;           // float2 or double2, per slot
-    double2 *sk;           // S(k), per slot
-    double2 *dsk;          // d S(k) along the tangent direction, per slot
+    void *sites;           // 4 reals per site (x, y, z, q), per slot
+    void *opos;            // wrapped oxygen positions, 4 reals per molecule, per slot
+    void *phase;           // complex phase tables, per slot
     void *tan_sites;       // tangent of the site positions (mode 1), per slot
-    double *energy;        // per job
+    double *part;          // partial site forces [MAX_PART][total_sites][3]
+    long long total_sites; // sites summed over all slots (plane stride of part)
+    double2 *skp;          // partial S(k) [MAX_SC][total_k]
+    double2 *dskp;         // partial dS(k) along the tangent direction
+    long long total_k;     // k-vectors summed over all slots (plane stride of skp)
+    double *energy;        // per slot
     unsigned *status;
-    int sites_are_input;   // 1: positions are charge sites (M,H1,H2) -> kwald only
-    int skip_short_range;  // 1: no LJ / intramolecular terms (kwald only)
-    int sr_only;           // 1: only the FP64 short-range terms (LJ, intramolecular,
-                           //    same-molecule Ewald); site forces are ignored
+    int n_rj, n_sc, n_kc;  // chunk counts, chosen by the launcher
+    int sites_are_input;   // 1: positions are charge sites (M,H1,H2) -> reciprocal space only
+    int sr_only;           // 1: only the short-range terms (LJ, intramolecular,
+                           //    same-molecule Ewald), in FP64; Ewald partials ignored
     int mode;              // 0 = forces, 1 = directional derivative of the Ewald forces
     Consts c;
 };

@@ -9,9 +9,12 @@ Tolerances:
   summation order by ~1e5, so 1e-8 relative RMS (the oracle, a reordered FP64
   sum, sits at ~5e-13 only because its order is close to the reference's);
 * mixed mode (FP32 Ewald, FP64 accumulation): 1e-4 relative RMS per-atom force
-  error, and an energy error below 1e-8 Hartree per molecule (the total is a
-  small difference of large Ewald terms, so a relative bound on it would
-  measure the cancellation, not the arithmetic).
+  error, and an energy error below 1e-6 of the Ewald self-energy
+  sum_i kappa q_i^2 / sqrt(pi) (the total is a small difference of Ewald terms
+  of that size, so a bound relative to the total would measure the
+  cancellation, not the arithmetic; FP32 site positions alone, with absolute
+  resolution ~4e-6 bohr in a 47-bohr box, perturb a 512-water Ewald energy by
+  ~1e-5 Hartree).
 """
 import numpy as np
 import pytest
@@ -27,11 +30,16 @@ PIMD = [c for c in CASES if c not in P1]
 TOL_FP64 = 1e-9
 TOL_SC_FP64 = 1e-8
 TOL_MIXED_F = 1e-4
-TOL_MIXED_E_PER_MOL = 1e-8  # Hartree
+TOL_MIXED_E_SELF = 1e-6  # relative to the Ewald self-energy
 
 
 def rel_rms(a, b):
     return float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2)))
+
+
+def ewald_self(s):
+    q = s.charges()
+    return float(np.sum(0.5 * 2.0 * s.info.kappa / np.sqrt(3.14159265359) * q * q))
 
 
 def make(g, precision, propagator=None):
@@ -83,7 +91,7 @@ def test_single_configuration_forces(gpu_lib, case, precision):
         assert err_f < TOL_FP64, err_f
         assert np.abs(f - g["forces"]).max() < TOL_FP64 * np.abs(g["forces"]).max()
     else:
-        assert np.abs(e - g["energies"]).max() / s.N < TOL_MIXED_E_PER_MOL
+        assert np.abs(e - g["energies"]).max() < TOL_MIXED_E_SELF * ewald_self(s)
         assert err_f < TOL_MIXED_F, err_f
 
 
@@ -113,7 +121,7 @@ def test_suzuki_chin_forces(gpu_lib, case, precision):
         assert rel_rms(fp, g["sc_fphys"]) < TOL_FP64
         assert rel_rms(f, g["sc_f"]) < TOL_SC_FP64
     else:
-        assert abs(e - float(g["sc_energy"])) / (s.N * s.P) <= TOL_MIXED_E_PER_MOL
+        assert abs(e - float(g["sc_energy"])) <= TOL_MIXED_E_SELF * ewald_self(s) * s.P
         assert rel_rms(fp, g["sc_fphys"]) < TOL_MIXED_F
         assert rel_rms(f, g["sc_f"]) < TOL_MIXED_F
 
