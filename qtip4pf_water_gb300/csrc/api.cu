@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -119,6 +120,64 @@ void nm_matrix(int P, std::vector<double> &C) {
         for (int b = 0; b < P; ++b) C[(size_t)(P / 2) * P + b] = sqrt(1.0 / P) * ((b % 2 == 0) ? 1.0 : -1.0);
 }
 
+// Reorder the k-vectors into columns of fixed (kx, ky) with contiguous kz in
+// [-m, m] (fillers with c_k = 0 where the reference's set has a hole), and
+// build the structure-factor groups (<= 8 kz of one column) and the force
+// batches (whole columns, <= 128 vectors).
+void build_columns(const std::vector<KVec> &kv, std::vector<KVec> &kord, std::vector<KCol> &cols,
+                   std::vector<KGroup> &grps, std::vector<KBatch> &bats) {
+    std::map<std::pair<int, int>, std::map<int, KVec>> by;
+    for (const KVec &v : kv) by[{v.kx, v.ky}][v.kz] = v;
+    for (auto &col : by) {
+        int m = 0;
+        for (auto &e : col.second) m = std::max(m, std::abs(e.first));
+        KCol c;
+        c.kx = col.first.first;
+        c.ky = col.first.second;
+        c.m = m;
+        c.k_begin = (int)kord.size();
+        for (int kz = -m; kz <= m; ++kz) {
+            auto it = col.second.find(kz);
+            if (it != col.second.end()) {
+                kord.push_back(it->second);
+            } else {
+                KVec f;
+                f.kx = c.kx;
+                f.ky = c.ky;
+                f.kz = kz;
+                f.pad = 0;
+                f.coef = f.gx = f.gy = f.gz = 0.0;
+                kord.push_back(f);
+            }
+        }
+        const int ci = (int)cols.size();
+        cols.push_back(c);
+        for (int kz0 = -m; kz0 <= m; kz0 += 8) {
+            KGroup g;
+            g.col = ci;
+            g.kz0 = kz0;
+            g.n = std::min(8, m - kz0 + 1);
+            g.pad = 0;
+            grps.push_back(g);
+        }
+    }
+    int c0 = 0;
+    while (c0 < (int)cols.size()) {
+        int c1 = c0, n = 0;
+        while (c1 < (int)cols.size() && n + 2 * cols[c1].m + 1 <= 128) {
+            n += 2 * cols[c1].m + 1;
+            ++c1;
+        }
+        KBatch b;
+        b.c0 = c0;
+        b.c1 = c1;
+        b.k0 = cols[c0].k_begin;
+        b.k1 = cols[c1 - 1].k_begin + 2 * cols[c1 - 1].m + 1;
+        bats.push_back(b);
+        c0 = c1;
+    }
+}
+
 struct Table {  // a device job table plus its host copy
     std::vector<Job> h;
     Job *d = nullptr;
@@ -151,6 +210,10 @@ struct qtg_ctx {
     double *noise = nullptr;  // per-call noise (2 + (Pmax-1) * 9Nmax)
     size_t noise_len = 0;
     KVec *kvec = nullptr;
+    KCol *kcol = nullptr;
+    KGroup *kgrp = nullptr;
+    KBatch *kbatch = nullptr;
+    int max_grp = 0, max_batch = 0;
     double *nm = nullptr;
     ModeCoef *modes = nullptr;
     // per-slot scratch
@@ -223,6 +286,11 @@ EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, d
     a.point = c->point;
     a.list = c->list;
     a.kvec = c->kvec;
+    a.kcol = c->kcol;
+    a.kgrp = c->kgrp;
+    a.kbatch = c->kbatch;
+    a.max_grp = c->max_grp;
+    a.max_batch = c->max_batch;
     a.sites = c->sites;
     a.opos = c->opos;
     a.phase = c->phase;
@@ -498,6 +566,9 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     ctx->desc.assign(systems, systems + n_systems);
     const Consts &K = ctx->K;
     std::vector<KVec> kall;
+    std::vector<KCol> call;
+    std::vector<KGroup> gall;
+    std::vector<KBatch> ball;
     std::vector<double> nm_all;
     std::vector<ModeCoef> mode_all;
     std::vector<double> chg_all, mass_all;
@@ -560,11 +631,27 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         S.r_skin_sq = K.r_skin_sq;
         S.skin_margin = K.r_skin - K.r_cut;
         S.c1_centroid = d.thermostat == QTG_THERMO_PILE_L ? exp(-S.dt / (d.tau0_fs * K.fs2au)) : 0.0;
-        std::vector<KVec> kv;
+        std::vector<KVec> kv, kord;
+        std::vector<KCol> cols;
+        std::vector<KGroup> grps;
+        std::vector<KBatch> bats;
         enumerate_k(S, kc * kc, kv);
-        S.n_kvec = (int)kv.size();
+        build_columns(kv, kord, cols, grps, bats);
+        S.n_kvec_ref = (int)kv.size();
+        S.n_kvec = (int)kord.size();
         S.kvec_off = (int)kall.size();
-        kall.insert(kall.end(), kv.begin(), kv.end());
+        S.col_off = (int)call.size();
+        S.n_col = (int)cols.size();
+        S.grp_off = (int)gall.size();
+        S.n_grp = (int)grps.size();
+        S.batch_off = (int)ball.size();
+        S.n_batch = (int)bats.size();
+        kall.insert(kall.end(), kord.begin(), kord.end());
+        call.insert(call.end(), cols.begin(), cols.end());
+        gall.insert(gall.end(), grps.begin(), grps.end());
+        ball.insert(ball.end(), bats.begin(), bats.end());
+        ctx->max_grp = std::max(ctx->max_grp, S.n_grp);
+        ctx->max_batch = std::max(ctx->max_batch, S.n_batch);
         ctx->kc_sq.push_back(kc * kc);
         S.q_off = q_off;
         S.d_off = d_off;
@@ -730,6 +817,9 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->sc_scale, ctx->total_slots);
     AL(ctx->noise, ctx->noise_len);
     AL(ctx->kvec, kall.size());
+    AL(ctx->kcol, call.size());
+    AL(ctx->kgrp, gall.size());
+    AL(ctx->kbatch, ball.size());
     AL(ctx->nm, nm_all.size());
     AL(ctx->modes, mode_all.size());
     {
@@ -781,6 +871,9 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     cp(ctx->charge, chg_all.data(), sizeof(double) * chg_all.size());
     cp(ctx->mass, mass_all.data(), sizeof(double) * mass_all.size());
     cp(ctx->kvec, kall.data(), sizeof(KVec) * kall.size());
+    cp(ctx->kcol, call.data(), sizeof(KCol) * call.size());
+    cp(ctx->kgrp, gall.data(), sizeof(KGroup) * gall.size());
+    cp(ctx->kbatch, ball.data(), sizeof(KBatch) * ball.size());
     cp(ctx->nm, nm_all.data(), sizeof(double) * nm_all.size());
     cp(ctx->modes, mode_all.data(), sizeof(ModeCoef) * mode_all.size());
     cp(ctx->base.d, ctx->base.h.data(), sizeof(Job) * ctx->base.h.size());
@@ -820,7 +913,7 @@ void qtg_destroy(qtg_ctx *ctx) {
         if (ctx->graph[i]) cudaGraphExecDestroy(ctx->graph[i]);
     void *ptrs[] = {ctx->sys_d, ctx->q, ctx->p, ctx->f, ctx->fphys, ctx->qdisp, ctx->fdisp, ctx->fsr,
                     ctx->dirv, ctx->stage, ctx->disp, ctx->point, ctx->list, ctx->charge, ctx->mass,
-                    ctx->sc_scale, ctx->noise, ctx->kvec, ctx->nm, ctx->modes, ctx->sites, ctx->tan_sites,
+                    ctx->sc_scale, ctx->noise, ctx->kvec, ctx->kcol, ctx->kgrp, ctx->kbatch, ctx->nm, ctx->modes, ctx->sites, ctx->tan_sites,
                     ctx->phase, ctx->opos, ctx->part, ctx->skp, ctx->dskp, ctx->energy, ctx->energy_aux,
                     ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
@@ -845,7 +938,7 @@ qtg_status qtg_system_info_get(const qtg_ctx *ctx, int sys, qtg_system_info *out
     out->n_dof = S.n_dof;
     out->list_size = S.list_size;
     out->k_max = S.k_max;
-    out->n_kvectors = S.n_kvec;
+    out->n_kvectors = S.n_kvec_ref;
     out->kappa = S.kappa;
     out->rc = sqrt(S.rc_sq);
     out->kc = sqrt(ctx->kc_sq[sys]);

@@ -64,6 +64,29 @@ template <> __device__ __forceinline__ double sys_ibox<double>(const SysDev &S, 
 
 __device__ __forceinline__ int chunk_lo(int n, int c, int nc) { return (int)(((long long)n * c) / nc); }
 
+// Real-space pair kernel pieces. For FP32: 1/r from rsqrtf, exp(-x^2) from the
+// exp2 unit, and erfc(x) = t P(t) exp(-x^2), t = 1 / (1 + p x), the rational
+// approximation of Abramowitz & Stegun, Handbook of Mathematical Functions,
+// eq. 7.1.26 (absolute error <= 1.5e-7), which reuses the Gaussian the force
+// needs anyway. For FP64 the library functions are used.
+__device__ __forceinline__ void pair_terms(float r2, float kap, float kap2, float *inv, float *ex, float *ec) {
+    const float iv = rsqrtf(r2);
+    const float x = kap * (r2 * iv);
+    const float e = exp2f(-kap2 * r2 * 1.4426950408889634f);
+    const float t = __frcp_rn(fmaf(0.3275911f, x, 1.0f));
+    const float p = fmaf(fmaf(fmaf(fmaf(1.061405429f, t, -1.453152027f), t, 1.421413741f), t, -0.284496736f), t,
+                         0.254829592f);
+    *inv = iv;
+    *ex = e;
+    *ec = t * p * e;
+}
+__device__ __forceinline__ void pair_terms(double r2, double kap, double kap2, double *inv, double *ex, double *ec) {
+    const double r = sqrt(r2);
+    *inv = 1.0 / r;
+    *ex = exp(-kap2 * r2);
+    *ec = erfc(kap * r);
+}
+
 // ---- k_prep -------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(128) k_prep(EvalArgs a) {
@@ -183,7 +206,7 @@ __global__ void __launch_bounds__(RT) k_real(EvalArgs a) {
         si = sites[i];
         if (MODE == 1) ui = tans[i];
     }
-    const int mi = i / 3;
+    const int mlo = (i / 3) * 3;  // first site of i's molecule
     double Fx = 0.0, Fy = 0.0, Fz = 0.0, E = 0.0;
     for (int t0 = j0; t0 < j1; t0 += RT) {
         __syncthreads();
@@ -196,7 +219,7 @@ __global__ void __launch_bounds__(RT) k_real(EvalArgs a) {
         R fx = 0, fy = 0, fz = 0, e = 0;
         if (act) {
             for (int jj = 0; jj < nj; ++jj) {
-                if ((t0 + jj) / 3 == mi) continue;
+                if ((unsigned)(t0 + jj - mlo) < 3u) continue;  // same molecule
                 const V4<R> b = sj[jj];
                 R dx = si.x - b.x, dy = si.y - b.y, dz = si.z - b.z;
                 dx -= L0 * f_rint(dx * I0);
@@ -204,11 +227,10 @@ __global__ void __launch_bounds__(RT) k_real(EvalArgs a) {
                 dz -= L2 * f_rint(dz * I2);
                 const R r2 = dx * dx + dy * dy + dz * dz;
                 if (r2 < rc2) {
-                    const R r = f_sqrt(r2);
-                    const R inv = (R)1 / r;
+                    R inv, ex, ec;
+                    pair_terms(r2, kap, kap2, &inv, &ex, &ec);
                     const R qq = si.w * b.w;
-                    const R ex = f_exp(-kap2 * r2);
-                    const R en = qq * inv * f_erfc(kap * r);
+                    const R en = qq * inv * ec;
                     const R hq = qq * pref * ex;
                     const R phi = (en + hq) * inv * inv;
                     if (MODE == 0) {
@@ -249,35 +271,53 @@ __global__ void __launch_bounds__(RT) k_real(EvalArgs a) {
 }
 
 // ---- k_ksk: structure factors ---------------------------------------------------
-constexpr int KT = 128;  // threads (k-vectors) per block
+// One thread per group of <= 8 consecutive kz of one (kx, ky) column; the
+// column factor X(kx) Y(ky) of a site is formed once and multiplied by the
+// group's Z(kz). Sites are staged through shared memory in chunks of CH; each
+// chunk's partial sums (registers, working precision) are added to FP64 running
+// sums kept in shared memory.
+constexpr int KT = 128;  // threads (k groups) per block
 constexpr int CH = 32;   // sites per shared-memory chunk
+constexpr int KG = 8;    // kz per group
 
 template <typename R, int MODE>
 __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
     const int sc = blockIdx.y, jb = blockIdx.z;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
-    const int nk = S.n_kvec, ns = S.n_sites, km1 = S.k_max + 1;
-    if (blockIdx.x * KT >= nk) return;
+    const int ng = S.n_grp, ns = S.n_sites, km1 = S.k_max + 1;
+    if (blockIdx.x * KT >= ng) return;
     const int t = blockIdx.x * KT + threadIdx.x;
-    const bool act = t < nk;
+    const bool act = t < ng;
     const int s0 = chunk_lo(ns, sc, a.n_sc), s1 = chunk_lo(ns, sc + 1, a.n_sc);
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    // 16-byte elements first so every array stays aligned for vector access
-    V4<R> *ush = reinterpret_cast<V4<R> *>(smem_raw);  // [CH] (mode 1)
-    V2<R> *tab = reinterpret_cast<V2<R> *>(ush + CH);  // [3*km1][CH+1]
-    KVec kv;
-    kv.kx = kv.ky = kv.kz = 0;
-    kv.coef = 0.0;
-    if (act) kv = a.kvec[S.kvec_off + t];
-    const int ax = kv.kx, ay = abs(kv.ky), az = abs(kv.kz);
-    const R sy = kv.ky < 0 ? (R)-1 : (R)1, sz = kv.kz < 0 ? (R)-1 : (R)1;
-    const R kx = (R)(2.0 * PI_REF * kv.kx * S.inv_box[0]);
-    const R ky = (R)(2.0 * PI_REF * kv.ky * S.inv_box[1]);
-    const R kz = (R)(2.0 * PI_REF * kv.kz * S.inv_box[2]);
+    double2 *acc = reinterpret_cast<double2 *>(smem_raw);                // [(MODE+1)*KG][KT]
+    V4<R> *ush = reinterpret_cast<V4<R> *>(acc + (MODE + 1) * KG * KT);  // [CH] (mode 1)
+    V2<R> *tab = reinterpret_cast<V2<R> *>(ush + CH);                    // [3*km1][CH+1]
+    for (int g = 0; g < (MODE + 1) * KG; ++g) acc[g * KT + threadIdx.x] = make_double2(0.0, 0.0);
+    KGroup G;
+    G.col = G.kz0 = G.n = 0;
+    KCol C;
+    C.kx = C.ky = C.m = C.k_begin = 0;
+    if (act) {
+        G = a.kgrp[S.grp_off + t];
+        C = a.kcol[S.col_off + G.col];
+    }
+    const int ax = C.kx, ay = abs(C.ky);
+    const R sy = C.ky < 0 ? (R)-1 : (R)1;
+    const R bz = (R)(2.0 * PI_REF * S.inv_box[2]);
+    const R kx = (R)(2.0 * PI_REF * C.kx * S.inv_box[0]), ky = (R)(2.0 * PI_REF * C.ky * S.inv_box[1]);
+    int zrow[KG];
+    R zsg[KG], kzr[KG];
+#pragma unroll
+    for (int g = 0; g < KG; ++g) {
+        const int kz = G.kz0 + g;
+        zrow[g] = (2 * km1 + min(abs(kz), km1 - 1)) * (CH + 1);
+        zsg[g] = kz < 0 ? (R)-1 : (R)1;
+        kzr[g] = bz * (R)kz;
+    }
     const V2<R> *ph = reinterpret_cast<const V2<R> *>(a.phase) + J.phase_off;
     const V4<R> *tans = reinterpret_cast<const V4<R> *>(a.tan_sites) + J.site_off;
-    double Sr = 0.0, Si = 0.0, dSr = 0.0, dSi = 0.0;
     const int rows = 3 * km1;
     for (int c0 = s0; c0 < s1; c0 += CH) {
         __syncthreads();
@@ -295,135 +335,172 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
         }
         __syncthreads();
         const int nc = min(CH, s1 - c0);
-        R sr = 0, si = 0, dsr = 0, dsi = 0;
-        const V2<R> *X = tab + ax * (CH + 1);
-        const V2<R> *Y = tab + (km1 + ay) * (CH + 1);
-        const V2<R> *Z = tab + (2 * km1 + az) * (CH + 1);
+        R sr[KG], si[KG], dsr[KG], dsi[KG];
+#pragma unroll
+        for (int g = 0; g < KG; ++g) sr[g] = si[g] = dsr[g] = dsi[g] = (R)0;
         for (int c = 0; c < nc; ++c) {
-            const V2<R> x = X[c], y = Y[c], z = Z[c];
-            const R yi = sy * y.y, zi = sz * z.y;
+            const V2<R> x = tab[ax * (CH + 1) + c], y = tab[(km1 + ay) * (CH + 1) + c];
+            const R yi = sy * y.y;
             const R pr = x.x * y.x - x.y * yi, pi = x.x * yi + x.y * y.x;
-            const R er = pr * z.x - pi * zi, ei = pr * zi + pi * z.x;
-            sr += er;
-            si += ei;
+            R kxyu = (R)0, uz = (R)0;
             if (MODE == 1) {
                 const V4<R> u = ush[c];
-                const R ku = kx * u.x + ky * u.y + kz * u.z;
-                dsr -= ku * ei;
-                dsi += ku * er;
+                kxyu = kx * u.x + ky * u.y;
+                uz = u.z;
+            }
+#pragma unroll
+            for (int g = 0; g < KG; ++g) {
+                const V2<R> z = tab[zrow[g] + c];
+                const R zi = zsg[g] * z.y;
+                const R er = pr * z.x - pi * zi, ei = pr * zi + pi * z.x;
+                sr[g] += er;
+                si[g] += ei;
+                if (MODE == 1) {
+                    const R ku = kxyu + kzr[g] * uz;
+                    dsr[g] -= ku * ei;
+                    dsi[g] += ku * er;
+                }
             }
         }
-        Sr += (double)sr;
-        Si += (double)si;
-        if (MODE == 1) {
-            dSr += (double)dsr;
-            dSi += (double)dsi;
+#pragma unroll
+        for (int g = 0; g < KG; ++g) {
+            double2 v = acc[g * KT + threadIdx.x];
+            v.x += (double)sr[g];
+            v.y += (double)si[g];
+            acc[g * KT + threadIdx.x] = v;
+            if (MODE == 1) {
+                double2 d = acc[(KG + g) * KT + threadIdx.x];
+                d.x += (double)dsr[g];
+                d.y += (double)dsi[g];
+                acc[(KG + g) * KT + threadIdx.x] = d;
+            }
         }
     }
     if (act) {
-        const size_t at = (size_t)sc * a.total_k + J.sk_off + t;
-        a.skp[at] = make_double2(Sr, Si);
-        if (MODE == 1) a.dskp[at] = make_double2(dSr, dSi);
+        for (int g = 0; g < G.n; ++g) {
+            const size_t at = (size_t)sc * a.total_k + J.sk_off + C.k_begin + (G.kz0 + g + C.m);
+            a.skp[at] = acc[g * KT + threadIdx.x];
+            if (MODE == 1) a.dskp[at] = acc[(KG + g) * KT + threadIdx.x];
+        }
     }
 }
 
 // ---- k_kforce: reciprocal-space site forces -------------------------------------
+// One thread per site; the block walks batches of whole k columns. Per batch
+// the vectors' 2 c_k S(k) (and 2 c_k dS(k)) are summed over the structure-factor
+// partials and staged in shared memory; per column a site forms X(kx) Y(ky)
+// once, then for each kz the value v = Im(conj(2 c_k S) e_i), accumulating
+// sum_kz v and sum_kz kz v: since kx and ky are constant along a column,
+// F_x = b_x kx sum v, F_y = b_y ky sum v, F_z = b_z sum kz v.
 constexpr int FT = 128;  // threads (sites) per block
-constexpr int KC = 128;  // k-vectors per shared-memory chunk
+constexpr int KB = 128;  // k-vectors per batch (at most)
 
 template <typename R, int MODE>
 __global__ void __launch_bounds__(FT) k_kforce(EvalArgs a) {
     const int kc = blockIdx.y, jb = blockIdx.z;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
-    const int nk = S.n_kvec, ns = S.n_sites, km1 = S.k_max + 1;
+    const int nb = S.n_batch, ns = S.n_sites, km1 = S.k_max + 1;
     if (blockIdx.x * FT >= ns) return;
     const int i = blockIdx.x * FT + threadIdx.x;
     const bool act = i < ns;
-    const int k0 = chunk_lo(nk, kc, a.n_kc), k1 = chunk_lo(nk, kc + 1, a.n_kc);
+    const int bt0 = chunk_lo(nb, kc, a.n_kc), bt1 = chunk_lo(nb, kc + 1, a.n_kc);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     // 16-byte elements first so every array stays aligned for vector access
-    int4 *kk = reinterpret_cast<int4 *>(smem_raw);   // [KC]
-    V4<R> *gg = reinterpret_cast<V4<R> *>(kk + KC);  // [KC]
-    V2<R> *ss = reinterpret_cast<V2<R> *>(gg + KC);  // [KC]
-    V2<R> *ds = ss + KC;                             // [KC]
-    V2<R> *myph = ds + KC;                           // [3*km1][FT]
+    KCol *cs = reinterpret_cast<KCol *>(smem_raw);  // [KB]
+    V2<R> *ss = reinterpret_cast<V2<R> *>(cs + KB);  // [KB] 2 c_k S(k)
+    V2<R> *ds = ss + KB;                             // [KB] 2 c_k dS(k)
+    V2<R> *zr = ds + KB;                             // [km1][FT] my Z(kz) row
     __shared__ double red[FT / 32];
     const V2<R> *ph = reinterpret_cast<const V2<R> *>(a.phase) + J.phase_off;
-    for (int row = 0; row < 3 * km1; ++row) {
+    for (int m = 0; m < km1; ++m) {
         V2<R> v;
         v.x = v.y = (R)0;
-        if (act) v = ph[(size_t)row * ns + i];
-        myph[row * FT + threadIdx.x] = v;
+        if (act) v = ph[(size_t)(2 * km1 + m) * ns + i];
+        zr[m * FT + threadIdx.x] = v;
     }
     V4<R> ui;
     ui.x = ui.y = ui.z = ui.w = (R)0;
     if (MODE == 1 && act) ui = reinterpret_cast<const V4<R> *>(a.tan_sites)[J.site_off + i];
-    const R b0 = (R)(2.0 * PI_REF * S.inv_box[0]), b1 = (R)(2.0 * PI_REF * S.inv_box[1]),
-            b2 = (R)(2.0 * PI_REF * S.inv_box[2]);
+    const R bx = (R)(2.0 * PI_REF * S.inv_box[0]), by = (R)(2.0 * PI_REF * S.inv_box[1]),
+            bz = (R)(2.0 * PI_REF * S.inv_box[2]);
     const bool do_energy = (MODE == 0) && blockIdx.x == 0;
     double Fx = 0.0, Fy = 0.0, Fz = 0.0, E = 0.0;
-    for (int c0 = k0; c0 < k1; c0 += KC) {
+    const int ii = act ? i : 0;
+    for (int bt = bt0; bt < bt1; ++bt) {
+        const KBatch B = a.kbatch[S.batch_off + bt];
         __syncthreads();
-        for (int idx = threadIdx.x; idx < KC; idx += FT) {
-            const int k = c0 + idx;
-            if (k < k1) {
-                const KVec v = a.kvec[S.kvec_off + k];
-                kk[idx] = make_int4(v.kx, abs(v.ky), abs(v.kz), (v.ky < 0 ? 1 : 0) | (v.kz < 0 ? 2 : 0));
-                V4<R> g;
-                g.x = (R)v.gx;
-                g.y = (R)v.gy;
-                g.z = (R)v.gz;
-                g.w = (R)0;
-                gg[idx] = g;
-                double sr = 0.0, si = 0.0, dr = 0.0, di = 0.0;
-                for (int sc = 0; sc < a.n_sc; ++sc) {
-                    const size_t at = (size_t)sc * a.total_k + J.sk_off + k;
-                    const double2 p = a.skp[at];
-                    sr += p.x;
-                    si += p.y;
-                    if (MODE == 1) {
-                        const double2 d = a.dskp[at];
-                        dr += d.x;
-                        di += d.y;
-                    }
-                }
-                if (do_energy) E += v.coef * (sr * sr + si * si);
-                V2<R> s2;
-                s2.x = (R)sr;
-                s2.y = (R)si;
-                ss[idx] = s2;
+        for (int idx = threadIdx.x; idx < B.c1 - B.c0; idx += FT) cs[idx] = a.kcol[S.col_off + B.c0 + idx];
+        for (int idx = threadIdx.x; idx < B.k1 - B.k0; idx += FT) {
+            const int k = B.k0 + idx;
+            const double w = 2.0 * a.kvec[S.kvec_off + k].coef;
+            double sr = 0.0, si = 0.0, dr = 0.0, di = 0.0;
+            for (int sc = 0; sc < a.n_sc; ++sc) {
+                const size_t at = (size_t)sc * a.total_k + J.sk_off + k;
+                const double2 p = a.skp[at];
+                sr += p.x;
+                si += p.y;
                 if (MODE == 1) {
-                    V2<R> d2;
-                    d2.x = (R)dr;
-                    d2.y = (R)di;
-                    ds[idx] = d2;
+                    const double2 d = a.dskp[at];
+                    dr += d.x;
+                    di += d.y;
                 }
+            }
+            if (do_energy) E += 0.5 * w * (sr * sr + si * si);
+            V2<R> s2;
+            s2.x = (R)(w * sr);
+            s2.y = (R)(w * si);
+            ss[idx] = s2;
+            if (MODE == 1) {
+                V2<R> d2;
+                d2.x = (R)(w * dr);
+                d2.y = (R)(w * di);
+                ds[idx] = d2;
             }
         }
         __syncthreads();
-        const int nc = min(KC, k1 - c0);
         R fx = 0, fy = 0, fz = 0;
-        for (int c = 0; c < nc; ++c) {
-            const int4 k = kk[c];
-            const V2<R> x = myph[k.x * FT + threadIdx.x];
-            const V2<R> y = myph[(km1 + k.y) * FT + threadIdx.x];
-            const V2<R> z = myph[(2 * km1 + k.z) * FT + threadIdx.x];
-            const R yi = (k.w & 1) ? -y.y : y.y, zi = (k.w & 2) ? -z.y : z.y;
+        for (int cc = 0; cc < B.c1 - B.c0; ++cc) {
+            const KCol C = cs[cc];
+            const V2<R> x = ph[(size_t)C.kx * ns + ii];
+            const V2<R> y = ph[(size_t)(km1 + abs(C.ky)) * ns + ii];
+            const R yi = C.ky < 0 ? -y.y : y.y;
             const R pr = x.x * y.x - x.y * yi, pi = x.x * yi + x.y * y.x;
-            const R er = pr * z.x - pi * zi, ei = pr * zi + pi * z.x;
-            const V2<R> sk = ss[c];
-            R val = sk.x * ei - sk.y * er;  // q_i Im(conj(S) e_i)
-            if (MODE == 1) {
-                const V2<R> d = ds[c];
-                const R sgy = (k.w & 1) ? (R)-1 : (R)1, sgz = (k.w & 2) ? (R)-1 : (R)1;
-                const R ku = b0 * (R)k.x * ui.x + b1 * sgy * (R)k.y * ui.y + b2 * sgz * (R)k.z * ui.z;
-                val = (d.x * ei - d.y * er) + ku * (sk.x * er + sk.y * ei);
+            R kxyu = (R)0;
+            if (MODE == 1) kxyu = bx * (R)C.kx * ui.x + by * (R)C.ky * ui.y;
+            const int kb = C.k_begin - B.k0 + C.m;  // smem index of kz = 0
+            R v = 0, vz = 0;
+            // kz = -m .. -1 (Z conjugated), then kz = 0 .. m
+            for (int az = C.m; az >= 1; --az) {
+                const V2<R> z = zr[az * FT + threadIdx.x];
+                const R zi = -z.y;
+                const R er = pr * z.x - pi * zi, ei = pr * zi + pi * z.x;
+                const V2<R> sk = ss[kb - az];
+                R val = sk.x * ei - sk.y * er;
+                if (MODE == 1) {
+                    const V2<R> d = ds[kb - az];
+                    const R ku = kxyu - bz * (R)az * ui.z;
+                    val = (d.x * ei - d.y * er) + ku * (sk.x * er + sk.y * ei);
+                }
+                v += val;
+                vz -= (R)az * val;
             }
-            const V4<R> g = gg[c];
-            fx += val * g.x;
-            fy += val * g.y;
-            fz += val * g.z;
+            for (int az = 0; az <= C.m; ++az) {
+                const V2<R> z = zr[az * FT + threadIdx.x];
+                const R er = pr * z.x - pi * z.y, ei = pr * z.y + pi * z.x;
+                const V2<R> sk = ss[kb + az];
+                R val = sk.x * ei - sk.y * er;
+                if (MODE == 1) {
+                    const V2<R> d = ds[kb + az];
+                    const R ku = kxyu + bz * (R)az * ui.z;
+                    val = (d.x * ei - d.y * er) + ku * (sk.x * er + sk.y * ei);
+                }
+                v += val;
+                vz += (R)az * val;
+            }
+            fx += bx * (R)C.kx * v;
+            fy += by * (R)C.ky * v;
+            fz += bz * vz;
         }
         Fx += (double)fx;
         Fy += (double)fy;
@@ -713,11 +790,11 @@ __global__ void __launch_bounds__(256) k_fp32_probe(float *out, int iters) {
 
 template <typename R>
 size_t ksk_smem(int kmax) {
-    return (size_t)3 * (kmax + 1) * (CH + 1) * sizeof(V2<R>) + CH * sizeof(V4<R>);
+    return (size_t)2 * KG * KT * sizeof(double2) + CH * sizeof(V4<R>) + (size_t)3 * (kmax + 1) * (CH + 1) * sizeof(V2<R>);
 }
 template <typename R>
 size_t kforce_smem(int kmax) {
-    return (size_t)3 * (kmax + 1) * FT * sizeof(V2<R>) + KC * (sizeof(int4) + sizeof(V4<R>) + 2 * sizeof(V2<R>));
+    return (size_t)KB * (sizeof(KCol) + 2 * sizeof(V2<R>)) + (size_t)(kmax + 1) * FT * sizeof(V2<R>);
 }
 
 template <typename R>
@@ -729,9 +806,10 @@ void set_attrs() {
     cudaFuncSetAttribute(k_kforce<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
 }
 
-// Chunk counts so that each force kernel launches enough blocks to fill the GPU.
+// Chunk counts so that each force kernel launches enough 4-warp blocks to keep
+// 12 blocks (48 warps) resident on each of the 152 SMs.
 int chunks_for(long long base_blocks, int maxc) {
-    const long long want = 4LL * 152;
+    const long long want = 12LL * 152;
     const int c = (int)((want + base_blocks - 1) / std::max(1LL, base_blocks));
     return std::max(1, std::min(c, maxc));
 }
@@ -739,7 +817,7 @@ int chunks_for(long long base_blocks, int maxc) {
 template <typename R>
 void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n) {
     const int ns = 3 * a.max_mols;
-    const int tiles = (ns + RT - 1) / RT, ktiles = (a.max_kvec + KT - 1) / KT;
+    const int tiles = (ns + RT - 1) / RT, ktiles = (a.max_grp + KT - 1) / KT;
     a.n_rj = chunks_for((long long)tiles * a.n_jobs, MAX_RJ);
     a.n_sc = chunks_for((long long)ktiles * a.n_jobs, MAX_SC);
     a.n_kc = chunks_for((long long)tiles * a.n_jobs, MAX_KC);
@@ -771,7 +849,7 @@ void launch_fp32_probe(float *out, int blocks, int iters, cudaStream_t s) {
 void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaStream_t s) {
     EvalArgs a = a0;
     const int ns = 3 * a.max_mols;
-    const int tiles = (ns + RT - 1) / RT, ktiles = (a.max_kvec + KT - 1) / KT;
+    const int tiles = (ns + RT - 1) / RT, ktiles = (a.max_grp + KT - 1) / KT;
     a.n_rj = chunks_for((long long)tiles * a.n_jobs, MAX_RJ);
     a.n_sc = chunks_for((long long)ktiles * a.n_jobs, MAX_SC);
     a.n_kc = chunks_for((long long)tiles * a.n_jobs, MAX_KC);
@@ -833,7 +911,7 @@ void launch_kwald_only(const EvalArgs &a0, bool mixed, cudaStream_t s, unsigned 
     if (a0.n_jobs <= 0) return;
     EvalArgs a = a0;
     const int ns = 3 * a.max_mols;
-    const int tiles = (ns + FT - 1) / FT, ktiles = (a.max_kvec + KT - 1) / KT;
+    const int tiles = (ns + FT - 1) / FT, ktiles = (a.max_grp + KT - 1) / KT;
     a.n_rj = 0;
     a.n_sc = chunks_for((long long)ktiles * a.n_jobs, MAX_SC);
     a.n_kc = chunks_for((long long)tiles * a.n_jobs, MAX_KC);

@@ -44,7 +44,14 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
     double *Cm = sh;
     double *Xq = Cm + P * P;
     double *Xp = Xq + P * C;
+    double *Zq = Xp + P * C;  // folded sums / differences, then back-transformed values
+    double *Zp = Zq + P * C;
     __shared__ double red[8];
+    // Rows 0..P/2 of C are symmetric in b <-> P-b and rows P/2+1..P-1 are
+    // antisymmetric (zero at b = 0 and b = P/2), so each transform is applied to
+    // s_b = x_b + x_{P-b} and d_b = x_b - x_{P-b}, b = 1..h: half the FMAs.
+    const int h = (P - 1) / 2, half = P / 2;
+    const bool even = (P % 2) == 0;
     if (flags & (RF_FWD | RF_BACK))
         for (int t = threadIdx.x; t < P * P; t += blockDim.x) Cm[t] = a.nm[S.nm_off + t];
     const long long at = S.q_off + (long long)k * S.n_dof + col;
@@ -63,12 +70,36 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
             Xp[k * C + c] = pb;
         }
         __syncthreads();
+        if (k >= 1 && k <= h) {
+            const double aq = Xq[k * C + c], bq = Xq[(P - k) * C + c];
+            const double ap = Xp[k * C + c], bp = Xp[(P - k) * C + c];
+            Zq[(k - 1) * C + c] = aq + bq;
+            Zq[(h + k - 1) * C + c] = aq - bq;
+            Zp[(k - 1) * C + c] = ap + bp;
+            Zp[(h + k - 1) * C + c] = ap - bp;
+        }
+        __syncthreads();
         if (act) {
-            double sq = 0.0, sp = 0.0;
             const double *row = Cm + k * P;
-            for (int b = 0; b < P; ++b) {
-                sq += row[b] * Xq[b * C + c];
-                sp += row[b] * Xp[b * C + c];
+            double sq, sp;
+            if (k <= half) {  // symmetric row
+                sq = row[0] * Xq[c];
+                sp = row[0] * Xp[c];
+                if (even && half > 0 && k <= half) {
+                    sq += row[half] * Xq[half * C + c];
+                    sp += row[half] * Xp[half * C + c];
+                }
+                for (int b = 1; b <= h; ++b) {
+                    sq += row[b] * Zq[(b - 1) * C + c];
+                    sp += row[b] * Zp[(b - 1) * C + c];
+                }
+            } else {  // antisymmetric row
+                sq = 0.0;
+                sp = 0.0;
+                for (int b = 1; b <= h; ++b) {
+                    sq += row[b] * Zq[(h + b - 1) * C + c];
+                    sp += row[b] * Zp[(h + b - 1) * C + c];
+                }
             }
             yq = sq;
             yp = sp;
@@ -131,15 +162,33 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
             Xp[k * C + c] = yp;
         }
         __syncthreads();
-        if (act) {
-            double sq = 0.0, sp = 0.0;
-            for (int j = 0; j < P; ++j) {
-                const double cj = Cm[j * P + k];
-                sq += cj * Xq[j * C + c];
-                sp += cj * Xp[j * C + c];
+        // thread b <= P/2 forms A_b (symmetric rows) and B_b (antisymmetric rows);
+        // x_b = A_b + B_b and x_{P-b} = A_b - B_b
+        if (k <= half && k < P && c < W.ncols) {
+            double aq = Cm[k] * Xq[c], ap = Cm[k] * Xp[c];
+            if (even && half > 0) {
+                aq += Cm[half * P + k] * Xq[half * C + c];
+                ap += Cm[half * P + k] * Xp[half * C + c];
             }
-            qn = sq;
-            pn = sp;
+            double bq = 0.0, bp = 0.0;
+            for (int j = 1; j <= h; ++j) {
+                const double cs = Cm[j * P + k], sn = Cm[(P - j) * P + k];
+                aq += cs * Xq[j * C + c];
+                ap += cs * Xp[j * C + c];
+                bq += sn * Xq[(P - j) * C + c];
+                bp += sn * Xp[(P - j) * C + c];
+            }
+            Zq[k * C + c] = aq + bq;
+            Zp[k * C + c] = ap + bp;
+            if (k > 0 && 2 * k != P) {
+                Zq[(P - k) * C + c] = aq - bq;
+                Zp[(P - k) * C + c] = ap - bp;
+            }
+        }
+        __syncthreads();
+        if (act) {
+            qn = Zq[k * C + c];
+            pn = Zp[k * C + c];
         }
     }
     if (act) {
@@ -437,8 +486,8 @@ void launch_nm_energy(const SysDev *sys, int sysi, int P, int n_dof, const doubl
 
 void launch_ring(const RingArgs &a, cudaStream_t s, unsigned long long *n) {
     if (a.n_work <= 0) return;
-    // shared memory: P^2 + 2 P C doubles, with P C <= 256
-    size_t smem = (size_t)(a.max_p * a.max_p + 2 * 256) * sizeof(double);
+    // shared memory: P^2 + 4 P C doubles, with P C <= 256
+    size_t smem = (size_t)(a.max_p * a.max_p + 4 * 256) * sizeof(double);
     k_ring<<<a.n_work, 256, smem, s>>>(a);
     if (n) ++*n;
 }

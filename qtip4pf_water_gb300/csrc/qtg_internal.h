@@ -23,6 +23,8 @@ struct Consts {
 struct SysDev {
     int n_mols, n_beads, n_sites, n_dof, list_size, k_max, n_kvec, kvec_off;
     int propagator, thermostat, job_base, cols_per_block;
+    int n_kvec_ref;              // the reference's k-vector count (n_kvec includes c_k = 0 fillers)
+    int col_off, n_col, grp_off, n_grp, batch_off, n_batch, pad1;
     long long nm_off;   // doubles: P x P bead->normal-mode matrix C (y = C x)
     long long mode_off; // ModeCoef entries: P per system
     long long q_off;    // doubles: system block [P][9N] in q/p/f/fphys/aux arrays
@@ -55,6 +57,21 @@ struct ModeCoef {
 struct KVec {
     int kx, ky, kz, pad;
     double coef, gx, gy, gz;
+};
+
+// Reciprocal-space vectors are stored in columns of fixed (kx, ky) with kz
+// running over [-m, m]; points of a column outside the reference's set carry
+// c_k = 0. A column's vectors are contiguous in the KVec table.
+struct KCol {
+    int kx, ky, m, k_begin;
+};
+// Structure-factor work item: up to 8 consecutive kz of one column.
+struct KGroup {
+    int col, kz0, n, pad;
+};
+// Reciprocal-force work item: whole columns [c0, c1) holding k in [k0, k1), k1 - k0 <= 128.
+struct KBatch {
+    int c0, c1, k0, k1;
 };
 
 // One force evaluation ("job"): one configuration of one system.
@@ -291,6 +308,10 @@ struct EvalArgs {
     const double *charge;
     const int *point, *list;
     const KVec *kvec;
+    const KCol *kcol;
+    const KGroup *kgrp;
+    const KBatch *kbatch;
+    int max_grp, max_batch;
     void *sites;           // 4 reals per site (x, y, z, q), per slot
     void *opos;            // wrapped oxygen positions, 4 reals per molecule, per slot
     void *phase;           // complex phase tables, per slot
