@@ -301,7 +301,8 @@ def roofline(q, st, mix):
     s = make_system(q, q.MIXED, q.TROTTER, st)
     info = s.info
     nreal, nlj = count_pairs(st.q, st.box_bohr, info.rc ** 2, N_MOLS)
-    ms = {k: s.ctx.time_kernel(k, 20) for k in ("prep", "real", "ksk", "kforce", "combine", "lj", "ring", "end_step")}
+    ms = {k: s.ctx.time_kernel(k, 20)
+          for k in ("prep", "real", "ksk", "sk_reduce", "kforce", "combine", "lj", "ring", "end_step", "rebuild")}
     P, ns = N_BEADS, 3 * N_MOLS
     flop = {"real": 2 * nreal * FLOP_REAL * P,  # every pair is evaluated from both sides
             "ksk": ns * info.n_kvectors * FLOP_SK * P, "kforce": ns * info.n_kvectors * FLOP_KF * P}

@@ -203,8 +203,9 @@ struct qtg_ctx {
     bool any_sc = false, mixed = false;
     // state
     double *q = nullptr, *p = nullptr, *f = nullptr, *fphys = nullptr, *disp = nullptr;
-    int *point = nullptr, *list = nullptr;
-    double *charge = nullptr, *mass = nullptr;
+    int *point = nullptr, *list = nullptr, *point_full = nullptr, *list_full = nullptr;
+    size_t total_point_full = 0, total_list_full = 0;
+    double *charge = nullptr, *mass = nullptr, *inv_mass = nullptr, *sqrt_mass = nullptr;
     double *qdisp = nullptr, *fdisp = nullptr, *fsr = nullptr, *dirv = nullptr, *sc_scale = nullptr;
     double *stage = nullptr;  // per-call staging (total_dof doubles)
     double *noise = nullptr;  // per-call noise (2 + (Pmax-1) * 9Nmax)
@@ -220,6 +221,7 @@ struct qtg_ctx {
     void *sites = nullptr, *tan_sites = nullptr, *phase = nullptr, *opos = nullptr;
     double *part = nullptr;           // [MAX_PART][total_sites][3]
     double2 *skp = nullptr, *dskp = nullptr;  // [MAX_SC][total_k]
+    double2 *wsk = nullptr, *wdsk = nullptr;  // [total_k] (sized for FP64)
     size_t total_k = 0;
     double *energy = nullptr;      // per slot: energies of the base evaluations
     double *energy_aux = nullptr;  // per slot: displaced / derivative evaluations
@@ -285,6 +287,8 @@ EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, d
     a.charge = c->charge;
     a.point = c->point;
     a.list = c->list;
+    a.point_full = c->point_full;
+    a.list_full = c->list_full;
     a.kvec = c->kvec;
     a.kcol = c->kcol;
     a.kgrp = c->kgrp;
@@ -299,6 +303,8 @@ EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, d
     a.total_sites = (long long)c->total_sites;
     a.skp = c->skp;
     a.dskp = c->dskp;
+    a.wsk = c->wsk;
+    a.wdsk = c->wdsk;
     a.total_k = (long long)c->total_k;
     a.energy = c->energy;
     a.status = c->status;
@@ -337,6 +343,8 @@ RingArgs ring_args(qtg_ctx *c, int sys, int flags) {
     r.fphys = c->fphys;
     r.disp = c->disp;
     r.mass = c->mass;
+    r.inv_mass = c->inv_mass;
+    r.sqrt_mass = c->sqrt_mass;
     r.nm = c->nm;
     r.modes = c->modes;
     r.run = c->run;
@@ -374,6 +382,7 @@ ScArgs sc_args(qtg_ctx *c) {
     s.q = c->q;
     s.fphys = c->fphys;
     s.mass = c->mass;
+    s.inv_mass = c->inv_mass;
     s.qdisp = c->qdisp;
     s.dirv = c->dirv;
     s.fdisp = c->fdisp;
@@ -397,6 +406,8 @@ ListArgs list_args(qtg_ctx *c, int first_job, int n_jobs, int force) {
     l.disp = c->disp;
     l.point = c->point;
     l.list = c->list;
+    l.point_full = c->point_full;
+    l.list_full = c->list_full;
     l.acc = c->acc;
     l.status = c->status;
     l.force_rebuild = force;
@@ -410,7 +421,12 @@ ListArgs list_args(qtg_ctx *c, int first_job, int n_jobs, int force) {
 void enqueue_forces(qtg_ctx *c, int sys, bool force_sc) {
     const int jb = sys < 0 ? 0 : c->sys_h[sys].job_base;
     const int nj = sys < 0 ? (int)c->base.h.size() : c->sys_h[sys].n_beads;
-    launch_eval(c, eval_args(c, c->base.d + jb, nj, c->q, c->fphys, 0, 0));
+    // the device-resident stepper (sys < 0) maintains the symmetric lists itself;
+    // per-call entries work on the caller's half lists
+    const int full = sys < 0 ? 1 : 0;
+    EvalArgs base = eval_args(c, c->base.d + jb, nj, c->q, c->fphys, 0, 0);
+    base.lj_full = full;
+    launch_eval(c, base);
     // odd beads that need the Suzuki-Chin force gradient
     const int *osys, *obead;
     const Job *fdj, *tanj;
@@ -442,9 +458,13 @@ void enqueue_forces(qtg_ctx *c, int sys, bool force_sc) {
         launch_sc_prepare(sa, c->stream, &c->launches);
         if (c->mixed) {
             launch_eval(c, aux_args(c, tanj, tn, c->q, c->fdisp, 1, 0));
-            launch_eval(c, aux_args(c, fdj, fdn, c->qdisp, c->fsr, 0, 1));
+            EvalArgs sr = aux_args(c, fdj, fdn, c->qdisp, c->fsr, 0, 1);
+            sr.lj_full = full;
+            launch_eval(c, sr);
         } else {
-            launch_eval(c, aux_args(c, fdj, fdn, c->qdisp, c->fdisp, 0, 0));
+            EvalArgs fd = aux_args(c, fdj, fdn, c->qdisp, c->fdisp, 0, 0);
+            fd.lj_full = full;
+            launch_eval(c, fd);
         }
     }
     sa.job_sys = c->base_sys + jb;
@@ -505,6 +525,23 @@ cudaError_t down(qtg_ctx *c, void *dst, const void *src, size_t bytes) {
 
 qtg_status refresh_sys(qtg_ctx *ctx, int sys) {
     CK(cudaMemcpyAsync(ctx->sys_d + sys, &ctx->sys_h[sys], sizeof(SysDev), cudaMemcpyHostToDevice, ctx->stream));
+    return QTG_OK;
+}
+
+// masses, their inverses and square roots (the kernels multiply instead of dividing)
+qtg_status upload_masses(qtg_ctx *ctx, int sys, const double *mass) {
+    const SysDev &S = ctx->sys_h[sys];
+    std::vector<double> im(S.n_dof), sm(S.n_dof);
+    for (int k = 0; k < S.n_dof; ++k) {
+        im[k] = 1.0 / mass[k];
+        sm[k] = sqrt(mass[k]);
+    }
+    CK(up(ctx, ctx->mass + S.mass_off, mass, sizeof(double) * S.n_dof));
+    CK(cudaMemcpyAsync(ctx->inv_mass + S.mass_off, im.data(), sizeof(double) * S.n_dof, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(ctx->sqrt_mass + S.mass_off, sm.data(), sizeof(double) * S.n_dof, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // the host vectors go out of scope
     return QTG_OK;
 }
 
@@ -572,7 +609,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     std::vector<double> nm_all;
     std::vector<ModeCoef> mode_all;
     std::vector<double> chg_all, mass_all;
-    long long q_off = 0, d_off = 0, pt_off = 0, ls_off = 0, chg_off = 0, mass_off = 0;
+    long long q_off = 0, d_off = 0, pt_off = 0, ls_off = 0, chg_off = 0, mass_off = 0, pf_off = 0, lf_off = 0;
     long long nm_off = 0, mode_off = 0;
     int job_base = 0;
     for (int s = 0; s < n_systems; ++s) {
@@ -598,6 +635,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         // water.cpp:76-157 with the box given directly
         S.beta = 1.0 / (K.K2au * d.temp_K);
         S.beta_n = S.beta / P;
+        S.inv_sqrt_beta_n = 1.0 / sqrt(S.beta_n);
         const double omega_p = 1.0 / S.beta_n;
         S.omega_psq = omega_p * omega_p;
         S.dt = d.dt_fs * K.fs2au;
@@ -657,6 +695,8 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         S.d_off = d_off;
         S.pt_off = pt_off;
         S.ls_off = ls_off;
+        S.pf_off = pf_off;
+        S.lf_off = lf_off;
         S.chg_off = chg_off;
         S.mass_off = mass_off;
         S.nm_off = nm_off;
@@ -665,6 +705,8 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         d_off += (long long)P * 3 * N;
         pt_off += (long long)P * N;
         ls_off += (long long)P * S.list_size;
+        pf_off += (long long)P * (N + 1);
+        lf_off += (long long)P * 2 * S.list_size;
         chg_off += 3 * N;
         mass_off += 9 * N;
         nm_off += (long long)P * P;
@@ -707,6 +749,8 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     ctx->total_disp = (size_t)d_off;
     ctx->total_point = (size_t)pt_off;
     ctx->total_list = (size_t)ls_off;
+    ctx->total_point_full = (size_t)pf_off;
+    ctx->total_list_full = (size_t)lf_off;
     ctx->total_nm = (size_t)nm_off;
     ctx->total_modes = (size_t)mode_off;
     ctx->total_kvec = kall.size();
@@ -812,8 +856,12 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->disp, ctx->total_disp);
     AL(ctx->point, ctx->total_point);
     AL(ctx->list, ctx->total_list);
+    AL(ctx->point_full, ctx->total_point_full);
+    AL(ctx->list_full, ctx->total_list_full);
     AL(ctx->charge, chg_all.size());
     AL(ctx->mass, mass_all.size());
+    AL(ctx->inv_mass, mass_all.size());
+    AL(ctx->sqrt_mass, mass_all.size());
     AL(ctx->sc_scale, ctx->total_slots);
     AL(ctx->noise, ctx->noise_len);
     AL(ctx->kvec, kall.size());
@@ -842,6 +890,8 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->part, (size_t)MAX_PART * 3 * ctx->total_sites);
     AL(ctx->skp, (size_t)MAX_SC * ctx->total_k);
     AL(ctx->dskp, (size_t)MAX_SC * ctx->total_k);
+    AL(ctx->wsk, ctx->total_k);
+    AL(ctx->wdsk, ctx->total_k);
     AL(ctx->energy, ctx->total_slots);
     AL(ctx->energy_aux, ctx->total_slots);
     AL(ctx->base.d, ctx->base.h.size());
@@ -870,6 +920,15 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     cp(ctx->sys_d, ctx->sys_h.data(), sizeof(SysDev) * n_systems);
     cp(ctx->charge, chg_all.data(), sizeof(double) * chg_all.size());
     cp(ctx->mass, mass_all.data(), sizeof(double) * mass_all.size());
+    {
+        std::vector<double> im(mass_all.size()), sm(mass_all.size());
+        for (size_t k = 0; k < mass_all.size(); ++k) {
+            im[k] = 1.0 / mass_all[k];
+            sm[k] = sqrt(mass_all[k]);
+        }
+        cp(ctx->inv_mass, im.data(), sizeof(double) * im.size());
+        cp(ctx->sqrt_mass, sm.data(), sizeof(double) * sm.size());
+    }
     cp(ctx->kvec, kall.data(), sizeof(KVec) * kall.size());
     cp(ctx->kcol, call.data(), sizeof(KCol) * call.size());
     cp(ctx->kgrp, gall.data(), sizeof(KGroup) * gall.size());
@@ -912,9 +971,10 @@ void qtg_destroy(qtg_ctx *ctx) {
     for (int i = 0; i < 2; ++i)
         if (ctx->graph[i]) cudaGraphExecDestroy(ctx->graph[i]);
     void *ptrs[] = {ctx->sys_d, ctx->q, ctx->p, ctx->f, ctx->fphys, ctx->qdisp, ctx->fdisp, ctx->fsr,
-                    ctx->dirv, ctx->stage, ctx->disp, ctx->point, ctx->list, ctx->charge, ctx->mass,
+                    ctx->dirv, ctx->stage, ctx->disp, ctx->point, ctx->list, ctx->point_full, ctx->list_full,
+                    ctx->charge, ctx->mass, ctx->inv_mass, ctx->sqrt_mass,
                     ctx->sc_scale, ctx->noise, ctx->kvec, ctx->kcol, ctx->kgrp, ctx->kbatch, ctx->nm, ctx->modes, ctx->sites, ctx->tan_sites,
-                    ctx->phase, ctx->opos, ctx->part, ctx->skp, ctx->dskp, ctx->energy, ctx->energy_aux,
+                    ctx->phase, ctx->opos, ctx->part, ctx->skp, ctx->dskp, ctx->wsk, ctx->wdsk, ctx->energy, ctx->energy_aux,
                     ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
                     ctx->status, ctx->red_out};
@@ -964,8 +1024,7 @@ qtg_status qtg_set_charges(qtg_ctx *ctx, int sys, const double *charge) {
 qtg_status qtg_set_masses(qtg_ctx *ctx, int sys, const double *mass) {
     CKS(check_sys(ctx, sys));
     if (!mass) return fail(ctx, QTG_ERR_ARG, "null mass array");
-    const SysDev &S = ctx->sys_h[sys];
-    CK(up(ctx, ctx->mass + S.mass_off, mass, sizeof(double) * S.n_dof));
+    CKS(upload_masses(ctx, sys, mass));
     return sync_status(ctx);
 }
 
@@ -1066,7 +1125,7 @@ qtg_status qtg_force_eval_sc(qtg_ctx *ctx, int sys, const double *pos, double *f
     if (!pos || !f || !point || !list || !fphys || S.n_beads % 2) return fail(ctx, QTG_ERR_ARG, "bad argument");
     const size_t nt = (size_t)S.n_beads * S.n_dof;
     if (charge) CKS(upload_charges(ctx, sys, charge));
-    if (mass) CK(up(ctx, ctx->mass + S.mass_off, mass, sizeof(double) * S.n_dof));
+    if (mass) CKS(upload_masses(ctx, sys, mass));
     CK(up(ctx, ctx->q + S.q_off, pos, sizeof(double) * nt));
     CKS(upload_lists(ctx, sys, point, list, 0, S.n_beads));
     CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
@@ -1116,7 +1175,7 @@ qtg_status qtg_pile_g(qtg_ctx *ctx, int sys, double *p, const double *mass, cons
     const SysDev &S = ctx->sys_h[sys];
     if (!p) return fail(ctx, QTG_ERR_ARG, "bad argument");
     const size_t nt = (size_t)S.n_beads * S.n_dof;
-    if (mass) CK(up(ctx, ctx->mass + S.mass_off, mass, sizeof(double) * S.n_dof));
+    if (mass) CKS(upload_masses(ctx, sys, mass));
     CK(up(ctx, ctx->p + S.q_off, p, sizeof(double) * nt));
     if (noise) CK(up(ctx, ctx->noise, noise, sizeof(double) * (2 + (size_t)(S.n_beads - 1) * S.n_dof)));
     CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
@@ -1165,7 +1224,7 @@ qtg_status qtg_get_conserved(qtg_ctx *ctx, int sys, double *q, double *p, const 
     const SysDev &S = ctx->sys_h[sys];
     if (!q || !p || !out) return fail(ctx, QTG_ERR_ARG, "bad argument");
     const size_t nt = (size_t)S.n_beads * S.n_dof;
-    if (mass) CK(up(ctx, ctx->mass + S.mass_off, mass, sizeof(double) * S.n_dof));
+    if (mass) CKS(upload_masses(ctx, sys, mass));
     CK(up(ctx, ctx->q + S.q_off, q, sizeof(double) * nt));
     CK(up(ctx, ctx->p + S.q_off, p, sizeof(double) * nt));
     CK(cudaMemsetAsync(ctx->red_out, 0, 2 * sizeof(double), ctx->stream));
@@ -1194,7 +1253,7 @@ static qtg_status upload_dynamic(qtg_ctx *ctx, int sys, const double *q, const d
     const SysDev &S = ctx->sys_h[sys];
     const size_t nt = (size_t)S.n_beads * S.n_dof;
     if (charge) CKS(upload_charges(ctx, sys, charge));
-    if (mass) CK(up(ctx, ctx->mass + S.mass_off, mass, sizeof(double) * S.n_dof));
+    if (mass) CKS(upload_masses(ctx, sys, mass));
     CK(up(ctx, ctx->q + S.q_off, q, sizeof(double) * nt));
     CK(up(ctx, ctx->p + S.q_off, p, sizeof(double) * nt));
     CK(up(ctx, ctx->f + S.q_off, f, sizeof(double) * nt));
@@ -1382,10 +1441,12 @@ qtg_status qtg_get_estimators(qtg_ctx *ctx, int sys, double *out, int max_record
 qtg_status qtg_time_kernel(qtg_ctx *ctx, const char *name, int iters, double *avg_ms) {
     if (!ctx || !name || iters <= 0 || !avg_ms) return QTG_ERR_ARG;
     const std::string n(name);
-    const bool ewald = n == "prep" || n == "real" || n == "ksk" || n == "kforce" || n == "combine" || n == "lj";
+    const bool ewald = n == "prep" || n == "real" || n == "ksk" || n == "sk_reduce" || n == "kforce" ||
+                       n == "combine" || n == "lj";
     if (!ewald && n != "rebuild" && n != "ring" && n != "end_step") return fail(ctx, QTG_ERR_ARG, "unknown kernel name");
     const int nj = (int)ctx->base.h.size();
-    const EvalArgs a = eval_args(ctx, ctx->base.d, nj, ctx->q, ctx->fphys, 0, 0);
+    EvalArgs a = eval_args(ctx, ctx->base.d, nj, ctx->q, ctx->fphys, 0, 0);
+    a.lj_full = 1;  // as the stepper evaluates
     launch_eval(ctx, a);  // fills every scratch array the single kernels read
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));

@@ -280,6 +280,15 @@ constexpr int KT = 128;  // threads (k groups) per block
 constexpr int CH = 32;   // sites per shared-memory chunk
 constexpr int KG = 8;    // kz per group
 
+// Running sum s (+ compensation c) += v, Kahan's compensated summation.
+template <typename R>
+__device__ __forceinline__ void kahan_add(R &s, R &c, R v) {
+    const R y = v - c;
+    const R t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
 template <typename R, int MODE>
 __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
     const int sc = blockIdx.y, jb = blockIdx.z;
@@ -291,10 +300,8 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
     const bool act = t < ng;
     const int s0 = chunk_lo(ns, sc, a.n_sc), s1 = chunk_lo(ns, sc + 1, a.n_sc);
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double2 *acc = reinterpret_cast<double2 *>(smem_raw);                // [(MODE+1)*KG][KT]
-    V4<R> *ush = reinterpret_cast<V4<R> *>(acc + (MODE + 1) * KG * KT);  // [CH] (mode 1)
-    V2<R> *tab = reinterpret_cast<V2<R> *>(ush + CH);                    // [3*km1][CH+1]
-    for (int g = 0; g < (MODE + 1) * KG; ++g) acc[g * KT + threadIdx.x] = make_double2(0.0, 0.0);
+    V4<R> *ush = reinterpret_cast<V4<R> *>(smem_raw);  // [CH] (mode 1)
+    V2<R> *tab = reinterpret_cast<V2<R> *>(ush + CH);  // [3*km1][CH+1]
     KGroup G;
     G.col = G.kz0 = G.n = 0;
     KCol C;
@@ -316,6 +323,10 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
         zsg[g] = kz < 0 ? (R)-1 : (R)1;
         kzr[g] = bz * (R)kz;
     }
+    // compensated running sums over the chunk totals
+    R Sr[KG], Si[KG], Cr[KG], Ci[KG], dSr[KG], dSi[KG], dCr[KG], dCi[KG];
+#pragma unroll
+    for (int g = 0; g < KG; ++g) Sr[g] = Si[g] = Cr[g] = Ci[g] = dSr[g] = dSi[g] = dCr[g] = dCi[g] = (R)0;
     const V2<R> *ph = reinterpret_cast<const V2<R> *>(a.phase) + J.phase_off;
     const V4<R> *tans = reinterpret_cast<const V4<R> *>(a.tan_sites) + J.site_off;
     const int rows = 3 * km1;
@@ -364,24 +375,69 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
         }
 #pragma unroll
         for (int g = 0; g < KG; ++g) {
-            double2 v = acc[g * KT + threadIdx.x];
-            v.x += (double)sr[g];
-            v.y += (double)si[g];
-            acc[g * KT + threadIdx.x] = v;
+            kahan_add(Sr[g], Cr[g], sr[g]);
+            kahan_add(Si[g], Ci[g], si[g]);
             if (MODE == 1) {
-                double2 d = acc[(KG + g) * KT + threadIdx.x];
-                d.x += (double)dsr[g];
-                d.y += (double)dsi[g];
-                acc[(KG + g) * KT + threadIdx.x] = d;
+                kahan_add(dSr[g], dCr[g], dsr[g]);
+                kahan_add(dSi[g], dCi[g], dsi[g]);
             }
         }
     }
     if (act) {
-        for (int g = 0; g < G.n; ++g) {
-            const size_t at = (size_t)sc * a.total_k + J.sk_off + C.k_begin + (G.kz0 + g + C.m);
-            a.skp[at] = acc[g * KT + threadIdx.x];
-            if (MODE == 1) a.dskp[at] = acc[(KG + g) * KT + threadIdx.x];
+#pragma unroll
+        for (int g = 0; g < KG; ++g) {
+            if (g < G.n) {
+                const size_t at = (size_t)sc * a.total_k + J.sk_off + C.k_begin + (G.kz0 + g + C.m);
+                a.skp[at] = make_double2((double)Sr[g] - (double)Cr[g], (double)Si[g] - (double)Ci[g]);
+                if (MODE == 1)
+                    a.dskp[at] = make_double2((double)dSr[g] - (double)dCr[g], (double)dSi[g] - (double)dCi[g]);
+            }
         }
+    }
+}
+
+// Sum of the structure-factor partials of every k (FP64, fixed order), the
+// reciprocal-space energy sum_k c_k |S(k)|^2, and the force weights 2 c_k S(k)
+// (and 2 c_k dS(k)) in the working precision for k_kforce. One thread per k.
+template <typename R, int MODE>
+__global__ void __launch_bounds__(128) k_sk_reduce(EvalArgs a) {
+    const int jb = blockIdx.y;
+    const Job J = a.jobs[jb];
+    const SysDev &S = a.sys[J.sys];
+    if (blockIdx.x * 128 >= S.n_kvec) return;
+    const int k = blockIdx.x * 128 + threadIdx.x;
+    __shared__ double red[4];
+    double e = 0.0;
+    if (k < S.n_kvec) {
+        const double w = 2.0 * a.kvec[S.kvec_off + k].coef;
+        double sr = 0.0, si = 0.0, dr = 0.0, di = 0.0;
+        for (int sc = 0; sc < a.n_sc; ++sc) {
+            const size_t at = (size_t)sc * a.total_k + J.sk_off + k;
+            const double2 p = a.skp[at];
+            sr += p.x;
+            si += p.y;
+            if (MODE == 1) {
+                const double2 d = a.dskp[at];
+                dr += d.x;
+                di += d.y;
+            }
+        }
+        e = 0.5 * w * (sr * sr + si * si);
+        V2<R> *ws = reinterpret_cast<V2<R> *>(a.wsk) + J.sk_off;
+        V2<R> v;
+        v.x = (R)(w * sr);
+        v.y = (R)(w * si);
+        ws[k] = v;
+        if (MODE == 1) {
+            V2<R> *wd = reinterpret_cast<V2<R> *>(a.wdsk) + J.sk_off;
+            v.x = (R)(w * dr);
+            v.y = (R)(w * di);
+            wd[k] = v;
+        }
+    }
+    if (MODE == 0) {
+        const double t = block_sum(e, red);
+        if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
     }
 }
 
@@ -411,7 +467,6 @@ __global__ void __launch_bounds__(FT) k_kforce(EvalArgs a) {
     V2<R> *ss = reinterpret_cast<V2<R> *>(cs + KB);  // [KB] 2 c_k S(k)
     V2<R> *ds = ss + KB;                             // [KB] 2 c_k dS(k)
     V2<R> *zr = ds + KB;                             // [km1][FT] my Z(kz) row
-    __shared__ double red[FT / 32];
     const V2<R> *ph = reinterpret_cast<const V2<R> *>(a.phase) + J.phase_off;
     for (int m = 0; m < km1; ++m) {
         V2<R> v;
@@ -424,39 +479,17 @@ __global__ void __launch_bounds__(FT) k_kforce(EvalArgs a) {
     if (MODE == 1 && act) ui = reinterpret_cast<const V4<R> *>(a.tan_sites)[J.site_off + i];
     const R bx = (R)(2.0 * PI_REF * S.inv_box[0]), by = (R)(2.0 * PI_REF * S.inv_box[1]),
             bz = (R)(2.0 * PI_REF * S.inv_box[2]);
-    const bool do_energy = (MODE == 0) && blockIdx.x == 0;
-    double Fx = 0.0, Fy = 0.0, Fz = 0.0, E = 0.0;
+    double Fx = 0.0, Fy = 0.0, Fz = 0.0;
     const int ii = act ? i : 0;
+    const V2<R> *wsk = reinterpret_cast<const V2<R> *>(a.wsk) + J.sk_off;
+    const V2<R> *wdsk = reinterpret_cast<const V2<R> *>(a.wdsk) + J.sk_off;
     for (int bt = bt0; bt < bt1; ++bt) {
         const KBatch B = a.kbatch[S.batch_off + bt];
         __syncthreads();
         for (int idx = threadIdx.x; idx < B.c1 - B.c0; idx += FT) cs[idx] = a.kcol[S.col_off + B.c0 + idx];
         for (int idx = threadIdx.x; idx < B.k1 - B.k0; idx += FT) {
-            const int k = B.k0 + idx;
-            const double w = 2.0 * a.kvec[S.kvec_off + k].coef;
-            double sr = 0.0, si = 0.0, dr = 0.0, di = 0.0;
-            for (int sc = 0; sc < a.n_sc; ++sc) {
-                const size_t at = (size_t)sc * a.total_k + J.sk_off + k;
-                const double2 p = a.skp[at];
-                sr += p.x;
-                si += p.y;
-                if (MODE == 1) {
-                    const double2 d = a.dskp[at];
-                    dr += d.x;
-                    di += d.y;
-                }
-            }
-            if (do_energy) E += 0.5 * w * (sr * sr + si * si);
-            V2<R> s2;
-            s2.x = (R)(w * sr);
-            s2.y = (R)(w * si);
-            ss[idx] = s2;
-            if (MODE == 1) {
-                V2<R> d2;
-                d2.x = (R)(w * dr);
-                d2.y = (R)(w * di);
-                ds[idx] = d2;
-            }
+            ss[idx] = wsk[B.k0 + idx];
+            if (MODE == 1) ds[idx] = wdsk[B.k0 + idx];
         }
         __syncthreads();
         R fx = 0, fy = 0, fz = 0;
@@ -511,10 +544,6 @@ __global__ void __launch_bounds__(FT) k_kforce(EvalArgs a) {
         fs[0] = Fx;
         fs[1] = Fy;
         fs[2] = Fz;
-    }
-    if (do_energy) {
-        const double t = block_sum(E, red);
-        if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
     }
 }
 
@@ -661,7 +690,7 @@ __device__ __forceinline__ double lj_exact_disp(const double *qi, const double *
     return r2;
 }
 
-template <typename R>
+template <typename R, int FULL>
 __global__ void __launch_bounds__(128) k_lj(EvalArgs a) {
     const int jb = blockIdx.y;
     const Job J = a.jobs[jb];
@@ -674,20 +703,27 @@ __global__ void __launch_bounds__(128) k_lj(EvalArgs a) {
     double e = 0.0;
     const Consts &C = a.c;
     const double rc2 = C.r_cut_sq;
-    const double band = sizeof(R) == 4 ? 1e-5 : 1e-12;
+    const R rc2r = (R)rc2;
+    const R bandr = sizeof(R) == 4 ? (R)1e-5 : (R)1e-12;
     const R tie = sizeof(R) == 4 ? (R)1e-5 : (R)1e-12;
-    if (i < N - 1) {
+    // half list: rows 0..N-2, entries j > i, forces on j by atomics; symmetric
+    // list (FULL): rows 0..N-1, entries j != i, each pair seen from both ends, so
+    // a row's force needs no atomics and the energy is halved
+    if (i < (FULL ? N : N - 1)) {
         const double *q = a.pos + J.pos_off;
         double *f = a.out + J.out_off;
-        const int *pt = a.point + S.pt_off + (size_t)J.bead * N;
-        const int *ls = a.list + S.ls_off + (size_t)J.bead * S.list_size;
-        // a row outside [0, list_size] (overflowed or caller-corrupted list) or an index
-        // outside (i, N) is skipped and flagged instead of being read out of bounds
+        const int cap = FULL ? 2 * S.list_size : S.list_size;
+        const int *pt = FULL ? a.point_full + S.pf_off + (size_t)J.bead * (N + 1)
+                             : a.point + S.pt_off + (size_t)J.bead * N;
+        const int *ls = FULL ? a.list_full + S.lf_off + (size_t)J.bead * cap
+                             : a.list + S.ls_off + (size_t)J.bead * S.list_size;
+        // a row outside [0, capacity] (overflowed or caller-corrupted list) or an index
+        // outside the row's range is skipped and flagged instead of being read out of bounds
         int n0 = pt[i], n1 = pt[i + 1];
-        if (n0 < 0 || n1 > S.list_size || n0 > n1) {
+        if (n0 < 0 || n1 > cap || n0 > n1) {
             if (lane == 0) atomicOr(a.status, (unsigned)ST_LIST_OVERFLOW);
-            n0 = max(0, min(n0, S.list_size));
-            n1 = max(n0, min(n1, S.list_size));
+            n0 = max(0, min(n0, cap));
+            n1 = max(n0, min(n1, cap));
         }
         R xi[3];
         const V4<R> *opos = reinterpret_cast<const V4<R> *>(a.opos) + J.site_off / 3;
@@ -703,7 +739,7 @@ __global__ void __launch_bounds__(128) k_lj(EvalArgs a) {
         R fi0 = 0, fi1 = 0, fi2 = 0, el = 0;
         for (int n = n0 + lane; n < n1; n += 32) {
             const int j = ls[n];
-            if (j <= i || j >= N) {
+            if ((FULL ? j == i : j <= i) || j < 0 || j >= N) {
                 atomicOr(a.status, (unsigned)ST_LIST_OVERFLOW);
                 continue;
             }
@@ -724,7 +760,7 @@ __global__ void __launch_bounds__(128) k_lj(EvalArgs a) {
                 r[d] -= sys_box<R>(S, d) * f_rint(t);
             }
             R r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
-            if (exact || fabs((double)r2 - rc2) <= band * rc2) {
+            if (exact || fabs(r2 - rc2r) <= bandr * rc2r) {
                 double rd[3];
                 const double r2d = lj_exact_disp(q + 9 * i, q + 9 * j, S, rd);
                 for (int d = 0; d < 3; ++d) r[d] = (R)rd[d];
@@ -742,17 +778,25 @@ __global__ void __launch_bounds__(128) k_lj(EvalArgs a) {
                 fi0 += ff * r[0];
                 fi1 += ff * r[1];
                 fi2 += ff * r[2];
-                atomicAdd(&f[9 * j], -(double)(ff * r[0]));
-                atomicAdd(&f[9 * j + 1], -(double)(ff * r[1]));
-                atomicAdd(&f[9 * j + 2], -(double)(ff * r[2]));
+                if (!FULL) {
+                    atomicAdd(&f[9 * j], -(double)(ff * r[0]));
+                    atomicAdd(&f[9 * j + 1], -(double)(ff * r[1]));
+                    atomicAdd(&f[9 * j + 2], -(double)(ff * r[2]));
+                }
             }
         }
         const double d0 = warp_sum((double)fi0), d1 = warp_sum((double)fi1), d2 = warp_sum((double)fi2);
-        e = warp_sum((double)el);
+        e = warp_sum((double)el) * (FULL ? 0.5 : 1.0);
         if (lane == 0) {
-            atomicAdd(&f[9 * i], d0);
-            atomicAdd(&f[9 * i + 1], d1);
-            atomicAdd(&f[9 * i + 2], d2);
+            if (FULL) {
+                f[9 * i] += d0;
+                f[9 * i + 1] += d1;
+                f[9 * i + 2] += d2;
+            } else {
+                atomicAdd(&f[9 * i], d0);
+                atomicAdd(&f[9 * i + 1], d1);
+                atomicAdd(&f[9 * i + 2], d2);
+            }
         } else {
             e = 0.0;
         }
@@ -790,7 +834,7 @@ __global__ void __launch_bounds__(256) k_fp32_probe(float *out, int iters) {
 
 template <typename R>
 size_t ksk_smem(int kmax) {
-    return (size_t)2 * KG * KT * sizeof(double2) + CH * sizeof(V4<R>) + (size_t)3 * (kmax + 1) * (CH + 1) * sizeof(V2<R>);
+    return CH * sizeof(V4<R>) + (size_t)3 * (kmax + 1) * (CH + 1) * sizeof(V2<R>);
 }
 template <typename R>
 size_t kforce_smem(int kmax) {
@@ -825,17 +869,20 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n) {
     if (a.mode == 0) {
         k_real<R, 0><<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         k_ksk<R, 0><<<dim3(ktiles, a.n_sc, a.n_jobs), KT, ksk_smem<R>(a.max_kmax), s>>>(a);
+        k_sk_reduce<R, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
         k_kforce<R, 0><<<dim3(tiles, a.n_kc, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
     } else {
         k_real<R, 1><<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         k_ksk<R, 1><<<dim3(ktiles, a.n_sc, a.n_jobs), KT, ksk_smem<R>(a.max_kmax), s>>>(a);
+        k_sk_reduce<R, 1><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
         k_kforce<R, 1><<<dim3(tiles, a.n_kc, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
     }
     const dim3 gm((a.max_mols + 127) / 128, a.n_jobs);
     k_combine<R><<<gm, 128, 0, s>>>(a);
-    if (n) *n += 5;
+    if (n) *n += 6;
     if (a.mode == 0) {
-        k_lj<R><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
+        if (a.lj_full) k_lj<R, 1><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
+        else k_lj<R, 0><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
         if (n) *n += 1;
     }
 }
@@ -866,6 +913,9 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
     } else if (n == "ksk") {
         if (mixed) k_ksk<float, 0><<<gk, KT, ksk_smem<float>(a.max_kmax), s>>>(a);
         else k_ksk<double, 0><<<gk, KT, ksk_smem<double>(a.max_kmax), s>>>(a);
+    } else if (n == "sk_reduce") {
+        if (mixed) k_sk_reduce<float, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
+        else k_sk_reduce<double, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
     } else if (n == "kforce") {
         if (mixed) k_kforce<float, 0><<<gf, FT, kforce_smem<float>(a.max_kmax), s>>>(a);
         else k_kforce<double, 0><<<gf, FT, kforce_smem<double>(a.max_kmax), s>>>(a);
@@ -873,8 +923,13 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
         if (mixed) k_combine<float><<<gm, 128, 0, s>>>(a);
         else k_combine<double><<<gm, 128, 0, s>>>(a);
     } else if (n == "lj") {
-        if (mixed) k_lj<float><<<gl, 128, 0, s>>>(a);
-        else k_lj<double><<<gl, 128, 0, s>>>(a);
+        if (mixed) {
+            if (a.lj_full) k_lj<float, 1><<<gl, 128, 0, s>>>(a);
+            else k_lj<float, 0><<<gl, 128, 0, s>>>(a);
+        } else {
+            if (a.lj_full) k_lj<double, 1><<<gl, 128, 0, s>>>(a);
+            else k_lj<double, 0><<<gl, 128, 0, s>>>(a);
+        }
     }
 }
 
@@ -892,7 +947,8 @@ void launch_eval_fp64(const EvalArgs &a, cudaStream_t s, unsigned long long *n) 
     // short-range terms only (FP64): LJ reads the raw positions, no preparation pass
     const dim3 gm((a.max_mols + 127) / 128, a.n_jobs);
     k_combine<double><<<gm, 128, 0, s>>>(a);
-    k_lj<double><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
+    if (a.lj_full) k_lj<double, 1><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
+    else k_lj<double, 0><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
     if (n) *n += 2;
 }
 
@@ -916,17 +972,20 @@ void launch_kwald_only(const EvalArgs &a0, bool mixed, cudaStream_t s, unsigned 
     a.n_sc = chunks_for((long long)ktiles * a.n_jobs, MAX_SC);
     a.n_kc = chunks_for((long long)tiles * a.n_jobs, MAX_KC);
     const dim3 gs((ns + 127) / 128, a.n_jobs), gk(ktiles, a.n_sc, a.n_jobs), gf(tiles, a.n_kc, a.n_jobs);
+    const dim3 gr((a.max_kvec + 127) / 128, a.n_jobs);
     if (mixed) {
         k_prep<float><<<gs, 128, 0, s>>>(a);
         k_ksk<float, 0><<<gk, KT, ksk_smem<float>(a.max_kmax), s>>>(a);
+        k_sk_reduce<float, 0><<<gr, 128, 0, s>>>(a);
         k_kforce<float, 0><<<gf, FT, kforce_smem<float>(a.max_kmax), s>>>(a);
     } else {
         k_prep<double><<<gs, 128, 0, s>>>(a);
         k_ksk<double, 0><<<gk, KT, ksk_smem<double>(a.max_kmax), s>>>(a);
+        k_sk_reduce<double, 0><<<gr, 128, 0, s>>>(a);
         k_kforce<double, 0><<<gf, FT, kforce_smem<double>(a.max_kmax), s>>>(a);
     }
     k_sum_parts<<<dim3((3 * ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
-    if (n) *n += 4;
+    if (n) *n += 5;
 }
 
 }  // namespace qtg

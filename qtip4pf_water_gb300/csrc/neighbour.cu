@@ -172,6 +172,38 @@ __global__ void __launch_bounds__(512) k_skin_rebuild(ListArgs a) {
         }
     }
     for (int k = total + threadIdx.x; k < S.list_size; k += blockDim.x) list[k] = 0;
+    if (a.point_full) {
+        // the symmetric list: every j != i with the same pair test (which is exactly
+        // antisymmetric under i <-> j), ascending j; capacity 2 list_size per bead
+        __syncthreads();
+        for (int i = w; i < N; i += nw) {
+            int c = 0;
+            for (int j0 = 0; j0 < N; j0 += 32) {
+                const int j = j0 + lane;
+                const bool in = (j < N) && (j != i) && pair_in(i, j, pos, qb, S, rs2);
+                c += __popc(__ballot_sync(0xffffffffu, in));
+            }
+            if (lane == 0) cnt[i] = c;
+        }
+        __syncthreads();
+        const int tot2 = block_exclusive_scan(cnt, N, wtot);
+        const int cap = 2 * S.list_size;
+        int *pf = a.point_full + S.pf_off + (size_t)bead * (N + 1);
+        int *lf = a.list_full + S.lf_off + (size_t)bead * cap;
+        for (int i = threadIdx.x; i < N; i += blockDim.x) pf[i] = min(cnt[i], cap);
+        if (threadIdx.x == 0) pf[N] = min(tot2, cap);
+        for (int i = w; i < N; i += nw) {
+            int off = cnt[i];
+            for (int j0 = 0; j0 < N; j0 += 32) {
+                const int j = j0 + lane;
+                const bool in = (j < N) && (j != i) && pair_in(i, j, pos, qb, S, rs2);
+                const unsigned m = __ballot_sync(0xffffffffu, in);
+                const int at = off + __popc(m & lt);
+                if (in && at < cap) lf[at] = j;
+                off += __popc(m);
+            }
+        }
+    }
     for (int k = threadIdx.x; k < 3 * N; k += blockDim.x) disp[k] = 0.0;
     if (threadIdx.x == 0 && a.acc) atomicAdd(&a.acc[sid].rebuilds, 1.0);
 }

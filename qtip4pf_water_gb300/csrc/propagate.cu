@@ -57,6 +57,7 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
     const long long at = S.q_off + (long long)k * S.n_dof + col;
     double qb = 0.0, pb = 0.0;
     const double m = act ? a.mass[S.mass_off + col] : 1.0;
+    const double im = act ? a.inv_mass[S.mass_off + col] : 1.0;
     if (act) {
         qb = a.q[at];
         pb = a.p[at];
@@ -110,21 +111,21 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
     if (act) {
         if (flags & RF_VV) {
             // update.cpp:87-91
-            const double dq = yp * S.dt / m;
+            const double dq = yp * S.dt * im;
             if ((flags & RF_DISP) && (col % 9) < 3) a.disp[S.d_off + 3 * (col / 9) + (col % 9)] += dq;
             yq += dq;
         }
         const ModeCoef mc = a.modes[S.mode_off + k];
         if (flags & RF_CAYLEY) {
             // update.cpp:301-320
-            double t = S.halfdt * yp / m + yq;
+            double t = S.halfdt * yp * im + yq;
             t *= mc.scale;
             yp = yp - S.halfdt * mc.w2 * yq * m;
             yp *= mc.scale;
             yq = t;
         }
         if ((flags & RF_THERMO) && (S.thermostat != 0 || a.pile_g)) {
-            const double before = 0.5 * yp * yp / m;
+            const double before = 0.5 * yp * yp * im;
             if (k == 0 && (S.thermostat == 1 || a.pile_g)) {
                 yp *= a.run[W.sys].alpha;  // PILE-G centroid (thermostat.cpp:88-104)
             } else {
@@ -143,12 +144,13 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
                     xi = normal_f32(philox4x32_10((uint32_t)col, (uint32_t)k, (uint32_t)st,
                                                   (uint32_t)(st >> 32), k0, k1));
                 }
-                yp = c1 * yp + sqrt(m / S.beta_n) * c2 * xi;  // thermostat.cpp:131-136
+                // thermostat.cpp:131-136: sqrt(m / beta_P) c2 xi
+                yp = c1 * yp + a.sqrt_mass[S.mass_off + col] * S.inv_sqrt_beta_n * c2 * xi;
             }
-            heat = 0.5 * yp * yp / m - before;
+            heat = 0.5 * yp * yp * im - before;
         }
         if (flags & RF_CAYLEY) {
-            double t = S.halfdt * yp / m + yq;
+            double t = S.halfdt * yp * im + yq;
             t *= mc.scale;
             yp = yp - S.halfdt * mc.w2 * yq * m;
             yp *= mc.scale;
@@ -214,10 +216,12 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
     extern __shared__ double sh[];
     double *Xq = sh;
     double *Xp = Xq + P * C;
-    __shared__ double red[8];
+    __shared__ double qbar[256];
+    __shared__ double red4[4][8];
     const long long at = S.q_off + (long long)b * S.n_dof + col;
     double qb = 0.0, pb = 0.0, fb = 0.0, fpb = 0.0;
     const double m = act ? a.mass[S.mass_off + col] : 1.0;
+    const double im = act ? a.inv_mass[S.mass_off + col] : 1.0;
     if (act) {
         qb = a.q[at];
         pb = a.p[at];
@@ -231,36 +235,48 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
         Xp[b * C + c] = pb + S.halfdt * fb;
     }
     __syncthreads();
-    double kin = 0.0, spring = 0.0, tq = 0.0, k0 = 0.0;
+    // bead 0 of each column: the centroid (path_integrals.cpp:10-26) and the
+    // centroid normal-mode kinetic energy after the next opening kick
+    double k0 = 0.0;
+    if (b == 0 && c < W.ncols) {
+        double sq = 0.0, sp = 0.0;
+        for (int j = 0; j < P; ++j) {
+            sq += Xq[j * C + c];
+            sp += Xp[j * C + c];
+        }
+        qbar[c] = sq / (double)P;
+        const double p0 = sqrt(1.0 / P) * sp;
+        k0 = 0.5 * p0 * p0 * im;
+    }
+    __syncthreads();
+    double kin = 0.0, spring = 0.0, tq = 0.0;
     if (act) {
-        kin = 0.5 * pb * pb / m;
+        kin = 0.5 * pb * pb * im;
         const double qn = Xq[((b + 1) % P) * C + c];
         const double dq = qb - qn;
         spring = 0.5 * m * S.omega_psq * dq * dq;
         const int all = a.kcv_all_beads < 0 ? (S.propagator == 1) : a.kcv_all_beads;
-        if (all || (b % 2 == 0)) {
-            double qc = 0.0;
-            for (int j = 0; j < P; ++j) qc += Xq[j * C + c];
-            qc /= (double)P;
-            tq = -(qb - qc) * fpb;
-        }
-        if (b == 0) {
-            double s = 0.0;
-            for (int j = 0; j < P; ++j) s += Xp[j * C + c];
-            const double p0 = sqrt(1.0 / P) * s;
-            k0 = 0.5 * p0 * p0 / m;
-        }
+        if (all || (b % 2 == 0)) tq = -(qb - qbar[c]) * fpb;
     }
-    double t0 = block_sum(kin, red);
-    double t1 = block_sum(spring, red);
-    double t2 = block_sum(tq, red);
-    double t3 = block_sum(k0, red);
-    if (threadIdx.x == 0) {
+    // one fused block reduction of the four sums
+    kin = warp_sum(kin);
+    spring = warp_sum(spring);
+    tq = warp_sum(tq);
+    k0 = warp_sum(k0);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        red4[0][w] = kin;
+        red4[1][w] = spring;
+        red4[2][w] = tq;
+        red4[3][w] = k0;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red4[threadIdx.x][k];
         SysAcc *ac = &a.acc[W.sys];
-        atomicAdd(&ac->kin, t0);
-        atomicAdd(&ac->spring, t1);
-        atomicAdd(&ac->kcv_tq, t2);
-        atomicAdd(&ac->k0, t3);
+        double *dst = threadIdx.x == 0 ? &ac->kin : threadIdx.x == 1 ? &ac->spring : threadIdx.x == 2 ? &ac->kcv_tq : &ac->k0;
+        atomicAdd(dst, t);
     }
 }
 
@@ -273,7 +289,7 @@ __global__ void k_centroid_ke(RingArgs a) {
     for (int c = threadIdx.x; c < W.ncols; c += blockDim.x) {
         const int col = W.col0 + c;
         const double pv = a.p[S.q_off + col];
-        e += 0.5 * pv * pv / a.mass[S.mass_off + col];
+        e += 0.5 * pv * pv * a.inv_mass[S.mass_off + col];
     }
     double t = block_sum(e, red);
     if (threadIdx.x == 0) atomicAdd(&a.acc[W.sys].k0, t);
@@ -369,14 +385,14 @@ __global__ void __launch_bounds__(256) k_sc_prepare(ScArgs a) {
     const SysDev &S = a.sys[sid];
     const int nd = S.n_dof, P = S.n_beads;
     const double *fp = a.fphys + S.q_off + (size_t)b * nd;
-    const double *mass = a.mass + S.mass_off;
+    const double *im = a.inv_mass + S.mass_off;
     __shared__ double red[8];
     __shared__ double scl_sh;
     double fsq = 0.0, dl = 0.0;
     for (int i = threadIdx.x; i < nd; i += blockDim.x) {
-        const double f = fp[i], m = mass[i];
-        fsq += f * f / m;
-        const double t = f / m;
+        const double f = fp[i];
+        const double t = f * im[i];
+        fsq += f * t;
         dl += t * t;
     }
     fsq = block_sum(fsq, red);
@@ -395,10 +411,11 @@ __global__ void __launch_bounds__(256) k_sc_prepare(ScArgs a) {
     double *qp = a.qdisp + S.q_off + (size_t)b * nd;
     double *qm = a.qdisp + S.q_off + (size_t)(b - 1) * nd;
     for (int i = threadIdx.x; i < nd; i += blockDim.x) {
-        const double dq = scl * fp[i] / mass[i];
+        const double v = fp[i] * im[i];
+        const double dq = scl * v;
         qp[i] = qb[i] + dq;
         qm[i] = qb[i] - dq;
-        if (a.mixed) a.dirv[S.q_off + (size_t)b * nd + i] = fp[i] / mass[i];
+        if (a.mixed) a.dirv[S.q_off + (size_t)b * nd + i] = v;
     }
 }
 

@@ -31,12 +31,14 @@ struct SysDev {
     long long d_off;    // doubles: [P][3N] block in disp
     long long pt_off;   // ints: [P][N] block in point
     long long ls_off;   // ints: [P][list_size] block in list
+    long long pf_off;   // ints: [P][N+1] block in point_full (symmetric list row starts)
+    long long lf_off;   // ints: [P][2 list_size] block in list_full
     long long chg_off;  // doubles: [3N] in charge
     long long mass_off; // doubles: [9N] in mass
     double box[3], inv_box[3];
     double kappa, rc_sq, ewald_pref, k_pref, self_energy;
     double r_cut_sq, r_skin_sq, skin_margin;
-    double beta, beta_n, omega_psq, dt, halfdt, eps_sc, c1_centroid;
+    double beta, beta_n, omega_psq, dt, halfdt, eps_sc, c1_centroid, inv_sqrt_beta_n;
     float boxf[3], inv_boxf[3];
     float kappaf, rc_sqf, ewald_preff, kappa_sqf;
     unsigned long long seed;
@@ -219,6 +221,8 @@ struct RingArgs {
     const double *f;
     double *disp;
     const double *mass;
+    const double *inv_mass;  // 1 / m per dof
+    const double *sqrt_mass; // sqrt(m) per dof
     const double *nm;        // bead -> normal-mode matrices
     const ModeCoef *modes;
     SysRun *run;
@@ -254,7 +258,7 @@ struct ScArgs {
     const SysDev *sys;
     const int *job_sys, *job_bead;  // odd beads (prepare) or all base jobs (finish)
     int n_jobs;
-    const double *q, *fphys, *mass;
+    const double *q, *fphys, *mass, *inv_mass;
     double *qdisp;      // displaced positions (q + d at bead b, q - d at bead b-1)
     double *dirv;       // direction f/m at bead b (mixed mode)
     const double *fdisp;   // FP64: F(q+d) at b, F(q-d) at b-1; mixed: dF_ewald at b
@@ -307,6 +311,8 @@ struct EvalArgs {
     const double *dir;     // tangent direction base (mode 1 jobs), same offsets as pos
     const double *charge;
     const int *point, *list;
+    const int *point_full, *list_full;  // symmetric lists built by the stepper's rebuild
+    int lj_full;                        // 1: Lennard-Jones over the symmetric list (no atomics)
     const KVec *kvec;
     const KCol *kcol;
     const KGroup *kgrp;
@@ -320,6 +326,7 @@ struct EvalArgs {
     long long total_sites; // sites summed over all slots (plane stride of part)
     double2 *skp;          // partial S(k) [MAX_SC][total_k]
     double2 *dskp;         // partial dS(k) along the tangent direction
+    void *wsk, *wdsk;      // 2 c_k S(k) and 2 c_k dS(k), working precision, per slot
     long long total_k;     // k-vectors summed over all slots (plane stride of skp)
     double *energy;        // per slot
     unsigned *status;
@@ -353,6 +360,7 @@ struct ListArgs {
     const double *q;
     double *disp;
     int *point, *list;
+    int *point_full, *list_full;  // may be null: only the half list is built
     SysAcc *acc;
     unsigned *status;
     int force_rebuild;  // 1: rebuild unconditionally (initial build / per-call API)
