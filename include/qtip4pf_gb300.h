@@ -177,6 +177,33 @@ qtg_status qtg_sync(qtg_ctx *ctx);
 qtg_status qtg_get_estimators(qtg_ctx *ctx, int sys, double *out, int max_records, int *n_records);
 qtg_status qtg_reset_estimators(qtg_ctx *ctx);
 
+/* ---- without device allocation --------------------------------------------- */
+/* No counterpart in the reference: the reciprocal-space Ewald sum of qtg_kwald
+ * (FP64) for callers that cannot allocate device memory -- engines and plugins
+ * that own the GPU memory budget and pass preallocated buffers to their force
+ * routines, and work issued while another library captures the stream into a
+ * CUDA graph. It calls no cudaMalloc/cudaFree and needs no qtg_ctx: all scratch
+ * lives in one static device array of 2.76 MiB (2,895,616 bytes) that every GPU loading the
+ * library holds until exit.
+ *   sites   device, double[3 n_sites]: charge sites (M, H1, H2 per molecule)
+ *   charge  device, double[n_sites]
+ *   box     host, double[3] (bohr); eps_ewald as config.txt (kappa, k_max and
+ *           the k set derived as forces.cpp:574-584, :251-445)
+ *   f_sites device, double[3 n_sites]: the k-space forces are ADDED
+ *   energy  device, one double: the k-space energy is WRITTEN
+ * Limits: n_sites <= QTG_NOALLOC_MAX_SITES, k_max <= QTG_NOALLOC_MAX_KMAX;
+ * anything larger returns QTG_ERR_ARG. Work is queued on `cuda_stream` and the
+ * call returns without waiting. The first call on a device looks up the array's
+ * device address (once per device, that device current) and should therefore
+ * come before any stream capture. Every call shares the array, so calls that
+ * overlap on the GPU (other streams, other host threads) race; each call
+ * rebuilds every table it reads, so nothing carries over between calls. */
+#define QTG_NOALLOC_MAX_SITES 1536
+#define QTG_NOALLOC_MAX_KMAX 12
+qtg_status qtg_kwald_noalloc(const double *sites, const double *charge, int n_sites,
+                             const double *box_bohr, double eps_ewald, double *f_sites,
+                             double *energy, void *cuda_stream);
+
 /* ---- measurement helpers (no reference counterpart) ------------------------ */
 /* Average duration (ms, CUDA events on the context's stream) of `iters`
  * back-to-back launches of one kernel of the force / step pipeline over every

@@ -100,6 +100,7 @@ def load(build_if_missing: bool = True):
         "qtg_reset_estimators": ([V], C.c_int),
         "qtg_time_kernel": ([V, C.c_char_p, C.c_int, D], C.c_int),
         "qtg_fp32_peak": ([D], C.c_int),
+        "qtg_kwald_noalloc": ([V, V, C.c_int, D, C.c_double, V, V, V], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

@@ -26,8 +26,10 @@ COMPAT = os.path.join(BUILD, "libqtip_compat.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-           "-Xptxas", "-warn-spills"]
+# host code: no floating-point contraction, so the host-side parameter derivations
+# round like the reference's x86-64 build on every host architecture
+NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+           "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 
 def nvcc() -> str:
@@ -84,7 +86,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     compat_src = os.path.join(CSRC, "compat", "compat.cpp")
     if os.path.exists(compat_src) and (force or _stale(COMPAT, [compat_src, LIB] + hdrs)):
         cxx = shutil.which("g++") or "g++"
-        _run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-I", INCLUDE, compat_src, "-o", COMPAT,
+        _run([cxx, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-shared", "-I", INCLUDE, compat_src, "-o", COMPAT,
               "-L", BUILD, "-lqtipgpu", "-Wl,-rpath,$ORIGIN"], verbose)
     return LIB
 
