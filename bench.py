@@ -38,6 +38,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_MOLS, N_BEADS, TEMP, DT_FS, SEED = 512, 32, 298.0, 0.25, 2024
+METRIC = "ns/day, 512 H2O P=32 PIMD: plain FP64 vs mixed/surrogate-CMD at stated error"
+REF_SECONDS = 60.0
 WORKLOAD = "512 H2O (L=24.85 A), P=32 PIMD, Trotter + PILE-G, 298 K, dt=0.25 fs, eps_ewald=1e-6"
 # algorithmic work per force evaluation (fixed convention): real-space pair within
 # r_c 60 flop, LJ pair within 9 A 30 flop, (site, k-vector) 20 flop (S(k) 8 +
@@ -73,6 +75,9 @@ class ClockSampler:
             return
         self._thr = threading.Thread(target=self._read, daemon=True)
         self._thr.start()
+        t0 = time.time()  # nvidia-smi takes a moment to start: let the samples cover the timed region
+        while not self.samples and time.time() - t0 < 5.0:
+            time.sleep(0.02)
 
     def _read(self):
         for line in self._proc.stdout:
@@ -230,7 +235,7 @@ def run_gpu(args):
     # ---- roofline of the dominant kernel -----------------------------------------------------
     roof = roofline(q, st, mix)
     line = {
-        "metric": "ns/day, 512 H2O P=32 PIMD (mixed precision, device-resident)",
+        "metric": METRIC,
         "value": value, "unit": "ns/day", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32 Ewald / fp64 accumulation, integration, normal modes",
@@ -327,6 +332,12 @@ def roofline(q, st, mix):
             "pairs_within_rc_per_bead": nreal, "lj_pairs_per_bead": nlj}
 
 
+def pile_noise(rng, n_dof, n_beads):
+    """One PILE-G step's draws in the oracle's layout [R, chi^2(n_dof - 1), xi(beads 1..P-1)]."""
+    return np.concatenate(([rng.standard_normal(), rng.chisquare(n_dof - 1)],
+                           rng.standard_normal((n_beads - 1) * n_dof)))
+
+
 def cpu_baseline(st, seconds):
     """The oracle's Trotter step on the host cores (OpenMP over beads), bounded sample."""
     from oracle.binding import Oracle, build
@@ -339,16 +350,18 @@ def cpu_baseline(st, seconds):
     f = np.zeros_like(qq)
     fp = np.zeros_like(qq)
     o.force_eval_trotter(qq, f, point, lst)
+    rng = np.random.default_rng(SEED)
     t0 = time.perf_counter()
     n = 0
     while True:
-        o.update_pimd(qq, pp, f, fp, point, lst, disp, is_nvt=False, trotter=True)
+        o.update_pimd(qq, pp, f, fp, point, lst, disp, is_nvt=True, trotter=True,
+                      noise=pile_noise(rng, 9 * N_MOLS, N_BEADS))
         n += 1
         if time.perf_counter() - t0 > seconds:
             break
     dt = (time.perf_counter() - t0) / n
     return {"value": ns_per_day(dt), "unit": "ns/day", "cores": threads, "kind": "port",
-            "sample": f"{n} Trotter NVE steps of the benchmark workload (512 H2O, P=32) with the C oracle, "
+            "sample": f"{n} Trotter + PILE-G steps of the benchmark workload (512 H2O, P=32) with the C oracle, "
                       f"OpenMP over beads, {threads} threads; {dt:.3f} s/step"}
 
 
@@ -369,21 +382,30 @@ def run_reference(args):
     f = np.zeros_like(qq)
     fp = np.zeros_like(qq)
     o.force_eval_trotter(qq, f, point, lst)
+    rng = np.random.default_rng(SEED)
     for _ in range(args.warmup):
-        o.update_pimd(qq, pp, f, fp, point, lst, disp, is_nvt=False, trotter=True)
+        o.update_pimd(qq, pp, f, fp, point, lst, disp, is_nvt=True, trotter=True,
+                      noise=pile_noise(rng, 9 * N_MOLS, N_BEADS))
+    # each oracle step takes ~0.2 s on 16 cores: time at most REF_SECONDS of the K steps asked for
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        o.update_pimd(qq, pp, f, fp, point, lst, disp, is_nvt=False, trotter=True)
-    dt = (time.perf_counter() - t0) / args.steps
+    n = 0
+    while n < args.steps:
+        o.update_pimd(qq, pp, f, fp, point, lst, disp, is_nvt=True, trotter=True,
+                      noise=pile_noise(rng, 9 * N_MOLS, N_BEADS))
+        n += 1
+        if time.perf_counter() - t0 > REF_SECONDS:
+            break
+    dt = (time.perf_counter() - t0) / n
     v = ns_per_day(dt)
-    line = {"impl": "reference", "metric": "ns/day, 512 H2O P=32 PIMD", "value": v, "unit": "ns/day",
-            "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "ns/day",
+            "n_gpus": 0, "steps": n, "warmup": args.warmup, "ms_per_step": dt * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
             "data": "synthetic (seeded lattice start, 512 waters, 32 beads)",
             "config": {"workload": WORKLOAD, "precision": "fp64", "propagator": "trotter"},
             "cpu_baseline": {"value": v, "unit": "ns/day", "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} timed Trotter steps (after {args.warmup} warm-up) of the "
-                                       f"benchmark workload with the C oracle, OpenMP over beads, {threads} threads"},
+                             "sample": f"{n} timed Trotter + PILE-G steps (of {args.steps} asked; at most {REF_SECONDS:.0f} s, "
+                                       f"after {args.warmup} warm-up) of the benchmark workload with the C oracle, "
+                                       f"OpenMP over beads, {threads} threads"},
             "e2e": {"value": v, "unit": "ns/day", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -391,7 +413,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=3000)  # ~1.7 s timed: several clock samples
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

@@ -152,11 +152,11 @@ void build_columns(const std::vector<KVec> &kv, std::vector<KVec> &kord, std::ve
         }
         const int ci = (int)cols.size();
         cols.push_back(c);
-        for (int kz0 = -m; kz0 <= m; kz0 += 8) {
+        for (int az0 = 0; az0 <= m; az0 += 4) {  // |kz| groups, each |kz| covering +kz and -kz
             KGroup g;
             g.col = ci;
-            g.kz0 = kz0;
-            g.n = std::min(8, m - kz0 + 1);
+            g.kz0 = az0;
+            g.n = std::min(4, m - az0 + 1);
             g.pad = 0;
             grps.push_back(g);
         }

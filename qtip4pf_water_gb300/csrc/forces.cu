@@ -271,14 +271,14 @@ __global__ void __launch_bounds__(RT) k_real(EvalArgs a) {
 }
 
 // ---- k_ksk: structure factors ---------------------------------------------------
-// One thread per group of <= 8 consecutive kz of one (kx, ky) column; the
-// column factor X(kx) Y(ky) of a site is formed once and multiplied by the
-// group's Z(kz). Sites are staged through shared memory in chunks of CH; each
+// One thread per group of <= 4 consecutive |kz| of one (kx, ky) column, each
+// |kz| covering the pair kz = +|kz|, -|kz|; the column factor X(kx) Y(ky) of a
+// site is formed once and multiplied by Z and conj(Z) with shared products. Sites are staged through shared memory in chunks of CH; each
 // chunk's partial sums (registers, working precision) are added to FP64 running
 // sums kept in shared memory.
 constexpr int KT = 128;  // threads (k groups) per block
 constexpr int CH = 32;   // sites per shared-memory chunk
-constexpr int KG = 8;    // kz per group
+constexpr int KZ = 4;    // |kz| values per group (each covering +kz and -kz)
 
 // Running sum s (+ compensation c) += v, Kahan's compensated summation.
 template <typename R>
@@ -314,19 +314,20 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
     const R sy = C.ky < 0 ? (R)-1 : (R)1;
     const R bz = (R)(2.0 * PI_REF * S.inv_box[2]);
     const R kx = (R)(2.0 * PI_REF * C.kx * S.inv_box[0]), ky = (R)(2.0 * PI_REF * C.ky * S.inv_box[1]);
-    int zrow[KG];
-    R zsg[KG], kzr[KG];
+    // the group's |kz| values az = kz0 .. kz0 + n - 1; each covers kz = +az and -az
+    int zrow[KZ];
+    R kzr[KZ];
 #pragma unroll
-    for (int g = 0; g < KG; ++g) {
-        const int kz = G.kz0 + g;
-        zrow[g] = (2 * km1 + min(abs(kz), km1 - 1)) * (CH + 1);
-        zsg[g] = kz < 0 ? (R)-1 : (R)1;
-        kzr[g] = bz * (R)kz;
+    for (int g = 0; g < KZ; ++g) {
+        zrow[g] = (2 * km1 + min(G.kz0 + g, km1 - 1)) * (CH + 1);
+        kzr[g] = bz * (R)(G.kz0 + g);
     }
-    // compensated running sums over the chunk totals
-    R Sr[KG], Si[KG], Cr[KG], Ci[KG], dSr[KG], dSi[KG], dCr[KG], dCi[KG];
+    // compensated running sums over the chunk totals, [g][0] for +az, [g][1] for -az
+    R Sr[KZ][2], Si[KZ][2], Cr[KZ][2], Ci[KZ][2], dSr[KZ][2], dSi[KZ][2], dCr[KZ][2], dCi[KZ][2];
 #pragma unroll
-    for (int g = 0; g < KG; ++g) Sr[g] = Si[g] = Cr[g] = Ci[g] = dSr[g] = dSi[g] = dCr[g] = dCi[g] = (R)0;
+    for (int g = 0; g < KZ; ++g)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) Sr[g][h] = Si[g][h] = Cr[g][h] = Ci[g][h] = dSr[g][h] = dSi[g][h] = dCr[g][h] = dCi[g][h] = (R)0;
     const V2<R> *ph = reinterpret_cast<const V2<R> *>(a.phase) + J.phase_off;
     const V4<R> *tans = reinterpret_cast<const V4<R> *>(a.tan_sites) + J.site_off;
     const int rows = 3 * km1;
@@ -346,9 +347,11 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
         }
         __syncthreads();
         const int nc = min(CH, s1 - c0);
-        R sr[KG], si[KG], dsr[KG], dsi[KG];
+        R sr[KZ][2], si[KZ][2], dsr[KZ][2], dsi[KZ][2];
 #pragma unroll
-        for (int g = 0; g < KG; ++g) sr[g] = si[g] = dsr[g] = dsi[g] = (R)0;
+        for (int g = 0; g < KZ; ++g)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) sr[g][h] = si[g][h] = dsr[g][h] = dsi[g][h] = (R)0;
         for (int c = 0; c < nc; ++c) {
             const V2<R> x = tab[ax * (CH + 1) + c], y = tab[(km1 + ay) * (CH + 1) + c];
             const R yi = sy * y.y;
@@ -360,37 +363,52 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
                 uz = u.z;
             }
 #pragma unroll
-            for (int g = 0; g < KG; ++g) {
+            for (int g = 0; g < KZ; ++g) {
                 const V2<R> z = tab[zrow[g] + c];
-                const R zi = zsg[g] * z.y;
-                const R er = pr * z.x - pi * zi, ei = pr * zi + pi * z.x;
-                sr[g] += er;
-                si[g] += ei;
+                // A Z (kz = +az) and A conj(Z) (kz = -az) share their products
+                const R t1 = pr * z.x, t2 = pi * z.x;
+                const R erp = t1 - pi * z.y, eip = t2 + pr * z.y;
+                const R erm = t1 + pi * z.y, eim = t2 - pr * z.y;
+                sr[g][0] += erp;
+                si[g][0] += eip;
+                sr[g][1] += erm;
+                si[g][1] += eim;
                 if (MODE == 1) {
-                    const R ku = kxyu + kzr[g] * uz;
-                    dsr[g] -= ku * ei;
-                    dsi[g] += ku * er;
+                    const R kup = kxyu + kzr[g] * uz, kum = kxyu - kzr[g] * uz;
+                    dsr[g][0] -= kup * eip;
+                    dsi[g][0] += kup * erp;
+                    dsr[g][1] -= kum * eim;
+                    dsi[g][1] += kum * erm;
                 }
             }
         }
 #pragma unroll
-        for (int g = 0; g < KG; ++g) {
-            kahan_add(Sr[g], Cr[g], sr[g]);
-            kahan_add(Si[g], Ci[g], si[g]);
-            if (MODE == 1) {
-                kahan_add(dSr[g], dCr[g], dsr[g]);
-                kahan_add(dSi[g], dCi[g], dsi[g]);
+        for (int g = 0; g < KZ; ++g)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                kahan_add(Sr[g][h], Cr[g][h], sr[g][h]);
+                kahan_add(Si[g][h], Ci[g][h], si[g][h]);
+                if (MODE == 1) {
+                    kahan_add(dSr[g][h], dCr[g][h], dsr[g][h]);
+                    kahan_add(dSi[g][h], dCi[g][h], dsi[g][h]);
+                }
             }
-        }
     }
     if (act) {
 #pragma unroll
-        for (int g = 0; g < KG; ++g) {
+        for (int g = 0; g < KZ; ++g) {
             if (g < G.n) {
-                const size_t at = (size_t)sc * a.total_k + J.sk_off + C.k_begin + (G.kz0 + g + C.m);
-                a.skp[at] = make_double2((double)Sr[g] - (double)Cr[g], (double)Si[g] - (double)Ci[g]);
-                if (MODE == 1)
-                    a.dskp[at] = make_double2((double)dSr[g] - (double)dCr[g], (double)dSi[g] - (double)dCi[g]);
+                const int az = G.kz0 + g;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (h == 1 && az == 0) continue;  // kz = 0 has one entry
+                    const int kz = h ? -az : az;
+                    const size_t at = (size_t)sc * a.total_k + J.sk_off + C.k_begin + (kz + C.m);
+                    a.skp[at] = make_double2((double)Sr[g][h] - (double)Cr[g][h], (double)Si[g][h] - (double)Ci[g][h]);
+                    if (MODE == 1)
+                        a.dskp[at] = make_double2((double)dSr[g][h] - (double)dCr[g][h],
+                                                  (double)dSi[g][h] - (double)dCi[g][h]);
+                }
             }
         }
     }
@@ -503,33 +521,31 @@ __global__ void __launch_bounds__(FT) k_kforce(EvalArgs a) {
             if (MODE == 1) kxyu = bx * (R)C.kx * ui.x + by * (R)C.ky * ui.y;
             const int kb = C.k_begin - B.k0 + C.m;  // smem index of kz = 0
             R v = 0, vz = 0;
-            // kz = -m .. -1 (Z conjugated), then kz = 0 .. m
-            for (int az = C.m; az >= 1; --az) {
-                const V2<R> z = zr[az * FT + threadIdx.x];
-                const R zi = -z.y;
-                const R er = pr * z.x - pi * zi, ei = pr * zi + pi * z.x;
-                const V2<R> sk = ss[kb - az];
-                R val = sk.x * ei - sk.y * er;
+            {   // kz = 0: Z = 1
+                const V2<R> sk = ss[kb];
+                R val = sk.x * pi - sk.y * pr;
                 if (MODE == 1) {
-                    const V2<R> d = ds[kb - az];
-                    const R ku = kxyu - bz * (R)az * ui.z;
-                    val = (d.x * ei - d.y * er) + ku * (sk.x * er + sk.y * ei);
+                    const V2<R> d = ds[kb];
+                    val = (d.x * pi - d.y * pr) + kxyu * (sk.x * pr + sk.y * pi);
                 }
                 v += val;
-                vz -= (R)az * val;
             }
-            for (int az = 0; az <= C.m; ++az) {
+            // kz = +az and -az share the products of A Z and A conj(Z)
+            for (int az = 1; az <= C.m; ++az) {
                 const V2<R> z = zr[az * FT + threadIdx.x];
-                const R er = pr * z.x - pi * z.y, ei = pr * z.y + pi * z.x;
-                const V2<R> sk = ss[kb + az];
-                R val = sk.x * ei - sk.y * er;
+                const R t1 = pr * z.x, t2 = pi * z.x;
+                const R erp = t1 - pi * z.y, eip = t2 + pr * z.y;
+                const R erm = t1 + pi * z.y, eim = t2 - pr * z.y;
+                const V2<R> sp = ss[kb + az], sm = ss[kb - az];
+                R vp = sp.x * eip - sp.y * erp, vm = sm.x * eim - sm.y * erm;
                 if (MODE == 1) {
-                    const V2<R> d = ds[kb + az];
-                    const R ku = kxyu + bz * (R)az * ui.z;
-                    val = (d.x * ei - d.y * er) + ku * (sk.x * er + sk.y * ei);
+                    const V2<R> dp = ds[kb + az], dm = ds[kb - az];
+                    const R kup = kxyu + bz * (R)az * ui.z, kum = kxyu - bz * (R)az * ui.z;
+                    vp = (dp.x * eip - dp.y * erp) + kup * (sp.x * erp + sp.y * eip);
+                    vm = (dm.x * eim - dm.y * erm) + kum * (sm.x * erm + sm.y * eim);
                 }
-                v += val;
-                vz += (R)az * val;
+                v += vp + vm;
+                vz += (R)az * (vp - vm);
             }
             fx += bx * (R)C.kx * v;
             fy += by * (R)C.ky * v;

@@ -30,7 +30,7 @@ constexpr int NA_MAX_SITES = QTG_NOALLOC_MAX_SITES;
 constexpr int NA_MAX_KMAX = QTG_NOALLOC_MAX_KMAX;
 constexpr int NA_COLS = (NA_MAX_KMAX + 1) * (2 * NA_MAX_KMAX + 1);  // every (kx >= 0, ky) column
 constexpr int NA_MAX_K = NA_COLS * (2 * NA_MAX_KMAX + 1);          // every kz of every column
-constexpr int NA_MAX_GRP = NA_COLS * ((2 * NA_MAX_KMAX + 1 + 7) / 8);
+constexpr int NA_MAX_GRP = NA_COLS * ((NA_MAX_KMAX + 1 + 3) / 4);
 constexpr int NA_MAX_BATCH = NA_COLS;
 
 constexpr size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -141,7 +141,8 @@ __global__ void __launch_bounds__(512) k_noalloc_setup(NAParams p, unsigned char
     int nk, ncol, ngrp;
     const int kb = block_scan_excl(n, sh, &nk);
     const int ci = block_scan_excl(n > 0 ? 1 : 0, sh, &ncol);
-    const int gi = block_scan_excl((n + 7) / 8, sh, &ngrp);
+    const int ng_col = m >= 0 ? (m + 4) / 4 : 0;  // groups of <= 4 |kz|
+    const int gi = block_scan_excl(ng_col, sh, &ngrp);
     if (n > 0) {
         KCol c;
         c.kx = kx;
@@ -166,11 +167,11 @@ __global__ void __launch_bounds__(512) k_noalloc_setup(NAParams p, unsigned char
             }
             kvec[kb + kz + m] = v;
         }
-        for (int g = 0; g < (n + 7) / 8; ++g) {
+        for (int g = 0; g < ng_col; ++g) {
             KGroup G;
             G.col = ci;
-            G.kz0 = -m + 8 * g;
-            G.n = min(8, m - G.kz0 + 1);
+            G.kz0 = 4 * g;
+            G.n = min(4, m - G.kz0 + 1);
             G.pad = 0;
             kgrp[gi + g] = G;
         }

@@ -67,7 +67,8 @@ struct KVec {
 struct KCol {
     int kx, ky, m, k_begin;
 };
-// Structure-factor work item: up to 8 consecutive kz of one column.
+// Structure-factor work item: up to 4 consecutive |kz| of one column, starting
+// at kz0 >= 0; each |kz| stands for the pair kz = +|kz|, -|kz|.
 struct KGroup {
     int col, kz0, n, pad;
 };
