@@ -20,6 +20,7 @@
 //              molecule real-space pairs (erfc - 1), quartic-Morse bonds, HOH
 //              angle (FP64 difference vectors), M-site chain rule;
 //   k_lj       O-O Lennard-Jones over the CSR Verlet list, one warp per row.
+//   k_lj_dense O-O Lennard-Jones of the device stepper (mixed), all pairs from shared memory.
 // The kernels are templated on the arithmetic type: double for the parity
 // mode, float (FP64 accumulation across tiles/chunks/planes) for the mixed
 // mode. Mode-1 jobs compute the directional derivative of the intermolecular
@@ -64,21 +65,41 @@ template <> __device__ __forceinline__ double sys_ibox<double>(const SysDev &S, 
 
 __device__ __forceinline__ int chunk_lo(int n, int c, int nc) { return (int)(((long long)n * c) / nc); }
 
-// Real-space pair kernel pieces. For FP32: 1/r from rsqrtf, exp(-x^2) from the
-// exp2 unit, and erfc(x) = t P(t) exp(-x^2), t = 1 / (1 + p x), the rational
-// approximation of Abramowitz & Stegun, Handbook of Mathematical Functions,
-// eq. 7.1.26 (absolute error <= 1.5e-7), which reuses the Gaussian the force
-// needs anyway. For FP64 the library functions are used.
+// Real-space pair kernel pieces. For FP32: 1/r, exp(-x^2) and 1/(1 + p x) from
+// the approximate special-function instructions of PTX (rsqrt.approx,
+// ex2.approx, rcp.approx: relative errors of a few ulp), and erfc(x) =
+// t P(t) exp(-x^2), t = 1 / (1 + p x), the rational approximation of
+// Abramowitz & Stegun, Handbook of Mathematical Functions, eq. 7.1.26 (absolute
+// error <= 1.5e-7, which bounds the accuracy of the whole term), reusing the
+// Gaussian the force needs anyway. For FP64 the library functions are used.
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+constexpr float AS_P = 0.3275911f;  // A&S 7.1.26
+__device__ __forceinline__ float as_poly(float t) {
+    return fmaf(fmaf(fmaf(fmaf(1.061405429f, t, -1.453152027f), t, 1.421413741f), t, -0.284496736f), t,
+                0.254829592f);
+}
 __device__ __forceinline__ void pair_terms(float r2, float kap, float kap2, float *inv, float *ex, float *ec) {
-    const float iv = rsqrtf(r2);
+    const float iv = rsqrt_approx(r2);
     const float x = kap * (r2 * iv);
-    const float e = exp2f(-kap2 * r2 * 1.4426950408889634f);
-    const float t = __frcp_rn(fmaf(0.3275911f, x, 1.0f));
-    const float p = fmaf(fmaf(fmaf(fmaf(1.061405429f, t, -1.453152027f), t, 1.421413741f), t, -0.284496736f), t,
-                         0.254829592f);
+    const float e = ex2_approx(-kap2 * r2 * 1.4426950408889634f);
+    const float t = rcp_approx(fmaf(AS_P, x, 1.0f));
     *inv = iv;
     *ex = e;
-    *ec = t * p * e;
+    *ec = t * as_poly(t) * e;
 }
 __device__ __forceinline__ void pair_terms(double r2, double kap, double kap2, double *inv, double *ex, double *ec) {
     const double r = sqrt(r2);
@@ -178,6 +199,35 @@ __global__ void __launch_bounds__(128) k_prep(EvalArgs a) {
     }
 }
 
+// Running sum s (+ compensation c) += v, Kahan's compensated summation.
+template <typename R>
+__device__ __forceinline__ void kahan_add(R &s, R &c, R v) {
+    const R y = v - c;
+    const R t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+// Partial site-force planes: FP64 in the FP64 form; FP32 in the mixed form
+// (each plane is a compensated FP32 sum rounded once; k_combine_f32 adds the
+// planes with compensation), which halves their traffic and keeps the plane
+// sum off the FP64 pipe.
+template <typename R>
+__device__ __forceinline__ void store_plane(double *part, size_t at3, R x, R y, R z);
+template <>
+__device__ __forceinline__ void store_plane<double>(double *part, size_t at3, double x, double y, double z) {
+    part[at3] = x;
+    part[at3 + 1] = y;
+    part[at3 + 2] = z;
+}
+template <>
+__device__ __forceinline__ void store_plane<float>(double *part, size_t at3, float x, float y, float z) {
+    float *p = reinterpret_cast<float *>(part) + at3;
+    p[0] = x;
+    p[1] = y;
+    p[2] = z;
+}
+
 // ---- k_real: intermolecular real-space Ewald ----------------------------------
 constexpr int RT = 128;
 
@@ -258,16 +308,79 @@ __global__ void __launch_bounds__(RT) k_real(EvalArgs a) {
         Fz += (double)fz;
         E += (double)e;
     }
-    if (act) {
-        double *fs = a.part + 3 * ((size_t)rj * a.total_sites + J.site_off + i);
-        fs[0] = Fx;
-        fs[1] = Fy;
-        fs[2] = Fz;
-    }
+    if (act) store_plane<R>(a.part, 3 * ((size_t)rj * a.total_sites + J.site_off + i), (R)Fx, (R)Fy, (R)Fz);
     if (MODE == 0) {
         const double t = block_sum(0.5 * E, red);
         if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
     }
+}
+
+// FP32 form of k_real<float, 0> (energies and forces): the pair term is
+// q_i q_j [A, (A + B) / r^2] with A = erfc(kappa r) / r and
+// B = (2 kappa / sqrt(pi)) exp(-kappa^2 r^2); q_i is factored out of the sums,
+// the same-molecule exclusion joins the cutoff predicate, and each 128-site
+// tile's FP32 sums are added into Kahan-compensated FP32 running sums (FP64
+// only when the plane is written).
+__global__ void __launch_bounds__(RT) k_real_f32(EvalArgs a) {
+    const int rj = blockIdx.y, jb = blockIdx.z;
+    const Job J = a.jobs[jb];
+    const SysDev &S = a.sys[J.sys];
+    const int ns = S.n_sites;
+    if (blockIdx.x * RT >= ns) return;
+    const int i = blockIdx.x * RT + threadIdx.x;
+    const bool act = i < ns;
+    const int j0 = chunk_lo(ns, rj, a.n_rj), j1 = chunk_lo(ns, rj + 1, a.n_rj);
+    const float4 *sites = reinterpret_cast<const float4 *>(a.sites) + J.site_off;
+    __shared__ float4 sj[RT];
+    __shared__ double red[RT / 32];
+    const float L0 = S.boxf[0], L1 = S.boxf[1], L2 = S.boxf[2];
+    const float I0 = S.inv_boxf[0], I1 = S.inv_boxf[1], I2 = S.inv_boxf[2];
+    const float rc2 = (float)S.rc_sq, ka = (float)(0.3275911 * S.kappa);
+    const float cex = (float)(-S.kappa * S.kappa * 1.4426950408889634), pref = (float)S.ewald_pref;
+    float4 si = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (act) si = sites[i];
+    const int mlo = (i / 3) * 3;  // first site of i's molecule
+    float Sx = 0.f, Sy = 0.f, Sz = 0.f, Se = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f, Ce = 0.f;
+    for (int t0 = j0; t0 < j1; t0 += RT) {
+        __syncthreads();
+        if (t0 + threadIdx.x < j1) sj[threadIdx.x] = sites[t0 + threadIdx.x];
+        __syncthreads();
+        const int nj = min(RT, j1 - t0);
+        const int moff = mlo - t0;  // same molecule: (unsigned)(jj - moff) < 3
+        float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
+        if (act) {
+#pragma unroll 4
+            for (int jj = 0; jj < nj; ++jj) {
+                const float4 b = sj[jj];
+                float dx = si.x - b.x, dy = si.y - b.y, dz = si.z - b.z;
+                dx = fmaf(-L0, rintf(dx * I0), dx);
+                dy = fmaf(-L1, rintf(dy * I1), dy);
+                dz = fmaf(-L2, rintf(dz * I2), dz);
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                if (r2 < rc2 && (unsigned)(jj - moff) >= 3u) {
+                    const float iv = rsqrt_approx(r2);
+                    const float ex = ex2_approx(cex * r2);
+                    const float t = rcp_approx(fmaf(ka, r2 * iv, 1.0f));
+                    const float A = (t * as_poly(t)) * ex * iv;
+                    const float w = b.w * fmaf(pref, ex, A) * (iv * iv);
+                    e = fmaf(b.w, A, e);
+                    fx = fmaf(w, dx, fx);
+                    fy = fmaf(w, dy, fy);
+                    fz = fmaf(w, dz, fz);
+                }
+            }
+        }
+        kahan_add(Sx, Cx, fx);
+        kahan_add(Sy, Cy, fy);
+        kahan_add(Sz, Cz, fz);
+        kahan_add(Se, Ce, e);
+    }
+    const double qi = (double)si.w;
+    if (act)
+        store_plane<float>(a.part, 3 * ((size_t)rj * a.total_sites + J.site_off + i), si.w * (Sx - Cx),
+                           si.w * (Sy - Cy), si.w * (Sz - Cz));
+    const double t = block_sum(0.5 * qi * ((double)Se - (double)Ce), red);
+    if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
 }
 
 // ---- k_ksk: structure factors ---------------------------------------------------
@@ -280,14 +393,6 @@ constexpr int KT = 128;  // threads (k groups) per block
 constexpr int CH = 32;   // sites per shared-memory chunk
 constexpr int KZ = 4;    // |kz| values per group (each covering +kz and -kz)
 
-// Running sum s (+ compensation c) += v, Kahan's compensated summation.
-template <typename R>
-__device__ __forceinline__ void kahan_add(R &s, R &c, R v) {
-    const R y = v - c;
-    const R t = s + y;
-    c = (t - s) - y;
-    s = t;
-}
 
 template <typename R, int MODE>
 __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
@@ -497,7 +602,8 @@ __global__ void __launch_bounds__(FT) k_kforce(EvalArgs a) {
     if (MODE == 1 && act) ui = reinterpret_cast<const V4<R> *>(a.tan_sites)[J.site_off + i];
     const R bx = (R)(2.0 * PI_REF * S.inv_box[0]), by = (R)(2.0 * PI_REF * S.inv_box[1]),
             bz = (R)(2.0 * PI_REF * S.inv_box[2]);
-    double Fx = 0.0, Fy = 0.0, Fz = 0.0;
+    // per-batch sums added into Kahan-compensated running sums in the working precision
+    R Fx = 0, Fy = 0, Fz = 0, Cx = 0, Cy = 0, Cz = 0;
     const int ii = act ? i : 0;
     const V2<R> *wsk = reinterpret_cast<const V2<R> *>(a.wsk) + J.sk_off;
     const V2<R> *wdsk = reinterpret_cast<const V2<R> *>(a.wdsk) + J.sk_off;
@@ -551,22 +657,20 @@ __global__ void __launch_bounds__(FT) k_kforce(EvalArgs a) {
             fy += by * (R)C.ky * v;
             fz += bz * vz;
         }
-        Fx += (double)fx;
-        Fy += (double)fy;
-        Fz += (double)fz;
+        kahan_add(Fx, Cx, fx);
+        kahan_add(Fy, Cy, fy);
+        kahan_add(Fz, Cz, fz);
     }
-    if (act) {
-        double *fs = a.part + 3 * ((size_t)(a.n_rj + kc) * a.total_sites + J.site_off + i);
-        fs[0] = Fx;
-        fs[1] = Fy;
-        fs[2] = Fz;
-    }
+    if (act) store_plane<R>(a.part, 3 * ((size_t)(a.n_rj + kc) * a.total_sites + J.site_off + i), Fx - Cx, Fy - Cy, Fz - Cz);
 }
 
 // ---- k_combine: partial sums, short-range terms and the M-site chain rule ---------
 
+// Minimum image of an intramolecular vector. |r / L| is far below 1/2, where
+// round(r * (1/L)) and the reference's round(r / L) agree (both 0, or the same
+// integer for a molecule split by wrapping), so no FP64 division is needed.
 __device__ __forceinline__ void min_image3(double *r, const SysDev &S) {
-    for (int d = 0; d < 3; ++d) r[d] -= S.box[d] * round(r[d] / S.box[d]);
+    for (int d = 0; d < 3; ++d) r[d] -= S.box[d] * round(r[d] * S.inv_box[d]);
 }
 
 // same-molecule real-space pair with erfc - 1 (forces.cpp:141-177); the
@@ -682,6 +786,146 @@ __global__ void __launch_bounds__(128) k_combine(EvalArgs a) {
     }
     if (J.mode == 0) {
         if (m == 0 && !a.sr_only) e -= S.self_energy;
+        const double t = block_sum(e, red);
+        if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
+    }
+}
+
+// Mixed form of k_combine: the FP32 planes are added with Kahan compensation;
+// the atom differences are formed in FP64 and rounded to FP32 (intramolecular
+// vectors are ~1-3 bohr, so FP32 keeps them to ~1e-7 relative); the bond
+// lengths, whose offsets from r_eq set the stiff Morse force, are taken to FP64
+// accuracy as l = l0 + (s - l0^2) / (2 l0), with s = |r|^2 in FP64 and l0 its
+// FP32 square root; everything else (same-molecule Ewald, Morse, angle, chain
+// rule) is FP32, and the energy is accumulated in FP64.
+__device__ __forceinline__ void min_image3f(float *r, const SysDev &S) {
+    for (int d = 0; d < 3; ++d) r[d] = fmaf(-S.boxf[d], rintf(r[d] * S.inv_boxf[d]), r[d]);
+}
+
+// same-molecule real-space pair with erfc - 1 (forces.cpp:141-177), FP32
+__device__ __forceinline__ float ewald_same_mol_f32(const float *rd, float qiqj, const SysDev &S, float *fi, float *fj) {
+    const float r2 = rd[0] * rd[0] + rd[1] * rd[1] + rd[2] * rd[2];
+    if (!(r2 < (float)S.rc_sq)) return 0.f;
+    const float rl = sqrtf(r2), inv = 1.0f / rl, kap = (float)S.kappa;
+    const float e = qiqj * inv * (erfcf(kap * rl) - 1.0f);
+    const float ff = (e + qiqj * (float)S.ewald_pref * expf(-(kap * kap) * r2)) * inv * inv;
+    for (int d = 0; d < 3; ++d) {
+        fi[d] += ff * rd[d];
+        fj[d] -= ff * rd[d];
+    }
+    return e;
+}
+
+__global__ void __launch_bounds__(128) k_combine_f32(EvalArgs a) {
+    const int jb = blockIdx.y;
+    const Job J = a.jobs[jb];
+    const SysDev &S = a.sys[J.sys];
+    const int N = S.n_mols;
+    if (blockIdx.x * blockDim.x >= N) return;
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double red[4];
+    double e = 0.0;
+    if (m < N) {
+        const double *q = a.pos + J.pos_off + 9 * m;
+        double *f = a.out + J.out_off + 9 * m;
+        float fs[9], cs[9];
+        for (int k = 0; k < 9; ++k) fs[k] = cs[k] = 0.f;
+        {
+            const int np = a.n_rj + a.n_kc;
+            const size_t stride = 3 * (size_t)a.total_sites;
+            const float *pl = reinterpret_cast<const float *>(a.part) + 3 * ((size_t)J.site_off + 3 * m);
+            for (int p = 0; p < np; ++p)
+                for (int k = 0; k < 9; ++k) kahan_add(fs[k], cs[k], pl[p * stride + k]);
+            for (int k = 0; k < 9; ++k) fs[k] -= cs[k];
+        }
+        float fa[9];
+        for (int k = 0; k < 9; ++k) fa[k] = 0.f;
+        if (J.mode == 0) {
+            const Consts &C = a.c;
+            const double g = C.gamma_vs, h = 0.5 * (1.0 - g);
+            const double *cq = a.charge + S.chg_off + 3 * m;
+            // charge sites M, H1, H2 (forces.cpp:558-564) and their differences
+            double site[9];
+            for (int d = 0; d < 3; ++d) {
+                site[d] = g * q[d] + h * (q[3 + d] + q[6 + d]);
+                site[3 + d] = q[3 + d];
+                site[6 + d] = q[6 + d];
+            }
+            float dm1[3], dm2[3], d12[3];
+            for (int d = 0; d < 3; ++d) {
+                dm1[d] = (float)(site[d] - site[3 + d]);
+                dm2[d] = (float)(site[d] - site[6 + d]);
+                d12[d] = (float)(site[3 + d] - site[6 + d]);
+            }
+            min_image3f(dm1, S);
+            min_image3f(dm2, S);
+            min_image3f(d12, S);
+            float ef = ewald_same_mol_f32(dm1, (float)(cq[0] * cq[1]), S, fs, fs + 3);
+            ef += ewald_same_mol_f32(dm2, (float)(cq[0] * cq[2]), S, fs, fs + 6);
+            ef += ewald_same_mol_f32(d12, (float)(cq[1] * cq[2]), S, fs + 3, fs + 6);
+            e += (double)ef;
+            // quartic Morse bonds (forces.cpp:65-93, :519-551)
+            double rad[3], rbd[3];
+            for (int d = 0; d < 3; ++d) {
+                rad[d] = q[d] - q[3 + d];
+                rbd[d] = q[d] - q[6 + d];
+            }
+            min_image3(rad, S);
+            min_image3(rbd, S);
+            float ra[3], rb[3], xs[2], ls[2];
+            for (int d = 0; d < 3; ++d) {
+                ra[d] = (float)rad[d];
+                rb[d] = (float)rbd[d];
+            }
+            for (int bnd = 0; bnd < 2; ++bnd) {
+                const double *r = bnd ? rbd : rad;
+                const double s2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+                const float l0 = sqrtf((float)s2);
+                const float corr = (float)(s2 - (double)l0 * (double)l0) * (0.5f / l0);
+                xs[bnd] = (float)((double)l0 - C.roheq) + corr;
+                ls[bnd] = l0 + corr;
+            }
+            const float ar2 = (float)C.ar2, ar3 = (float)C.ar3, ar4 = (float)C.ar4fac, Dr = (float)C.Dr;
+            float eb = 0.f;
+            for (int bnd = 0; bnd < 2; ++bnd) {
+                const float *r = bnd ? rb : ra;
+                const float x = xs[bnd], x2 = x * x, x3 = x2 * x, x4 = x2 * x2;
+                eb += Dr * (ar2 * x2 - ar3 * x3 + ar4 * x4);
+                const float gg = (2.f * ar2 * x - 3.f * ar3 * x2 + 4.f * ar4 * x3) * Dr / ls[bnd];
+                for (int d = 0; d < 3; ++d) {
+                    fa[d] -= gg * r[d];
+                    fa[3 + 3 * bnd + d] += gg * r[d];
+                }
+            }
+            e += (double)eb;
+            // harmonic HOH angle (forces.cpp:96-138)
+            {
+                const float la = ls[0], lb = ls[1];
+                const float dot = ra[0] * rb[0] + ra[1] * rb[1] + ra[2] * rb[2];
+                const float ia = 1.f / la, ib = 1.f / lb, iab = ia * ib;
+                const float c = dot * iab;
+                const float dacos = 1.f / sqrtf(1.f - c * c);
+                const float ca = dot * ia * ia * iab, cb = dot * ib * ib * iab;
+                const float dth = acosf(c) - (float)C.theta_eq;
+                e += 0.5 * C.ktheta * (double)dth * (double)dth;
+                const float gp = (float)C.ktheta * dth * dacos;
+                for (int d = 0; d < 3; ++d) {
+                    fa[d] += gp * (iab * (ra[d] + rb[d]) - ca * ra[d] - cb * rb[d]);
+                    fa[3 + d] -= gp * (iab * rb[d] - ca * ra[d]);
+                    fa[6 + d] -= gp * (iab * ra[d] - cb * rb[d]);
+                }
+            }
+        }
+        // M-site chain rule (forces.cpp:613-619)
+        const float g = (float)a.c.gamma_vs, h = 0.5f * (1.0f - g);
+        for (int d = 0; d < 3; ++d) {
+            f[d] = (double)(fa[d] + g * fs[d]);
+            f[3 + d] = (double)(fa[3 + d] + fs[3 + d] + h * fs[d]);
+            f[6 + d] = (double)(fa[6 + d] + fs[6 + d] + h * fs[d]);
+        }
+    }
+    if (J.mode == 0) {
+        if (m == 0) e -= S.self_energy;
         const double t = block_sum(e, red);
         if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
     }
@@ -821,14 +1065,121 @@ __global__ void __launch_bounds__(128) k_lj(EvalArgs a) {
     if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
 }
 
+// ---- k_lj_dense: O-O Lennard-Jones of the device stepper, mixed precision -------
+// The stepper rebuilds its Verlet list whenever the skin test (update.cpp:356-385)
+// fires, before the forces are evaluated, so the list holds every pair that can
+// be inside r_cut: the sum over all pairs with r^2 < r_cut^2 has the pair set of
+// the list loop of forces.cpp:489-515. This kernel forms that sum without going
+// through the list: the bead's wrapped oxygen positions are staged through
+// shared memory, LJD_SUB lanes share a row and split its j's (each warp reads
+// LJD_SUB consecutive positions per step: one shared-memory wavefront), and the
+// row's sums are reduced over those lanes in FP32 with shuffles. Cutoff band and
+// half-box ties take the reference's FP64 arithmetic as in k_lj. Each pair is
+// seen from both ends; the energy is halved.
+constexpr int LJD_SUB = 8;                  // lanes per row
+constexpr int LJD_ROWS = 128 / LJD_SUB;     // rows per 128-thread block
+constexpr int LJD_CH = 1024;                // oxygens per shared-memory chunk
+
+__global__ void __launch_bounds__(128) k_lj_dense(EvalArgs a) {
+    const int jb = blockIdx.y;
+    const Job J = a.jobs[jb];
+    const SysDev &S = a.sys[J.sys];
+    const int N = S.n_mols;
+    if (blockIdx.x * LJD_ROWS >= N) return;
+    __shared__ float4 sj[LJD_CH];
+    __shared__ double red[4];
+    const int sub = threadIdx.x & (LJD_SUB - 1);
+    const int i = blockIdx.x * LJD_ROWS + threadIdx.x / LJD_SUB;
+    const bool act = i < N;
+    const Consts &C = a.c;
+    const double rc2 = C.r_cut_sq;
+    const float rc2f = (float)rc2, band = 1e-5f * rc2f, tie = 1e-5f;
+    const float4 *opos = reinterpret_cast<const float4 *>(a.opos) + J.site_off / 3;
+    const double *q = a.pos + J.pos_off;
+    const float L0 = sys_box<float>(S, 0), L1 = sys_box<float>(S, 1), L2 = sys_box<float>(S, 2);
+    const float I0 = sys_ibox<float>(S, 0), I1 = sys_ibox<float>(S, 1), I2 = sys_ibox<float>(S, 2);
+    const float s6c = (float)C.sigmalj6, s12c = (float)C.sigmalj12;
+    const float eps4 = (float)(4.0 * C.epslj), eps24 = (float)(24.0 * C.epslj), ecut = (float)C.e_cut;
+    // two images of a pair tied in dimension d are both L_d / 2 away in d: the tie
+    // can change the cutoff decision only when (L_d / 2)^2 is not clearly above r_cut^2
+    const bool tx_on = 0.25 * S.box[0] * S.box[0] < 1.001 * rc2, ty_on = 0.25 * S.box[1] * S.box[1] < 1.001 * rc2,
+               tz_on = 0.25 * S.box[2] * S.box[2] < 1.001 * rc2;
+    float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (act) oi = opos[i];
+    float fx = 0.f, fy = 0.f, fz = 0.f, el = 0.f;
+    for (int t0 = 0; t0 < N; t0 += LJD_CH) {
+        const int nj = min(LJD_CH, N - t0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < nj; k += 128) sj[k] = opos[t0 + k];
+        __syncthreads();
+        if (!act) continue;
+#pragma unroll 4
+        for (int jj = sub; jj < nj; jj += LJD_SUB) {
+            const int j = t0 + jj;
+            const float4 o = sj[jj];
+            // wrapped positions lie in [0, L]: |t| <= 1, and two images tie at |t| = 1/2;
+            // a tie decides anything only where half a box lies inside r_cut
+            const float t0x = (oi.x - o.x) * I0, t0y = (oi.y - o.y) * I1, t0z = (oi.z - o.z) * I2;
+            bool exact = (tx_on && fabsf(fabsf(t0x) - 0.5f) < tie) || (ty_on && fabsf(fabsf(t0y) - 0.5f) < tie) ||
+                         (tz_on && fabsf(fabsf(t0z) - 0.5f) < tie);
+            float r0 = (oi.x - o.x) - L0 * rintf(t0x);
+            float r1 = (oi.y - o.y) - L1 * rintf(t0y);
+            float r2 = (oi.z - o.z) - L2 * rintf(t0z);
+            float rr = r0 * r0 + r1 * r1 + r2 * r2;
+            exact = exact || fabsf(rr - rc2f) <= band;
+            bool in;
+            if (exact) {
+                double rd[3];
+                const double r2d = lj_exact_disp(q + 9 * i, q + 9 * j, S, rd);
+                r0 = (float)rd[0];
+                r1 = (float)rd[1];
+                r2 = (float)rd[2];
+                rr = (float)r2d;
+                in = r2d < rc2;
+            } else {
+                in = rr < rc2f;
+            }
+            if (in && j != i) {
+                const float i2 = 1.0f / rr, i6 = i2 * i2 * i2;
+                const float s6 = i6 * s6c, s12 = i6 * i6 * s12c;
+                const float en = s12 - s6;
+                el += en * eps4 - ecut;
+                const float ff = (en + s12) * eps24 * i2;
+                fx += ff * r0;
+                fy += ff * r1;
+                fz += ff * r2;
+            }
+        }
+    }
+#pragma unroll
+    for (int m = 1; m < LJD_SUB; m <<= 1) {
+        fx += __shfl_xor_sync(0xffffffffu, fx, m);
+        fy += __shfl_xor_sync(0xffffffffu, fy, m);
+        fz += __shfl_xor_sync(0xffffffffu, fz, m);
+        el += __shfl_xor_sync(0xffffffffu, el, m);
+    }
+    double e = 0.0;
+    if (act && sub == 0) {
+        double *f = a.out + J.out_off;
+        f[9 * i] += (double)fx;
+        f[9 * i + 1] += (double)fy;
+        f[9 * i + 2] += (double)fz;
+        e = 0.5 * (double)el;
+    }
+    const double t = block_sum(e, red);
+    if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
+}
+
 // site-force output of the reciprocal-space-only path: out += sum of the k-chunk planes
+template <typename R>
 __global__ void k_sum_parts(EvalArgs a) {
     const Job J = a.jobs[blockIdx.y];
     const SysDev &S = a.sys[J.sys];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * S.n_sites) return;
+    const R *part = reinterpret_cast<const R *>(a.part);
     double v = 0.0;
-    for (int p = 0; p < a.n_rj + a.n_kc; ++p) v += a.part[3 * ((size_t)p * a.total_sites + J.site_off) + t];
+    for (int p = 0; p < a.n_rj + a.n_kc; ++p) v += (double)part[3 * ((size_t)p * a.total_sites + J.site_off) + t];
     a.out[J.out_off + t] += v;
 }
 
@@ -883,7 +1234,8 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n) {
     a.n_kc = chunks_for((long long)tiles * a.n_jobs, MAX_KC);
     k_prep<R><<<dim3((ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
     if (a.mode == 0) {
-        k_real<R, 0><<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
+        if (sizeof(R) == 4) k_real_f32<<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
+        else k_real<R, 0><<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         k_ksk<R, 0><<<dim3(ktiles, a.n_sc, a.n_jobs), KT, ksk_smem<R>(a.max_kmax), s>>>(a);
         k_sk_reduce<R, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
         k_kforce<R, 0><<<dim3(tiles, a.n_kc, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
@@ -894,10 +1246,13 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n) {
         k_kforce<R, 1><<<dim3(tiles, a.n_kc, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
     }
     const dim3 gm((a.max_mols + 127) / 128, a.n_jobs);
-    k_combine<R><<<gm, 128, 0, s>>>(a);
+    if (sizeof(R) == 4) k_combine_f32<<<gm, 128, 0, s>>>(a);
+    else k_combine<double><<<gm, 128, 0, s>>>(a);
     if (n) *n += 6;
     if (a.mode == 0) {
-        if (a.lj_full) k_lj<R, 1><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
+        if (sizeof(R) == 4 && a.lj_full)
+            k_lj_dense<<<dim3((a.max_mols + LJD_ROWS - 1) / LJD_ROWS, a.n_jobs), 128, 0, s>>>(a);
+        else if (a.lj_full) k_lj<R, 1><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
         else k_lj<R, 0><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
         if (n) *n += 1;
     }
@@ -924,7 +1279,7 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
         if (mixed) k_prep<float><<<gs, 128, 0, s>>>(a);
         else k_prep<double><<<gs, 128, 0, s>>>(a);
     } else if (n == "real") {
-        if (mixed) k_real<float, 0><<<gr, RT, 0, s>>>(a);
+        if (mixed) k_real_f32<<<gr, RT, 0, s>>>(a);
         else k_real<double, 0><<<gr, RT, 0, s>>>(a);
     } else if (n == "ksk") {
         if (mixed) k_ksk<float, 0><<<gk, KT, ksk_smem<float>(a.max_kmax), s>>>(a);
@@ -936,11 +1291,11 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
         if (mixed) k_kforce<float, 0><<<gf, FT, kforce_smem<float>(a.max_kmax), s>>>(a);
         else k_kforce<double, 0><<<gf, FT, kforce_smem<double>(a.max_kmax), s>>>(a);
     } else if (n == "combine") {
-        if (mixed) k_combine<float><<<gm, 128, 0, s>>>(a);
+        if (mixed) k_combine_f32<<<gm, 128, 0, s>>>(a);
         else k_combine<double><<<gm, 128, 0, s>>>(a);
     } else if (n == "lj") {
         if (mixed) {
-            if (a.lj_full) k_lj<float, 1><<<gl, 128, 0, s>>>(a);
+            if (a.lj_full) k_lj_dense<<<dim3((a.max_mols + LJD_ROWS - 1) / LJD_ROWS, a.n_jobs), 128, 0, s>>>(a);
             else k_lj<float, 0><<<gl, 128, 0, s>>>(a);
         } else {
             if (a.lj_full) k_lj<double, 1><<<gl, 128, 0, s>>>(a);
@@ -1000,7 +1355,8 @@ void launch_kwald_only(const EvalArgs &a0, bool mixed, cudaStream_t s, unsigned 
         k_sk_reduce<double, 0><<<gr, 128, 0, s>>>(a);
         k_kforce<double, 0><<<gf, FT, kforce_smem<double>(a.max_kmax), s>>>(a);
     }
-    k_sum_parts<<<dim3((3 * ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
+    if (mixed) k_sum_parts<float><<<dim3((3 * ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
+    else k_sum_parts<double><<<dim3((3 * ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
     if (n) *n += 5;
 }
 

@@ -85,16 +85,18 @@ __global__ void __launch_bounds__(512) k_skin_rebuild(ListArgs a) {
     const int N = S.n_mols;
     double *disp = a.disp + S.d_off + (size_t)bead * 3 * N;
     extern __shared__ unsigned char smem[];
-    __shared__ double red[2][33];
+    __shared__ unsigned long long red[2][33];
     __shared__ int wtot[33];
     __shared__ int do_build;
 
     if (!a.force_rebuild) {
-        // two largest squared displacements (update.cpp:361-375)
-        double m1 = 0.0, m2 = 0.0;
+        // two largest squared displacements (update.cpp:361-375). Squared norms are
+        // non-negative doubles, which order exactly as their 64-bit patterns do, so
+        // the top-2 selection runs on integer compares instead of the FP64 pipe.
+        unsigned long long m1 = 0ull, m2 = 0ull;
         for (int i = threadIdx.x; i < N; i += blockDim.x) {
-            double x = disp[3 * i], y = disp[3 * i + 1], z = disp[3 * i + 2];
-            double d2 = x * x + y * y + z * z;
+            const double x = disp[3 * i], y = disp[3 * i + 1], z = disp[3 * i + 2];
+            const unsigned long long d2 = (unsigned long long)__double_as_longlong(x * x + y * y + z * z);
             if (d2 > m1) {
                 m2 = m1;
                 m1 = d2;
@@ -103,8 +105,8 @@ __global__ void __launch_bounds__(512) k_skin_rebuild(ListArgs a) {
             }
         }
         for (int o = 16; o > 0; o >>= 1) {
-            double b1 = __shfl_xor_sync(0xffffffffu, m1, o), b2 = __shfl_xor_sync(0xffffffffu, m2, o);
-            double n1 = fmax(m1, b1), n2 = fmax(fmin(m1, b1), fmax(m2, b2));
+            const unsigned long long b1 = __shfl_xor_sync(0xffffffffu, m1, o), b2 = __shfl_xor_sync(0xffffffffu, m2, o);
+            const unsigned long long n1 = max(m1, b1), n2 = max(min(m1, b1), max(m2, b2));
             m1 = n1;
             m2 = n2;
         }
@@ -115,14 +117,15 @@ __global__ void __launch_bounds__(512) k_skin_rebuild(ListArgs a) {
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            double t1 = 0.0, t2 = 0.0;
+            unsigned long long t1 = 0ull, t2 = 0ull;
             for (int k = 0; k < nw; ++k) {
-                double b1 = red[0][k], b2 = red[1][k];
-                double n1 = fmax(t1, b1), n2 = fmax(fmin(t1, b1), fmax(t2, b2));
+                const unsigned long long b1 = red[0][k], b2 = red[1][k];
+                const unsigned long long n1 = max(t1, b1), n2 = max(min(t1, b1), max(t2, b2));
                 t1 = n1;
                 t2 = n2;
             }
-            do_build = (sqrt(t1) + sqrt(t2) > S.skin_margin) ? 1 : 0;
+            do_build = (sqrt(__longlong_as_double((long long)t1)) + sqrt(__longlong_as_double((long long)t2)) >
+                        S.skin_margin) ? 1 : 0;
         }
         __syncthreads();
         if (!do_build) return;

@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
     double *Xp = Xq + P * C;
     double *Zq = Xp + P * C;  // folded sums / differences, then back-transformed values
     double *Zp = Zq + P * C;
-    __shared__ double red[8];
+    __shared__ double hred[256];
     // Rows 0..P/2 of C are symmetric in b <-> P-b and rows P/2+1..P-1 are
     // antisymmetric (zero at b = 0 and b = P/2), so each transform is applied to
     // s_b = x_b + x_{P-b} and d_b = x_b - x_{P-b}, b = 1..h: half the FMAs.
@@ -200,8 +200,15 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
             a.disp[S.d_off + (long long)k * 3 * S.n_mols + 3 * (col / 9) + (col % 9)] += qn - q_old;
     }
     if (flags & RF_THERMO) {
-        double t = block_sum(heat, red);
-        if (threadIdx.x == 0) atomicAdd(&a.run[W.sys].heat, t);
+        // one warp sums the block's values (8 a lane), then one 5-level shuffle reduction
+        hred[threadIdx.x] = heat;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double t = 0.0;
+            for (int k = threadIdx.x; k < (int)blockDim.x; k += 32) t += hred[k];
+            t = warp_sum(t);
+            if (threadIdx.x == 0) atomicAdd(&a.run[W.sys].heat, t);
+        }
     }
 }
 
@@ -217,7 +224,7 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
     double *Xq = sh;
     double *Xp = Xq + P * C;
     __shared__ double qbar[256];
-    __shared__ double red4[4][8];
+    __shared__ double red4[4][256];
     const long long at = S.q_off + (long long)b * S.n_dof + col;
     double qb = 0.0, pb = 0.0, fb = 0.0, fpb = 0.0;
     const double m = act ? a.mass[S.mass_off + col] : 1.0;
@@ -258,25 +265,24 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
         const int all = a.kcv_all_beads < 0 ? (S.propagator == 1) : a.kcv_all_beads;
         if (all || (b % 2 == 0)) tq = -(qb - qbar[c]) * fpb;
     }
-    // one fused block reduction of the four sums
-    kin = warp_sum(kin);
-    spring = warp_sum(spring);
-    tq = warp_sum(tq);
-    k0 = warp_sum(k0);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) {
-        red4[0][w] = kin;
-        red4[1][w] = spring;
-        red4[2][w] = tq;
-        red4[3][w] = k0;
-    }
+    // block reduction of the four sums: transposed through shared memory so that
+    // warp w sums quantity w (8 values a lane, then 5 shuffle levels), a third of
+    // the FP64 adds of four full warp reductions per warp
+    red4[0][threadIdx.x] = kin;
+    red4[1][threadIdx.x] = spring;
+    red4[2][threadIdx.x] = tq;
+    red4[3][threadIdx.x] = k0;
     __syncthreads();
-    if (threadIdx.x < 4) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (w < 4) {
         double t = 0.0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red4[threadIdx.x][k];
-        SysAcc *ac = &a.acc[W.sys];
-        double *dst = threadIdx.x == 0 ? &ac->kin : threadIdx.x == 1 ? &ac->spring : threadIdx.x == 2 ? &ac->kcv_tq : &ac->k0;
-        atomicAdd(dst, t);
+        for (int k = lane; k < (int)blockDim.x; k += 32) t += red4[w][k];
+        t = warp_sum(t);
+        if (lane == 0) {
+            SysAcc *ac = &a.acc[W.sys];
+            double *dst = w == 0 ? &ac->kin : w == 1 ? &ac->spring : w == 2 ? &ac->kcv_tq : &ac->k0;
+            atomicAdd(dst, t);
+        }
     }
 }
 
@@ -296,34 +302,46 @@ __global__ void k_centroid_ke(RingArgs a) {
 }
 
 // Gamma(shape) by Marsaglia & Tsang, "A simple method for generating gamma
-// variables" (ACM TOMS 26, 2000), for shape >= 1, with a bounded loop.
-__device__ double gamma_mt(double shape, const SysDev &S, int sys, unsigned long long st, bool *ok) {
+// variables" (ACM TOMS 26, 2000), for shape >= 1, with a bounded number of
+// candidates. Candidate `it` is drawn from Philox counters (2 it, 2 it + 1), so
+// the candidates are independent of one another: the 32 lanes of a warp test
+// 32 of them at once and the first accepted one (lowest `it`, found by ballot)
+// is the value the sequential loop would return. Called by a whole warp.
+__device__ double gamma_mt_warp(double shape, const SysDev &S, int sys, unsigned long long st, bool *ok) {
+    const int lane = threadIdx.x & 31;
     const double d = shape - 1.0 / 3.0, cc = 1.0 / sqrt(9.0 * d);
     uint32_t k0, k1;
     philox_key(S, sys, RNG_GAMMA, &k0, &k1);
-    for (uint32_t it = 0; it < 64; ++it) {
+    for (uint32_t base = 0; base < 64; base += 32) {
+        const uint32_t it = base + (uint32_t)lane;
         const double x = normal2(philox4x32_10(2 * it, 0u, (uint32_t)st, (uint32_t)(st >> 32), k0, k1)).x;
         double v = 1.0 + cc * x;
-        if (v <= 0.0) continue;
-        v = v * v * v;
-        const Philox4 r = philox4x32_10(2 * it + 1, 0u, (uint32_t)st, (uint32_t)(st >> 32), k0, k1);
-        const double u = u01_from(r.v[0], r.v[1]);
-        if (u < 1.0 - 0.0331 * x * x * x * x) return d * v;
-        if (log(u) < 0.5 * x * x + d * (1.0 - v + log(v))) return d * v;
+        bool acc = false;
+        if (v > 0.0) {
+            v = v * v * v;
+            const Philox4 r = philox4x32_10(2 * it + 1, 0u, (uint32_t)st, (uint32_t)(st >> 32), k0, k1);
+            const double u = u01_from(r.v[0], r.v[1]);
+            acc = (u < 1.0 - 0.0331 * x * x * x * x) || (log(u) < 0.5 * x * x + d * (1.0 - v + log(v)));
+        }
+        const unsigned hit = __ballot_sync(0xffffffffu, acc);
+        if (hit) return __shfl_sync(0xffffffffu, d * v, __ffs(hit) - 1);
     }
     *ok = false;
     return shape;
 }
 
+// One warp per system: the step's estimator record and the next centroid
+// draw for PILE-G. One block, so the step counters advance after every system.
 __global__ void k_finalize(FinalizeArgs a) {
     const unsigned long long st = *a.step;
     const unsigned long long rec = *a.records;
-    for (int s = a.sys_begin + threadIdx.x; s < a.sys_end; s += blockDim.x) {
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int s = a.sys_begin + (int)(threadIdx.x >> 5); s < a.sys_end; s += nw) {
         const SysDev &S = a.sys[s];
         SysAcc *ac = &a.acc[s];
         SysRun *run = &a.run[s];
         const int P = S.n_beads;
-        if (a.record) {
+        if (a.record && lane == 0) {
             double vsum = 0.0, veven = 0.0;
             for (int b = 0; b < P; ++b) {
                 const double e = a.energy[S.job_base + b];
@@ -365,12 +383,13 @@ __global__ void k_finalize(FinalizeArgs a) {
                 // g2 ~ chi^2 with (n_dof - 1) degrees of freedom: both branches of
                 // thermostat.cpp:102-110 draw exactly this distribution
                 bool ok = true;
-                g2 = 2.0 * gamma_mt(0.5 * (S.n_dof - 1), S, s, st, &ok);
-                if (!ok) atomicOr(a.status, (unsigned)ST_GAMMA_LIMIT);
+                g2 = 2.0 * gamma_mt_warp(0.5 * (S.n_dof - 1), S, s, st, &ok);
+                if (!ok && lane == 0) atomicOr(a.status, (unsigned)ST_GAMMA_LIMIT);
             }
-            run->alpha = sqrt((R * R + g2) / (2.0 * S.beta_n * ac->k0));
+            if (lane == 0) run->alpha = sqrt((R * R + g2) / (2.0 * S.beta_n * ac->k0));
         }
-        ac->kin = ac->spring = ac->kcv_tq = ac->k0 = ac->sc_extra = ac->rebuilds = 0.0;
+        __syncwarp();
+        if (lane == 0) ac->kin = ac->spring = ac->kcv_tq = ac->k0 = ac->sc_extra = ac->rebuilds = 0.0;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -522,7 +541,7 @@ void launch_centroid_ke(const RingArgs &a, cudaStream_t s, unsigned long long *n
 }
 
 void launch_finalize(const FinalizeArgs &a, cudaStream_t s, unsigned long long *n) {
-    k_finalize<<<1, 64, 0, s>>>(a);
+    k_finalize<<<1, 512, 0, s>>>(a);
     if (n) ++*n;
 }
 
