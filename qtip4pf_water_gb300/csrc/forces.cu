@@ -470,15 +470,25 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
 #pragma unroll
             for (int g = 0; g < KZ; ++g) {
                 const V2<R> z = tab[zrow[g] + c];
-                // A Z (kz = +az) and A conj(Z) (kz = -az) share their products
-                const R t1 = pr * z.x, t2 = pi * z.x;
-                const R erp = t1 - pi * z.y, eip = t2 + pr * z.y;
-                const R erm = t1 + pi * z.y, eim = t2 - pr * z.y;
-                sr[g][0] += erp;
-                si[g][0] += eip;
-                sr[g][1] += erm;
-                si[g][1] += eim;
-                if (MODE == 1) {
+                if (MODE == 0) {
+                    // A Z (kz = +az) and A conj(Z) (kz = -az) accumulated by FMAs alone
+                    sr[g][0] = fma(pr, z.x, sr[g][0]);
+                    sr[g][0] = fma(-pi, z.y, sr[g][0]);
+                    si[g][0] = fma(pi, z.x, si[g][0]);
+                    si[g][0] = fma(pr, z.y, si[g][0]);
+                    sr[g][1] = fma(pr, z.x, sr[g][1]);
+                    sr[g][1] = fma(pi, z.y, sr[g][1]);
+                    si[g][1] = fma(pi, z.x, si[g][1]);
+                    si[g][1] = fma(-pr, z.y, si[g][1]);
+                } else {
+                    // A Z (kz = +az) and A conj(Z) (kz = -az) share their products
+                    const R t1 = pr * z.x, t2 = pi * z.x;
+                    const R erp = t1 - pi * z.y, eip = t2 + pr * z.y;
+                    const R erm = t1 + pi * z.y, eim = t2 - pr * z.y;
+                    sr[g][0] += erp;
+                    si[g][0] += eip;
+                    sr[g][1] += erm;
+                    si[g][1] += eim;
                     const R kup = kxyu + kzr[g] * uz, kum = kxyu - kzr[g] * uz;
                     dsr[g][0] -= kup * eip;
                     dsi[g][0] += kup * erp;
@@ -1073,12 +1083,51 @@ __global__ void __launch_bounds__(128) k_lj(EvalArgs a) {
 // through the list: the bead's wrapped oxygen positions are staged through
 // shared memory, LJD_SUB lanes share a row and split its j's (each warp reads
 // LJD_SUB consecutive positions per step: one shared-memory wavefront), and the
-// row's sums are reduced over those lanes in FP32 with shuffles. Cutoff band and
-// half-box ties take the reference's FP64 arithmetic as in k_lj. Each pair is
+// row's sums are reduced over those lanes in FP32 with shuffles. Each pair is
 // seen from both ends; the energy is halved.
+//
+// Pairs whose FP32 r^2 lies in a narrow band around r_cut^2, or that sit at a
+// half-box tie where half a box is inside r_cut, must take the reference's FP64
+// arithmetic (as in k_lj). They are rare, and that FP64 code is kept out of the
+// main loop: the loop skips them and raises a block flag, and only blocks that
+// saw one run a second pass that evaluates exactly those pairs.
 constexpr int LJD_SUB = 8;                  // lanes per row
 constexpr int LJD_ROWS = 128 / LJD_SUB;     // rows per 128-thread block
 constexpr int LJD_CH = 1024;                // oxygens per shared-memory chunk
+
+struct LjdConst {
+    float L[3], I[3], rc2, band, tie, s6, s12, eps4, eps24, ecut;
+    int tie_mask;  // bit d: half of box side d is inside r_cut
+};
+
+// 0: outside r_cut; 1: inside, displacement in r; 2: needs the FP64 decision
+__device__ __forceinline__ int ljd_classify(const float4 &oi, const float4 &o, const LjdConst &K, float *r,
+                                            float *rr) {
+    const float dx = oi.x - o.x, dy = oi.y - o.y, dz = oi.z - o.z;
+    const float tx = dx * K.I[0], ty = dy * K.I[1], tz = dz * K.I[2];
+    // wrapped positions lie in [0, L]: |t| <= 1, and two images tie at |t| = 1/2
+    const bool tie = ((K.tie_mask & 1) && fabsf(fabsf(tx) - 0.5f) < K.tie) ||
+                     ((K.tie_mask & 2) && fabsf(fabsf(ty) - 0.5f) < K.tie) ||
+                     ((K.tie_mask & 4) && fabsf(fabsf(tz) - 0.5f) < K.tie);
+    r[0] = fmaf(-K.L[0], rintf(tx), dx);
+    r[1] = fmaf(-K.L[1], rintf(ty), dy);
+    r[2] = fmaf(-K.L[2], rintf(tz), dz);
+    *rr = fmaf(r[0], r[0], fmaf(r[1], r[1], r[2] * r[2]));
+    if (tie || fabsf(*rr - K.rc2) <= K.band) return 2;
+    return *rr < K.rc2 ? 1 : 0;
+}
+
+__device__ __forceinline__ void ljd_pair(const float *r, float rr, const LjdConst &K, float &fx, float &fy, float &fz,
+                                         float &el) {
+    const float i2 = rcp_approx(rr), i6 = i2 * i2 * i2;
+    const float s6 = i6 * K.s6, s12 = i6 * i6 * K.s12;
+    const float en = s12 - s6;
+    el += en * K.eps4 - K.ecut;
+    const float ff = (en + s12) * K.eps24 * i2;
+    fx = fmaf(ff, r[0], fx);
+    fy = fmaf(ff, r[1], fy);
+    fz = fmaf(ff, r[2], fz);
+}
 
 __global__ void __launch_bounds__(128) k_lj_dense(EvalArgs a) {
     const int jb = blockIdx.y;
@@ -1093,20 +1142,29 @@ __global__ void __launch_bounds__(128) k_lj_dense(EvalArgs a) {
     const bool act = i < N;
     const Consts &C = a.c;
     const double rc2 = C.r_cut_sq;
-    const float rc2f = (float)rc2, band = 1e-5f * rc2f, tie = 1e-5f;
-    const float4 *opos = reinterpret_cast<const float4 *>(a.opos) + J.site_off / 3;
-    const double *q = a.pos + J.pos_off;
-    const float L0 = sys_box<float>(S, 0), L1 = sys_box<float>(S, 1), L2 = sys_box<float>(S, 2);
-    const float I0 = sys_ibox<float>(S, 0), I1 = sys_ibox<float>(S, 1), I2 = sys_ibox<float>(S, 2);
-    const float s6c = (float)C.sigmalj6, s12c = (float)C.sigmalj12;
-    const float eps4 = (float)(4.0 * C.epslj), eps24 = (float)(24.0 * C.epslj), ecut = (float)C.e_cut;
+    LjdConst K;
+    for (int d = 0; d < 3; ++d) {
+        K.L[d] = S.boxf[d];
+        K.I[d] = S.inv_boxf[d];
+    }
+    K.rc2 = (float)rc2;
+    K.band = 1e-5f * K.rc2;
+    K.tie = 1e-5f;
+    K.s6 = (float)C.sigmalj6;
+    K.s12 = (float)C.sigmalj12;
+    K.eps4 = (float)(4.0 * C.epslj);
+    K.eps24 = (float)(24.0 * C.epslj);
+    K.ecut = (float)C.e_cut;
     // two images of a pair tied in dimension d are both L_d / 2 away in d: the tie
     // can change the cutoff decision only when (L_d / 2)^2 is not clearly above r_cut^2
-    const bool tx_on = 0.25 * S.box[0] * S.box[0] < 1.001 * rc2, ty_on = 0.25 * S.box[1] * S.box[1] < 1.001 * rc2,
-               tz_on = 0.25 * S.box[2] * S.box[2] < 1.001 * rc2;
+    K.tie_mask = 0;
+    for (int d = 0; d < 3; ++d)
+        if (0.25 * S.box[d] * S.box[d] < 1.001 * rc2) K.tie_mask |= 1 << d;
+    const float4 *opos = reinterpret_cast<const float4 *>(a.opos) + J.site_off / 3;
     float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
     if (act) oi = opos[i];
     float fx = 0.f, fy = 0.f, fz = 0.f, el = 0.f;
+    int flagged = 0;
     for (int t0 = 0; t0 < N; t0 += LJD_CH) {
         const int nj = min(LJD_CH, N - t0);
         __syncthreads();
@@ -1115,39 +1173,33 @@ __global__ void __launch_bounds__(128) k_lj_dense(EvalArgs a) {
         if (!act) continue;
 #pragma unroll 4
         for (int jj = sub; jj < nj; jj += LJD_SUB) {
-            const int j = t0 + jj;
-            const float4 o = sj[jj];
-            // wrapped positions lie in [0, L]: |t| <= 1, and two images tie at |t| = 1/2;
-            // a tie decides anything only where half a box lies inside r_cut
-            const float t0x = (oi.x - o.x) * I0, t0y = (oi.y - o.y) * I1, t0z = (oi.z - o.z) * I2;
-            bool exact = (tx_on && fabsf(fabsf(t0x) - 0.5f) < tie) || (ty_on && fabsf(fabsf(t0y) - 0.5f) < tie) ||
-                         (tz_on && fabsf(fabsf(t0z) - 0.5f) < tie);
-            float r0 = (oi.x - o.x) - L0 * rintf(t0x);
-            float r1 = (oi.y - o.y) - L1 * rintf(t0y);
-            float r2 = (oi.z - o.z) - L2 * rintf(t0z);
-            float rr = r0 * r0 + r1 * r1 + r2 * r2;
-            exact = exact || fabsf(rr - rc2f) <= band;
-            bool in;
-            if (exact) {
+            float r[3], rr;
+            const int c = ljd_classify(oi, sj[jj], K, r, &rr);
+            if (c == 1 && t0 + jj != i) ljd_pair(r, rr, K, fx, fy, fz, el);
+            flagged |= (c == 2);
+        }
+    }
+    // second pass, only in blocks that saw a pair needing the FP64 decision
+    if (__syncthreads_or(flagged)) {
+        const double *q = a.pos + J.pos_off;
+        for (int t0 = 0; t0 < N; t0 += LJD_CH) {
+            const int nj = min(LJD_CH, N - t0);
+            __syncthreads();
+            for (int k = threadIdx.x; k < nj; k += 128) sj[k] = opos[t0 + k];
+            __syncthreads();
+            if (!act || !flagged) continue;
+            for (int jj = sub; jj < nj; jj += LJD_SUB) {
+                const int j = t0 + jj;
+                float r[3], rr;
+                if (j == i || ljd_classify(oi, sj[jj], K, r, &rr) != 2) continue;
                 double rd[3];
                 const double r2d = lj_exact_disp(q + 9 * i, q + 9 * j, S, rd);
-                r0 = (float)rd[0];
-                r1 = (float)rd[1];
-                r2 = (float)rd[2];
-                rr = (float)r2d;
-                in = r2d < rc2;
-            } else {
-                in = rr < rc2f;
-            }
-            if (in && j != i) {
-                const float i2 = 1.0f / rr, i6 = i2 * i2 * i2;
-                const float s6 = i6 * s6c, s12 = i6 * i6 * s12c;
-                const float en = s12 - s6;
-                el += en * eps4 - ecut;
-                const float ff = (en + s12) * eps24 * i2;
-                fx += ff * r0;
-                fy += ff * r1;
-                fz += ff * r2;
+                if (r2d < rc2) {
+                    r[0] = (float)rd[0];
+                    r[1] = (float)rd[1];
+                    r[2] = (float)rd[2];
+                    ljd_pair(r, (float)r2d, K, fx, fy, fz, el);
+                }
             }
         }
     }
