@@ -215,6 +215,22 @@ qtg_status qtg_time_kernel(qtg_ctx *ctx, const char *name, int iters, double *av
  * per FMA) from a dependent-chain kernel filling every SM. */
 qtg_status qtg_fp32_peak(double *tflops);
 
+/* ---- launch-shape autotuner (no reference counterpart) ---------------------- */
+/* The three dominant force kernels split their work into chunks whose counts
+ * set the grid sizes: real-space j-chunks (k_real), structure-factor site
+ * chunks (k_ksk) and k-vector chunks (k_kforce), each in [1, 8]. By default a
+ * heuristic sizes each grid for about 12 blocks per SM over all of the
+ * context's systems. qtg_autotune times every candidate count of each kernel
+ * on the context's own batch (iters launches each), then keeps the tuned
+ * triple if a whole force evaluation with it beats the heuristic, and reports
+ * both evaluation times (ms). Call it after qtg_set_state and before
+ * qtg_init_forces: it rebuilds the Verlet lists and overwrites the forces, so
+ * a qtg_init_forces must follow. A changed shape takes effect at the next
+ * step graph capture. qtg_set_tuning fixes the counts by hand (0: heuristic). */
+qtg_status qtg_autotune(qtg_ctx *ctx, int iters, double *ms_heuristic, double *ms_tuned);
+qtg_status qtg_set_tuning(qtg_ctx *ctx, int n_rj, int n_sc, int n_kc);
+qtg_status qtg_get_tuning(qtg_ctx *ctx, int *n_rj, int *n_sc, int *n_kc);
+
 #ifdef __cplusplus
 }
 #endif

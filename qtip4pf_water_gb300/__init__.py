@@ -100,6 +100,9 @@ def load(build_if_missing: bool = True):
         "qtg_reset_estimators": ([V], C.c_int),
         "qtg_time_kernel": ([V, C.c_char_p, C.c_int, D], C.c_int),
         "qtg_fp32_peak": ([D], C.c_int),
+        "qtg_autotune": ([V, C.c_int, D, D], C.c_int),
+        "qtg_set_tuning": ([V, C.c_int, C.c_int, C.c_int], C.c_int),
+        "qtg_get_tuning": ([V, I, I, I], C.c_int),
         "qtg_kwald_noalloc": ([V, V, C.c_int, D, C.c_double, V, V, V], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -164,6 +167,22 @@ class Context:
 
     def init_forces(self):
         self.check(self.L.qtg_init_forces(self.h))
+
+    def autotune(self, iters=10):
+        """Pick the chunk counts of k_real / k_ksk / k_kforce for this batch
+        (qtg_autotune); returns (heuristic ms, tuned ms) of one force evaluation.
+        Call after set_state and before init_forces."""
+        t0, t1 = C.c_double(0.0), C.c_double(0.0)
+        self.check(self.L.qtg_autotune(self.h, int(iters), C.byref(t0), C.byref(t1)))
+        return t0.value, t1.value
+
+    def set_tuning(self, n_rj=0, n_sc=0, n_kc=0):
+        self.check(self.L.qtg_set_tuning(self.h, int(n_rj), int(n_sc), int(n_kc)))
+
+    def tuning(self):
+        a, b, c = C.c_int(0), C.c_int(0), C.c_int(0)
+        self.check(self.L.qtg_get_tuning(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
 
     def run_steps(self, n_steps, is_nvt=True):
         self.check(self.L.qtg_run_steps(self.h, int(n_steps), 1 if is_nvt else 0))

@@ -245,6 +245,7 @@ struct qtg_ctx {
     unsigned *status = nullptr;
     double *red_out = nullptr;  // small reduction output
     bool forces_ready = false;
+    int tune[3] = {0, 0, 0};  // real-space j-chunks, structure-factor site chunks, k-chunks (0: heuristic)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     unsigned long long graph_kernels[2] = {0, 0};
     unsigned long long launches = 0;
@@ -310,6 +311,9 @@ EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, d
     a.status = c->status;
     a.mode = mode;
     a.sr_only = sr_only;
+    a.tune_rj = c->tune[0];
+    a.tune_sc = c->tune[1];
+    a.tune_kc = c->tune[2];
     a.c = c->K;
     return a;
 }
@@ -557,6 +561,39 @@ qtg_status upload_charges(qtg_ctx *ctx, int sys, const double *charge) {
 }  // namespace
 
 // ============================================================================
+namespace {
+
+// Drops the captured step graphs, so that the next qtg_run_steps captures
+// the step again with the current launch shapes.
+void drop_graphs(qtg_ctx *ctx) {
+    for (int i = 0; i < 2; ++i) {
+        if (ctx->graph[i]) cudaGraphExecDestroy(ctx->graph[i]);
+        ctx->graph[i] = nullptr;
+        ctx->graph_kernels[i] = 0;
+    }
+}
+
+// Average duration (ms) of `iters` launches of `fn` on the context's stream.
+template <typename F>
+qtg_status time_on_stream(qtg_ctx *ctx, int iters, F fn, double *ms_out) {
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    fn();  // warm-up
+    CK(cudaEventRecord(e0, ctx->stream));
+    for (int i = 0; i < iters; ++i) fn();
+    CK(cudaEventRecord(e1, ctx->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms_out = (double)ms / iters;
+    return QTG_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *qtg_status_string(int s) {
@@ -1472,6 +1509,76 @@ qtg_status qtg_time_kernel(qtg_ctx *ctx, const char *name, int iters, double *av
     CK(cudaMemsetAsync(ctx->acc, 0, sizeof(SysAcc) * ctx->n_sys, ctx->stream));
     *avg_ms = (double)ms / iters;
     ctx->forces_ready = false;
+    return sync_status(ctx);
+}
+
+qtg_status qtg_set_tuning(qtg_ctx *ctx, int n_rj, int n_sc, int n_kc) {
+    if (!ctx || n_rj < 0 || n_sc < 0 || n_kc < 0 || n_rj > MAX_RJ || n_sc > MAX_SC || n_kc > MAX_KC)
+        return fail(ctx, QTG_ERR_ARG, "chunk counts must lie in [0, 8] (0: heuristic)");
+    ctx->tune[0] = n_rj;
+    ctx->tune[1] = n_sc;
+    ctx->tune[2] = n_kc;
+    drop_graphs(ctx);
+    return QTG_OK;
+}
+
+qtg_status qtg_get_tuning(qtg_ctx *ctx, int *n_rj, int *n_sc, int *n_kc) {
+    if (!ctx || !n_rj || !n_sc || !n_kc) return QTG_ERR_ARG;
+    *n_rj = ctx->tune[0];
+    *n_sc = ctx->tune[1];
+    *n_kc = ctx->tune[2];
+    return QTG_OK;
+}
+
+qtg_status qtg_autotune(qtg_ctx *ctx, int iters, double *ms_heuristic, double *ms_tuned) {
+    if (!ctx || iters <= 0) return QTG_ERR_ARG;
+    const int nj = (int)ctx->base.h.size();
+    // lists for the current positions (the FP64 Lennard-Jones reads them)
+    CK(cudaMemsetAsync(ctx->disp, 0, sizeof(double) * ctx->total_disp, ctx->stream));
+    launch_skin_rebuild(list_args(ctx, 0, nj, 1), ctx->stream, &ctx->launches);
+    ctx->forces_ready = false;  // the timing runs overwrite the forces
+    auto eval_ms = [&](const int *t, double *ms) {
+        for (int k = 0; k < 3; ++k) ctx->tune[k] = t[k];
+        EvalArgs a = eval_args(ctx, ctx->base.d, nj, ctx->q, ctx->fphys, 0, 0);
+        a.lj_full = 1;
+        return time_on_stream(ctx, iters, [&] { launch_eval(ctx, a); }, ms);
+    };
+    // each count governs one kernel: k_real (n_rj), k_ksk (n_sc), k_kforce (n_kc)
+    static const int cand[] = {1, 2, 3, 4, 5, 6, 8};
+    static const char *kname[3] = {"real", "ksk", "kforce"};
+    int best[3] = {0, 0, 0};
+    {
+        const int zero[3] = {0, 0, 0};
+        double ms;
+        CKS(eval_ms(zero, &ms));  // fills the scratch arrays the single kernels read
+    }
+    for (int k = 0; k < 3; ++k) {
+        double best_ms = 1e30;
+        for (int c : cand) {
+            int t[3] = {0, 0, 0};
+            t[k] = c;
+            for (int q = 0; q < 3; ++q) ctx->tune[q] = t[q];
+            EvalArgs a = eval_args(ctx, ctx->base.d, nj, ctx->q, ctx->fphys, 0, 0);
+            a.lj_full = 1;
+            double ms;
+            CKS(time_on_stream(ctx, iters, [&] { launch_ewald_kernel(a, ctx->mixed, kname[k], ctx->stream); }, &ms));
+            if (ms < best_ms) {
+                best_ms = ms;
+                best[k] = c;
+            }
+        }
+    }
+    // the whole force evaluation decides between the tuned counts and the heuristic
+    const int zero[3] = {0, 0, 0};
+    double t0 = 0.0, t1 = 0.0;
+    CKS(eval_ms(zero, &t0));
+    CKS(eval_ms(best, &t1));
+    const int *pick = t1 < t0 ? best : zero;
+    for (int k = 0; k < 3; ++k) ctx->tune[k] = pick[k];
+    if (ms_heuristic) *ms_heuristic = t0;
+    if (ms_tuned) *ms_tuned = t1 < t0 ? t1 : t0;
+    drop_graphs(ctx);
+    CK(cudaMemsetAsync(ctx->acc, 0, sizeof(SysAcc) * ctx->n_sys, ctx->stream));
     return sync_status(ctx);
 }
 

@@ -1276,14 +1276,18 @@ int chunks_for(long long base_blocks, int maxc) {
     const int c = (int)((want + base_blocks - 1) / std::max(1LL, base_blocks));
     return std::max(1, std::min(c, maxc));
 }
+// a tuned count when the autotuner fixed one, else the heuristic
+int chunks_or(int tuned, long long base_blocks, int maxc) {
+    return tuned > 0 ? std::min(tuned, maxc) : chunks_for(base_blocks, maxc);
+}
 
 template <typename R>
 void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n) {
     const int ns = 3 * a.max_mols;
     const int tiles = (ns + RT - 1) / RT, ktiles = (a.max_grp + KT - 1) / KT;
-    a.n_rj = chunks_for((long long)tiles * a.n_jobs, MAX_RJ);
-    a.n_sc = chunks_for((long long)ktiles * a.n_jobs, MAX_SC);
-    a.n_kc = chunks_for((long long)tiles * a.n_jobs, MAX_KC);
+    a.n_rj = chunks_or(a.tune_rj, (long long)tiles * a.n_jobs, MAX_RJ);
+    a.n_sc = chunks_or(a.tune_sc, (long long)ktiles * a.n_jobs, MAX_SC);
+    a.n_kc = chunks_or(a.tune_kc, (long long)tiles * a.n_jobs, MAX_KC);
     k_prep<R><<<dim3((ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
     if (a.mode == 0) {
         if (sizeof(R) == 4) k_real_f32<<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
@@ -1320,9 +1324,9 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
     EvalArgs a = a0;
     const int ns = 3 * a.max_mols;
     const int tiles = (ns + RT - 1) / RT, ktiles = (a.max_grp + KT - 1) / KT;
-    a.n_rj = chunks_for((long long)tiles * a.n_jobs, MAX_RJ);
-    a.n_sc = chunks_for((long long)ktiles * a.n_jobs, MAX_SC);
-    a.n_kc = chunks_for((long long)tiles * a.n_jobs, MAX_KC);
+    a.n_rj = chunks_or(a.tune_rj, (long long)tiles * a.n_jobs, MAX_RJ);
+    a.n_sc = chunks_or(a.tune_sc, (long long)ktiles * a.n_jobs, MAX_SC);
+    a.n_kc = chunks_or(a.tune_kc, (long long)tiles * a.n_jobs, MAX_KC);
     const dim3 gs((ns + 127) / 128, a.n_jobs), gr(tiles, a.n_rj, a.n_jobs);
     const dim3 gk(ktiles, a.n_sc, a.n_jobs), gf(tiles, a.n_kc, a.n_jobs);
     const dim3 gm((a.max_mols + 127) / 128, a.n_jobs), gl((a.max_mols + 3) / 4, a.n_jobs);
@@ -1392,8 +1396,8 @@ void launch_kwald_only(const EvalArgs &a0, bool mixed, cudaStream_t s, unsigned 
     const int ns = 3 * a.max_mols;
     const int tiles = (ns + FT - 1) / FT, ktiles = (a.max_grp + KT - 1) / KT;
     a.n_rj = 0;
-    a.n_sc = chunks_for((long long)ktiles * a.n_jobs, MAX_SC);
-    a.n_kc = chunks_for((long long)tiles * a.n_jobs, MAX_KC);
+    a.n_sc = chunks_or(a.tune_sc, (long long)ktiles * a.n_jobs, MAX_SC);
+    a.n_kc = chunks_or(a.tune_kc, (long long)tiles * a.n_jobs, MAX_KC);
     const dim3 gs((ns + 127) / 128, a.n_jobs), gk(ktiles, a.n_sc, a.n_jobs), gf(tiles, a.n_kc, a.n_jobs);
     const dim3 gr((a.max_kvec + 127) / 128, a.n_jobs);
     if (mixed) {

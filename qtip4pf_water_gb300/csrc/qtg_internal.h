@@ -332,6 +332,7 @@ struct EvalArgs {
     double *energy;        // per slot
     unsigned *status;
     int n_rj, n_sc, n_kc;  // chunk counts, chosen by the launcher
+    int tune_rj, tune_sc, tune_kc;  // chunk counts fixed by the autotuner (0: launcher heuristic)
     int sites_are_input;   // 1: positions are charge sites (M,H1,H2) -> reciprocal space only
     int sr_only;           // 1: only the short-range terms (LJ, intramolecular,
                            //    same-molecule Ewald), in FP64; Ewald partials ignored
