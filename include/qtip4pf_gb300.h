@@ -215,6 +215,61 @@ qtg_status qtg_time_kernel(qtg_ctx *ctx, const char *name, int iters, double *av
  * per FMA) from a dependent-chain kernel filling every SM. */
 qtg_status qtg_fp32_peak(double *tflops);
 
+/* ---- centroid-constrained PIMD (no reference counterpart) ------------------- */
+/* With the centroid fixed, the device stepper holds each atom's bead centroid
+ * where it is (the centroid normal mode carries no momentum and is not
+ * thermostatted) while the internal modes evolve, and every step adds the
+ * bead-averaged physical force (1/P) sum_b F_b to a per-dof sum: its mean is
+ * the constrained-PIMD mean centroid force, the target of the learned centroid
+ * correction. Trotter systems; qtg_get_centroid_force returns the mean
+ * (double[9N], reference layout) and the number of steps in it. */
+qtg_status qtg_set_centroid_fixed(qtg_ctx *ctx, int sys, int fixed);
+qtg_status qtg_reset_centroid_force(qtg_ctx *ctx, int sys);
+qtg_status qtg_get_centroid_force(qtg_ctx *ctx, int sys, double *f_mean, double *n_samples);
+
+/* ---- learned centroid correction (no reference counterpart) ------------------ */
+/* A per-molecule network maps Behler-Parrinello symmetry functions of the
+ * molecule's three atoms (G2 and G4 within 6 A, QTG_DESC_PER_ATOM per atom,
+ * O H1 H2 concatenated: QTG_MLP_IN inputs) through two hidden layers of
+ * QTG_MLP_HIDDEN SiLU units to the centroid-force correction of its three atoms
+ * in the molecule's frame (QTG_MLP_OUT values, padded to QTG_MLP_OUT_PAD). It
+ * replaces the reference's tabulated CMD spline (forces.cpp:452-466). These
+ * entries take DEVICE pointers and queue work on `stream` without waiting. */
+#define QTG_DESC_PER_ATOM 32
+#define QTG_MLP_IN 96
+#define QTG_MLP_HIDDEN 64
+#define QTG_MLP_OUT 9
+#define QTG_MLP_OUT_PAD 16
+typedef struct qtg_mlp_weights {
+    const void *w1, *w2, *w3;    /* BF16, row-major [out][in]: [64][96], [64][64], [16][64] (rows 9..15 zero) */
+    const float *b1, *b2, *b3;   /* FP32: [64], [64], [16] */
+} qtg_mlp_weights;
+/* Symmetry functions of every atom of n_conf configurations of n_mols waters
+ * (pos: double[n_conf][9N] bohr, orthorhombic box with every side above 12 A):
+ * desc float[n_conf][3N][32]. */
+qtg_status qtg_sym_descriptors(const double *pos, int n_conf, int n_mols, const double *box_bohr, float *desc,
+                               void *stream);
+/* Forward pass on the tensor cores: x BF16 [m][96] -> y float[m][16]. */
+qtg_status qtg_mlp_forward(const qtg_mlp_weights *w, const void *x_bf16, int m, float *y, void *stream);
+/* Training. Parameters are one FP32 vector of QTG_MLP_NPARAMS values:
+ * w1 [64][96] | w2 [64][64] | w3 [16][64] | b1 [64] | b2 [64] | b3 [16].
+ * qtg_mlp_train_batch runs the forward and backward pass of m rows (x BF16
+ * [m][96], targets t float[m][16], the first QTG_MLP_OUT used) on the tensor
+ * cores with dL/dy = grad_scale (y - t), and writes the summed gradients and the
+ * summed squared error: grad_out float[QTG_MLP_NPARAMS + 1]. partial is scratch
+ * of max_ctas x (QTG_MLP_NPARAMS + 1) floats; the sum over CTAs is taken in a
+ * fixed order. qtg_adam_step applies Adam to the FP32 parameters and refreshes
+ * the BF16 copies of its first n_bf16 entries (the weights). */
+#define QTG_MLP_NPARAMS 11408
+qtg_status qtg_mlp_train_batch(const qtg_mlp_weights *w, const void *x_bf16, const float *t, int m, float grad_scale,
+                               float *partial, int max_ctas, float *grad_out, void *stream);
+qtg_status qtg_adam_step(float *params, float *m1, float *m2, const float *grad, int n, int step, float lr,
+                         float beta1, float beta2, float eps, void *w_bf16, int n_bf16, void *stream);
+/* Synchronises the device and returns the surrogate kernels' error bits (8: an
+ * atom had more than 256 neighbours within 6 A; 16: a tensor-core completion
+ * wait ran out), clearing them when `clear` is set. */
+qtg_status qtg_surrogate_status(unsigned *bits, int clear);
+
 /* ---- launch-shape autotuner (no reference counterpart) ---------------------- */
 /* The three dominant force kernels split their work into chunks whose counts
  * set the grid sizes: real-space j-chunks (k_real), structure-factor site

@@ -56,6 +56,11 @@ D = C.POINTER(C.c_double)
 I = C.POINTER(C.c_int)
 V = C.c_void_p
 
+
+class MlpWeights(C.Structure):
+    """qtg_mlp_weights: device pointers of the BF16 weights and FP32 biases."""
+    _fields_ = [("w1", V), ("w2", V), ("w3", V), ("b1", V), ("b2", V), ("b3", V)]
+
 _lib = None
 
 
@@ -101,6 +106,15 @@ def load(build_if_missing: bool = True):
         "qtg_time_kernel": ([V, C.c_char_p, C.c_int, D], C.c_int),
         "qtg_fp32_peak": ([D], C.c_int),
         "qtg_autotune": ([V, C.c_int, D, D], C.c_int),
+        "qtg_sym_descriptors": ([V, C.c_int, C.c_int, D, V, V], C.c_int),
+        "qtg_mlp_forward": ([C.POINTER(MlpWeights), V, C.c_int, V, V], C.c_int),
+        "qtg_surrogate_status": ([C.POINTER(C.c_uint), C.c_int], C.c_int),
+        "qtg_mlp_train_batch": ([C.POINTER(MlpWeights), V, V, C.c_int, C.c_float, V, C.c_int, V, V], C.c_int),
+        "qtg_adam_step": ([V, V, V, V, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, V, C.c_int, V],
+                          C.c_int),
+        "qtg_set_centroid_fixed": ([V, C.c_int, C.c_int], C.c_int),
+        "qtg_reset_centroid_force": ([V, C.c_int], C.c_int),
+        "qtg_get_centroid_force": ([V, C.c_int, D, D], C.c_int),
         "qtg_set_tuning": ([V, C.c_int, C.c_int, C.c_int], C.c_int),
         "qtg_get_tuning": ([V, I, I, I], C.c_int),
         "qtg_kwald_noalloc": ([V, V, C.c_int, D, C.c_double, V, V, V], C.c_int),
@@ -207,6 +221,47 @@ def fp32_peak_tflops():
     if st != 0:
         raise QtgError(st, "fp32 probe failed")
     return t.value
+
+
+def _check(st, what):
+    if st != 0:
+        raise QtgError(st, what + " failed")
+
+
+def sym_descriptors(pos_ptr, n_conf, n_mols, box_bohr, desc_ptr, stream=0):
+    """qtg_sym_descriptors on device buffers (pos double[n_conf][9N] -> desc float[n_conf][3N][32])."""
+    box = np.ascontiguousarray(np.broadcast_to(np.asarray(box_bohr, dtype=np.float64), (3,)))
+    _check(load().qtg_sym_descriptors(V(pos_ptr), int(n_conf), int(n_mols), _d(box), V(desc_ptr), V(stream)),
+           "qtg_sym_descriptors")
+
+
+def mlp_forward(weights: MlpWeights, x_ptr, m, y_ptr, stream=0):
+    """qtg_mlp_forward on device buffers (x BF16 [m][96] -> y float[m][16])."""
+    _check(load().qtg_mlp_forward(C.byref(weights), V(x_ptr), int(m), V(y_ptr), V(stream)), "qtg_mlp_forward")
+
+
+def mlp_train_batch(weights: MlpWeights, x_ptr, t_ptr, m, grad_scale, partial_ptr, max_ctas, grad_ptr, stream=0):
+    """qtg_mlp_train_batch: summed gradients and squared error of m rows into grad (float[NPARAMS + 1])."""
+    _check(load().qtg_mlp_train_batch(C.byref(weights), V(x_ptr), V(t_ptr), int(m), float(grad_scale), V(partial_ptr),
+                                      int(max_ctas), V(grad_ptr), V(stream)), "qtg_mlp_train_batch")
+
+
+def adam_step(params_ptr, m1_ptr, m2_ptr, grad_ptr, n, step, lr, w_bf16_ptr, n_bf16, beta1=0.9, beta2=0.999,
+              eps=1e-8, stream=0):
+    _check(load().qtg_adam_step(V(params_ptr), V(m1_ptr), V(m2_ptr), V(grad_ptr), int(n), int(step), float(lr),
+                                float(beta1), float(beta2), float(eps), V(w_bf16_ptr), int(n_bf16), V(stream)),
+           "qtg_adam_step")
+
+
+MLP_NPARAMS = 11408
+MLP_NW = 64 * 96 + 64 * 64 + 16 * 64  # weights, stored first in the parameter vector
+
+
+def surrogate_status(clear=True):
+    """Error bits of the surrogate kernels (synchronises the device)."""
+    b = C.c_uint(0)
+    _check(load().qtg_surrogate_status(C.byref(b), 1 if clear else 0), "qtg_surrogate_status")
+    return int(b.value)
 
 
 def system_desc(n_mols, n_beads, box_bohr, temp_K=298.0, dt_fs=0.25, eps_ewald=1e-6, eps_sc=1e-5,
@@ -343,6 +398,20 @@ class System:
         disp = np.zeros(self.P * 3 * self.N)
         self._c(self.ctx.L.qtg_get_state(self.ctx.h, self.idx, _d(q), _d(p), _d(f), _d(fp), _d(disp)))
         return dict(q=q, p=p, f=f, fphys=fp, disp=disp)
+
+    def set_centroid_fixed(self, fixed=True):
+        """Centroid-constrained PIMD: hold the bead centroid fixed (Trotter systems)."""
+        self._c(self.ctx.L.qtg_set_centroid_fixed(self.ctx.h, self.idx, 1 if fixed else 0))
+
+    def reset_centroid_force(self):
+        self._c(self.ctx.L.qtg_reset_centroid_force(self.ctx.h, self.idx))
+
+    def centroid_force(self):
+        """Mean over the steps so far of (1/P) sum_b F_b, double[9N], and the step count."""
+        out = np.zeros(9 * self.N)
+        n = C.c_double(0.0)
+        self._c(self.ctx.L.qtg_get_centroid_force(self.ctx.h, self.idx, _d(out), C.byref(n)))
+        return out, int(n.value)
 
     def estimators(self, max_records=1 << 20):
         n = C.c_int(0)

@@ -206,6 +206,8 @@ struct qtg_ctx {
     int *point = nullptr, *list = nullptr, *point_full = nullptr, *list_full = nullptr;
     size_t total_point_full = 0, total_list_full = 0;
     double *charge = nullptr, *mass = nullptr, *inv_mass = nullptr, *sqrt_mass = nullptr;
+    double *cf_acc = nullptr;  // mean-centroid-force sums of constrained systems, per dof (like mass)
+    size_t n_cf = 0;
     double *qdisp = nullptr, *fdisp = nullptr, *fsr = nullptr, *dirv = nullptr, *sc_scale = nullptr;
     double *stage = nullptr;  // per-call staging (total_dof doubles)
     double *noise = nullptr;  // per-call noise (2 + (Pmax-1) * 9Nmax)
@@ -356,6 +358,7 @@ RingArgs ring_args(qtg_ctx *c, int sys, int flags) {
     r.step = c->step;
     r.kcv_all_beads = -1;
     r.max_p = c->max_p;
+    r.cf_acc = c->cf_acc;
     return r;
 }
 
@@ -899,6 +902,8 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->mass, mass_all.size());
     AL(ctx->inv_mass, mass_all.size());
     AL(ctx->sqrt_mass, mass_all.size());
+    AL(ctx->cf_acc, mass_all.size());
+    ctx->n_cf = mass_all.size();
     AL(ctx->sc_scale, ctx->total_slots);
     AL(ctx->noise, ctx->noise_len);
     AL(ctx->kvec, kall.size());
@@ -989,9 +994,10 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         for (auto &r : runs) {
             r.heat = 0.0;
             r.alpha = 1.0;
-            r.pad[0] = r.pad[1] = 0.0;
+            r.cf_samples = r.pad = 0.0;
         }
         cp(ctx->run, runs.data(), sizeof(SysRun) * n_systems);
+        if (e == cudaSuccess) e = cudaMemset(ctx->cf_acc, 0, sizeof(double) * ctx->n_cf);
     }
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
@@ -1009,7 +1015,7 @@ void qtg_destroy(qtg_ctx *ctx) {
         if (ctx->graph[i]) cudaGraphExecDestroy(ctx->graph[i]);
     void *ptrs[] = {ctx->sys_d, ctx->q, ctx->p, ctx->f, ctx->fphys, ctx->qdisp, ctx->fdisp, ctx->fsr,
                     ctx->dirv, ctx->stage, ctx->disp, ctx->point, ctx->list, ctx->point_full, ctx->list_full,
-                    ctx->charge, ctx->mass, ctx->inv_mass, ctx->sqrt_mass,
+                    ctx->charge, ctx->mass, ctx->inv_mass, ctx->sqrt_mass, ctx->cf_acc,
                     ctx->sc_scale, ctx->noise, ctx->kvec, ctx->kcol, ctx->kgrp, ctx->kbatch, ctx->nm, ctx->modes, ctx->sites, ctx->tan_sites,
                     ctx->phase, ctx->opos, ctx->part, ctx->skp, ctx->dskp, ctx->wsk, ctx->wdsk, ctx->energy, ctx->energy_aux,
                     ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
@@ -1056,6 +1062,35 @@ qtg_status qtg_set_charges(qtg_ctx *ctx, int sys, const double *charge) {
     if (!charge) return fail(ctx, QTG_ERR_ARG, "null charge array");
     CKS(upload_charges(ctx, sys, charge));
     return sync_status(ctx);
+}
+
+qtg_status qtg_set_centroid_fixed(qtg_ctx *ctx, int sys, int fixed) {
+    CKS(check_sys(ctx, sys));
+    ctx->sys_h[sys].centroid_fixed = fixed ? 1 : 0;
+    CK(cudaMemcpyAsync(ctx->sys_d + sys, &ctx->sys_h[sys], sizeof(SysDev), cudaMemcpyHostToDevice, ctx->stream));
+    return sync_status(ctx);
+}
+
+qtg_status qtg_reset_centroid_force(qtg_ctx *ctx, int sys) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    CK(cudaMemsetAsync(ctx->cf_acc + S.mass_off, 0, sizeof(double) * S.n_dof, ctx->stream));
+    CK(cudaMemsetAsync(&ctx->run[sys].cf_samples, 0, sizeof(double), ctx->stream));
+    return sync_status(ctx);
+}
+
+qtg_status qtg_get_centroid_force(qtg_ctx *ctx, int sys, double *f_mean, double *n_samples) {
+    CKS(check_sys(ctx, sys));
+    if (!f_mean || !n_samples) return fail(ctx, QTG_ERR_ARG, "null output");
+    const SysDev &S = ctx->sys_h[sys];
+    std::vector<double> acc(S.n_dof);
+    double ns = 0.0;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(acc.data(), ctx->cf_acc + S.mass_off, sizeof(double) * S.n_dof, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&ns, &ctx->run[sys].cf_samples, sizeof(double), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < S.n_dof; ++i) f_mean[i] = ns > 0.0 ? acc[i] / ns : 0.0;
+    *n_samples = ns;
+    return QTG_OK;
 }
 
 qtg_status qtg_set_masses(qtg_ctx *ctx, int sys, const double *mass) {

@@ -108,6 +108,10 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
         __syncthreads();
     }
     double heat = 0.0;
+    // centroid-constrained PIMD: the centroid normal mode carries no momentum, so
+    // the free ring-polymer step (omega_0 = 0) leaves the centroid where it is
+    const bool fixed0 = S.centroid_fixed && k == 0 && (flags & RF_FWD);
+    if (fixed0) yp = 0.0;
     if (act) {
         if (flags & RF_VV) {
             // update.cpp:87-91
@@ -124,7 +128,7 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
             yp *= mc.scale;
             yq = t;
         }
-        if ((flags & RF_THERMO) && (S.thermostat != 0 || a.pile_g)) {
+        if ((flags & RF_THERMO) && (S.thermostat != 0 || a.pile_g) && !fixed0) {
             const double before = 0.5 * yp * yp * im;
             if (k == 0 && (S.thermostat == 1 || a.pile_g)) {
                 yp *= a.run[W.sys].alpha;  // PILE-G centroid (thermostat.cpp:88-104)
@@ -223,7 +227,9 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
     extern __shared__ double sh[];
     double *Xq = sh;
     double *Xp = Xq + P * C;
+    double *Xf = Xp + P * C;  // physical forces (centroid-constrained systems)
     __shared__ double qbar[256];
+    const bool cf = a.kick && S.centroid_fixed && a.cf_acc;
     __shared__ double red4[4][256];
     const long long at = S.q_off + (long long)b * S.n_dof + col;
     double qb = 0.0, pb = 0.0, fb = 0.0, fpb = 0.0;
@@ -240,8 +246,16 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
         }
         Xq[b * C + c] = qb;
         Xp[b * C + c] = pb + S.halfdt * fb;
+        if (cf) Xf[b * C + c] = fpb;
     }
     __syncthreads();
+    // mean centroid force of constrained PIMD: (1/P) sum_b F_b, accumulated per step
+    if (cf && b == 0 && c < W.ncols) {
+        double sf = 0.0;
+        for (int j = 0; j < P; ++j) sf += Xf[j * C + c];
+        a.cf_acc[S.mass_off + col] += sf / (double)P;
+        if (col == 0) a.run[W.sys].cf_samples += 1.0;
+    }
     // bead 0 of each column: the centroid (path_integrals.cpp:10-26) and the
     // centroid normal-mode kinetic energy after the next opening kick
     double k0 = 0.0;
@@ -530,7 +544,7 @@ void launch_ring(const RingArgs &a, cudaStream_t s, unsigned long long *n) {
 
 void launch_end_step(const RingArgs &a, cudaStream_t s, unsigned long long *n) {
     if (a.n_work <= 0) return;
-    k_end_step<<<a.n_work, 256, 2 * 256 * sizeof(double), s>>>(a);
+    k_end_step<<<a.n_work, 256, 3 * 256 * sizeof(double), s>>>(a);
     if (n) ++*n;
 }
 

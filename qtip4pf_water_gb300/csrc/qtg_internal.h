@@ -24,7 +24,8 @@ struct SysDev {
     int n_mols, n_beads, n_sites, n_dof, list_size, k_max, n_kvec, kvec_off;
     int propagator, thermostat, job_base, cols_per_block;
     int n_kvec_ref;              // the reference's k-vector count (n_kvec includes c_k = 0 fillers)
-    int col_off, n_col, grp_off, n_grp, batch_off, n_batch, pad1;
+    int col_off, n_col, grp_off, n_grp, batch_off, n_batch;
+    int centroid_fixed;          // 1: the centroid is held fixed (centroid-constrained PIMD)
     long long nm_off;   // doubles: P x P bead->normal-mode matrix C (y = C x)
     long long mode_off; // ModeCoef entries: P per system
     long long q_off;    // doubles: system block [P][9N] in q/p/f/fphys/aux arrays
@@ -103,9 +104,10 @@ struct SysAcc {
 
 // Per-system persistent thermostat / RNG state.
 struct SysRun {
-    double heat;   // accumulated thermostat heat (update.cpp:325)
-    double alpha;  // centroid rescale factor for the next O step (PILE-G)
-    double pad[2];
+    double heat;        // accumulated thermostat heat (update.cpp:325)
+    double alpha;       // centroid rescale factor for the next O step (PILE-G)
+    double cf_samples;  // steps accumulated into the mean centroid force
+    double pad;
 };
 
 // Status word written by kernels (bit flags), read by the host after a sync.
@@ -113,6 +115,8 @@ enum StatusBits : unsigned {
     ST_LIST_OVERFLOW = 1u,
     ST_NONFINITE = 2u,
     ST_GAMMA_LIMIT = 4u,
+    ST_DESC_OVERFLOW = 8u,   // an atom had more neighbours within the descriptor cutoff than kept
+    ST_MMA_TIMEOUT = 16u,    // a tensor-core completion wait ran out of its iteration limit
 };
 
 // ---- device helpers ---------------------------------------------------------
@@ -235,6 +239,8 @@ struct RingArgs {
     int kcv_all_beads;       // end step: -1 = by propagator, 0 = even beads, 1 = all beads
     int max_p;               // largest bead count (shared-memory sizing)
     int pile_g;              // 1: O step is PILE-G whatever the system's thermostat
+    double *cf_acc;          // end step: sum over steps of the bead-averaged force, per dof
+                             // (systems with a fixed centroid; indexed like mass)
 };
 
 struct FinalizeArgs {
