@@ -265,6 +265,15 @@ qtg_status qtg_mlp_train_batch(const qtg_mlp_weights *w, const void *x_bf16, con
                                float *partial, int max_ctas, float *grad_out, void *stream);
 qtg_status qtg_adam_step(float *params, float *m1, float *m2, const float *grad, int n, int step, float lr,
                          float beta1, float beta2, float eps, void *w_bf16, int n_bf16, void *stream);
+/* Surrogate centroid molecular dynamics: a trained network attached to a P = 1
+ * system (its positions are centroids) adds the learned correction to that
+ * system's forces in every force evaluation, inside the step graph. The
+ * context copies the weights (device pointers in `w`) and the input
+ * normalisation (host float[192]: mean[96] then 1/std[96]) into memory of its
+ * own; out_scale multiplies the network's outputs (Hartree/bohr). A
+ * qtg_init_forces must follow. */
+qtg_status qtg_attach_surrogate(qtg_ctx *ctx, int sys, const qtg_mlp_weights *w, const float *norm, float out_scale);
+qtg_status qtg_detach_surrogate(qtg_ctx *ctx, int sys);
 /* Synchronises the device and returns the surrogate kernels' error bits (8: an
  * atom had more than 256 neighbours within 6 A; 16: a tensor-core completion
  * wait ran out), clearing them when `clear` is set. */

@@ -110,6 +110,8 @@ def load(build_if_missing: bool = True):
         "qtg_mlp_forward": ([C.POINTER(MlpWeights), V, C.c_int, V, V], C.c_int),
         "qtg_surrogate_status": ([C.POINTER(C.c_uint), C.c_int], C.c_int),
         "qtg_mlp_train_batch": ([C.POINTER(MlpWeights), V, V, C.c_int, C.c_float, V, C.c_int, V, V], C.c_int),
+        "qtg_attach_surrogate": ([V, C.c_int, C.POINTER(MlpWeights), C.POINTER(C.c_float), C.c_float], C.c_int),
+        "qtg_detach_surrogate": ([V, C.c_int], C.c_int),
         "qtg_adam_step": ([V, V, V, V, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, V, C.c_int, V],
                           C.c_int),
         "qtg_set_centroid_fixed": ([V, C.c_int, C.c_int], C.c_int),
@@ -412,6 +414,15 @@ class System:
         n = C.c_double(0.0)
         self._c(self.ctx.L.qtg_get_centroid_force(self.ctx.h, self.idx, _d(out), C.byref(n)))
         return out, int(n.value)
+
+    def attach_surrogate(self, weights, norm, out_scale):
+        """Attach a trained centroid correction (qtg_attach_surrogate; P = 1 systems)."""
+        nm = np.ascontiguousarray(norm, dtype=np.float32)
+        self._c(self.ctx.L.qtg_attach_surrogate(self.ctx.h, self.idx, C.byref(weights),
+                                                nm.ctypes.data_as(C.POINTER(C.c_float)), float(out_scale)))
+
+    def detach_surrogate(self):
+        self._c(self.ctx.L.qtg_detach_surrogate(self.ctx.h, self.idx))
 
     def estimators(self, max_records=1 << 20):
         n = C.c_int(0)

@@ -248,6 +248,14 @@ struct qtg_ctx {
     double *red_out = nullptr;  // small reduction output
     bool forces_ready = false;
     int tune[3] = {0, 0, 0};  // real-space j-chunks, structure-factor site chunks, k-chunks (0: heuristic)
+    struct Surrogate {        // learned centroid correction attached to a P = 1 system
+        int sys = -1;
+        float out_scale = 1.f;
+        __nv_bfloat16 *wbf = nullptr, *feat = nullptr;
+        float *bias = nullptr, *norm = nullptr, *desc = nullptr, *y = nullptr, *frames = nullptr;
+    };
+    std::vector<Surrogate> surrogates;
+    int n_sm = 148;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     unsigned long long graph_kernels[2] = {0, 0};
     unsigned long long launches = 0;
@@ -434,6 +442,27 @@ void enqueue_forces(qtg_ctx *c, int sys, bool force_sc) {
     EvalArgs base = eval_args(c, c->base.d + jb, nj, c->q, c->fphys, 0, 0);
     base.lj_full = full;
     launch_eval(c, base);
+    // learned centroid corrections of the systems that carry one (P = 1)
+    for (const auto &g : c->surrogates) {
+        if (sys >= 0 && g.sys != sys) continue;
+        const SysDev &S = c->sys_h[g.sys];
+        SurrogateRun r;
+        r.pos = c->q + S.q_off;
+        r.f = c->fphys + S.q_off;
+        r.n_mols = S.n_mols;
+        r.n_sm = c->n_sm;
+        for (int k = 0; k < 3; ++k) r.box[k] = S.box[k];
+        r.wbf = g.wbf;
+        r.bias = g.bias;
+        r.norm = g.norm;
+        r.out_scale = g.out_scale;
+        r.desc = g.desc;
+        r.y = g.y;
+        r.frames = g.frames;
+        r.feat = g.feat;
+        r.status = c->status;
+        launch_surrogate_correction(r, c->stream, &c->launches);
+    }
     // odd beads that need the Suzuki-Chin force gradient
     const int *osys, *obead;
     const Job *fdj, *tanj;
@@ -513,6 +542,8 @@ qtg_status sync_status(qtg_ctx *ctx) {
         if (st & ST_LIST_OVERFLOW) return fail(ctx, QTG_ERR_LIST_OVERFLOW, "Verlet list exceeded list_size");
         if (st & ST_NONFINITE) return fail(ctx, QTG_ERR_NONFINITE, "non-finite energy or force");
         if (st & ST_GAMMA_LIMIT) return fail(ctx, QTG_ERR_NONFINITE, "gamma variate iteration limit reached");
+        if (st & ST_DESC_OVERFLOW) return fail(ctx, QTG_ERR_ARG, "more than 256 atoms within the descriptor cutoff");
+        if (st & ST_MMA_TIMEOUT) return fail(ctx, QTG_ERR_CUDA, "tensor-core completion wait ran out");
     }
     return QTG_OK;
 }
@@ -574,6 +605,13 @@ void drop_graphs(qtg_ctx *ctx) {
         ctx->graph[i] = nullptr;
         ctx->graph_kernels[i] = 0;
     }
+}
+
+void free_surrogate(qtg_ctx::Surrogate &g) {
+    void *ptrs[] = {g.wbf, g.feat, g.bias, g.norm, g.desc, g.y, g.frames};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    g = qtg_ctx::Surrogate();
 }
 
 // Average duration (ms) of `iters` launches of `fn` on the context's stream.
@@ -879,6 +917,10 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     init_force_kernel_attributes();
     init_list_kernel_attributes();
     init_propagate_kernel_attributes();
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&ctx->n_sm, cudaDevAttrMultiProcessorCount, dev);
+    }
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
     ctx->stream = ctx->own_stream;
 #define AL(ptr, n)                                  \
@@ -1023,6 +1065,7 @@ void qtg_destroy(qtg_ctx *ctx) {
                     ctx->status, ctx->red_out};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    for (auto &g : ctx->surrogates) free_surrogate(g);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -1090,6 +1133,66 @@ qtg_status qtg_get_centroid_force(qtg_ctx *ctx, int sys, double *f_mean, double 
     CK(cudaMemcpy(&ns, &ctx->run[sys].cf_samples, sizeof(double), cudaMemcpyDeviceToHost));
     for (int i = 0; i < S.n_dof; ++i) f_mean[i] = ns > 0.0 ? acc[i] / ns : 0.0;
     *n_samples = ns;
+    return QTG_OK;
+}
+
+qtg_status qtg_detach_surrogate(qtg_ctx *ctx, int sys) {
+    CKS(check_sys(ctx, sys));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (size_t i = 0; i < ctx->surrogates.size(); ++i)
+        if (ctx->surrogates[i].sys == sys) {
+            free_surrogate(ctx->surrogates[i]);
+            ctx->surrogates.erase(ctx->surrogates.begin() + (long)i);
+            drop_graphs(ctx);
+            break;
+        }
+    return QTG_OK;
+}
+
+qtg_status qtg_attach_surrogate(qtg_ctx *ctx, int sys, const qtg_mlp_weights *w, const float *norm, float out_scale) {
+    CKS(check_sys(ctx, sys));
+    if (!w || !w->w1 || !w->w2 || !w->w3 || !w->b1 || !w->b2 || !w->b3 || !norm)
+        return fail(ctx, QTG_ERR_ARG, "null surrogate array");
+    const SysDev &S = ctx->sys_h[sys];
+    if (S.n_beads != 1) return fail(ctx, QTG_ERR_ARG, "the centroid correction applies to P = 1 (centroid) systems");
+    const double rc = 6.0 / 0.529177210903;
+    for (int d = 0; d < 3; ++d)
+        if (!(S.box[d] > 2.0 * rc)) return fail(ctx, QTG_ERR_ARG, "box sides must exceed twice the 6 A cutoff");
+    CKS(qtg_detach_surrogate(ctx, sys));
+    init_surrogate_kernel_attributes();
+    qtg_ctx::Surrogate g;
+    g.sys = sys;
+    g.out_scale = out_scale;
+    const int N = S.n_mols, n1 = QTG_MLP_HIDDEN * QTG_MLP_IN, n2 = QTG_MLP_HIDDEN * QTG_MLP_HIDDEN,
+              n3 = QTG_MLP_OUT_PAD * QTG_MLP_HIDDEN;
+    cudaError_t e = cudaSuccess;
+    auto al = [&](void **p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    };
+    al((void **)&g.wbf, sizeof(__nv_bfloat16) * (n1 + n2 + n3));
+    al((void **)&g.bias, sizeof(float) * (2 * QTG_MLP_HIDDEN + QTG_MLP_OUT_PAD));
+    al((void **)&g.norm, sizeof(float) * 2 * QTG_MLP_IN);
+    al((void **)&g.desc, sizeof(float) * 3 * N * QTG_DESC_PER_ATOM);
+    al((void **)&g.feat, sizeof(__nv_bfloat16) * 2 * N * QTG_MLP_IN);
+    al((void **)&g.y, sizeof(float) * 2 * N * QTG_MLP_OUT_PAD);
+    al((void **)&g.frames, sizeof(float) * 9 * N);
+    auto cp = [&](void *dst, const void *src, size_t bytes, cudaMemcpyKind k) {
+        if (e == cudaSuccess) e = cudaMemcpy(dst, src, bytes, k);
+    };
+    cp(g.wbf, w->w1, sizeof(__nv_bfloat16) * n1, cudaMemcpyDeviceToDevice);
+    cp(g.wbf + n1, w->w2, sizeof(__nv_bfloat16) * n2, cudaMemcpyDeviceToDevice);
+    cp(g.wbf + n1 + n2, w->w3, sizeof(__nv_bfloat16) * n3, cudaMemcpyDeviceToDevice);
+    cp(g.bias, w->b1, sizeof(float) * QTG_MLP_HIDDEN, cudaMemcpyDeviceToDevice);
+    cp(g.bias + QTG_MLP_HIDDEN, w->b2, sizeof(float) * QTG_MLP_HIDDEN, cudaMemcpyDeviceToDevice);
+    cp(g.bias + 2 * QTG_MLP_HIDDEN, w->b3, sizeof(float) * QTG_MLP_OUT_PAD, cudaMemcpyDeviceToDevice);
+    cp(g.norm, norm, sizeof(float) * 2 * QTG_MLP_IN, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        free_surrogate(g);
+        return fail(ctx, QTG_ERR_CUDA, std::string("surrogate attach: ") + cudaGetErrorString(e));
+    }
+    ctx->surrogates.push_back(g);
+    drop_graphs(ctx);
+    ctx->forces_ready = false;
     return QTG_OK;
 }
 

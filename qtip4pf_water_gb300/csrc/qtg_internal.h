@@ -1,6 +1,7 @@
 // Internal definitions shared by the CUDA translation units of libqtipgpu.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -345,6 +346,25 @@ struct EvalArgs {
     int mode;              // 0 = forces, 1 = directional derivative of the Ewald forces
     Consts c;
 };
+
+// surrogate.cu: the learned centroid correction of one P = 1 system, added to
+// its forces inside a force evaluation (descriptors, features, tensor-core
+// forward pass, frames, lab-frame correction)
+struct SurrogateRun {
+    const double *pos;            // [9N] positions of the system
+    double *f;                    // [9N] forces to correct
+    int n_mols, n_sm;
+    double box[3];
+    const __nv_bfloat16 *wbf;     // w1 | w2 | w3, BF16
+    const float *bias;            // b1 | b2 | b3
+    const float *norm;            // input mean [96] | inverse standard deviation [96]
+    float out_scale;
+    float *desc, *y, *frames;     // scratch: [3N][32], [2N][16], [N][9]
+    __nv_bfloat16 *feat;          // scratch: [2N][96]
+    unsigned *status;
+};
+void launch_surrogate_correction(const SurrogateRun &r, cudaStream_t s, unsigned long long *launches);
+void init_surrogate_kernel_attributes();
 
 // forces.cu: individual Ewald kernels (for timing)
 void launch_ewald_kernel(const EvalArgs &a, bool mixed, const char *name, cudaStream_t s);

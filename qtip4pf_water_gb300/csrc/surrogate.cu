@@ -651,6 +651,126 @@ __global__ void k_adam(float *w, float *m1, float *m2, const float *g, int n, fl
 }  // namespace
 }  // namespace qtg
 
+namespace qtg {
+namespace {
+
+// ---- deployment: the correction inside a force evaluation ------------------------
+// Molecular frame of a water with its H atoms labelled (a, b): e1 along the
+// bisector d_a + d_b, e2 along d_a - d_b made orthogonal to e1, e3 = e1 x e2,
+// with d = r_H - r_O (minimum image). Swapping the labels maps (e1, e2, e3) to
+// (e1, -e2, -e3). frames: float[N][9] = e1, e2, e3 of labelling (H1, H2).
+__global__ void k_frames(const double *pos, int n_mols, double bx, double by, double bz, float *frames) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n_mols) return;
+    const double *r = pos + 9 * m;
+    const double L[3] = {bx, by, bz};
+    double d1[3], d2[3];
+    for (int k = 0; k < 3; ++k) {
+        d1[k] = r[3 + k] - r[k];
+        d2[k] = r[6 + k] - r[k];
+        d1[k] -= L[k] * rint(d1[k] / L[k]);
+        d2[k] -= L[k] * rint(d2[k] / L[k]);
+    }
+    float e1[3], e2[3], e3[3];
+    float n1 = 0.f, n2 = 0.f, pj = 0.f;
+    for (int k = 0; k < 3; ++k) {
+        e1[k] = (float)(d1[k] + d2[k]);
+        n1 += e1[k] * e1[k];
+    }
+    n1 = rsqrtf(n1);
+    for (int k = 0; k < 3; ++k) {
+        e1[k] *= n1;
+        e2[k] = (float)(d1[k] - d2[k]);
+        pj += e2[k] * e1[k];
+    }
+    for (int k = 0; k < 3; ++k) {
+        e2[k] -= pj * e1[k];
+        n2 += e2[k] * e2[k];
+    }
+    n2 = rsqrtf(n2);
+    for (int k = 0; k < 3; ++k) e2[k] *= n2;
+    e3[0] = e1[1] * e2[2] - e1[2] * e2[1];
+    e3[1] = e1[2] * e2[0] - e1[0] * e2[2];
+    e3[2] = e1[0] * e2[1] - e1[1] * e2[0];
+    float *f = frames + 9 * m;
+    for (int k = 0; k < 3; ++k) {
+        f[k] = e1[k];
+        f[3 + k] = e2[k];
+        f[6 + k] = e3[k];
+    }
+}
+
+// Network inputs of every molecule in both labellings: rows m (O, H1, H2) and
+// N + m (O, H2, H1), each value normalised as (g - mean) * inv_std, in BF16.
+__global__ void k_mol_features(const float *desc, int n_mols, const float *norm, __nv_bfloat16 *feat) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= 2LL * n_mols * DIN) return;
+    const int row = (int)(e / DIN), c = (int)(e - (long long)row * DIN);
+    const int m = row % n_mols, swap = row >= n_mols;
+    int atom = c / ND;  // 0 = O, 1 = first H, 2 = second H of this labelling
+    if (swap && atom > 0) atom = 3 - atom;
+    const float g = desc[((size_t)3 * m + atom) * ND + (c % ND)];
+    feat[e] = __float2bfloat16_rn((g - norm[c]) * norm[DIN + c]);
+}
+
+// Lab-frame correction, symmetrised over the two labellings, added to the
+// forces: for atom a of the molecule, F_a += s * (R_ab y_ab[a] + R_ba y_ba[a']) / 2
+// with R the frame matrices and y scaled by the output scale s.
+__global__ void k_apply_correction(const float *frames, const float *y, int n_mols, float out_scale, double *f) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n_mols) return;
+    const float *e = frames + 9 * m;
+    const float *ya = y + (size_t)m * DOUT, *yb = y + (size_t)(n_mols + m) * DOUT;
+    for (int a = 0; a < 3; ++a) {
+        const int ab = (a == 0) ? 0 : (3 - a);  // the same atom's slot in the swapped labelling
+        const float c1 = ya[3 * a], c2 = ya[3 * a + 1], c3 = ya[3 * a + 2];
+        const float s1 = yb[3 * ab], s2 = yb[3 * ab + 1], s3 = yb[3 * ab + 2];
+        for (int k = 0; k < 3; ++k) {
+            const float v = 0.5f * ((c1 + s1) * e[k] + (c2 - s2) * e[3 + k] + (c3 - s3) * e[6 + k]);
+            f[9 * m + 3 * a + k] += (double)(out_scale * v);
+        }
+    }
+}
+
+}  // namespace
+
+void launch_surrogate_correction(const SurrogateRun &r, cudaStream_t s, unsigned long long *launches) {
+    const int N = r.n_mols;
+    DescArgs d;
+    d.pos = r.pos;
+    d.n_conf = 1;
+    d.n_mols = N;
+    for (int k = 0; k < 3; ++k) d.box[k] = r.box[k];
+    d.desc = r.desc;
+    d.rc_ang = 6.0f;
+    d.status = r.status;
+    k_descriptors<<<(3 * N + DW - 1) / DW, 32 * DW, 0, s>>>(d);
+    const long long nf = 2LL * N * DIN;
+    k_mol_features<<<(unsigned)((nf + 255) / 256), 256, 0, s>>>(r.desc, N, r.norm, r.feat);
+    MlpArgs a;
+    a.w1 = r.wbf;
+    a.w2 = r.wbf + DH * DIN;
+    a.w3 = r.wbf + DH * DIN + DH * DH;
+    a.b1 = r.bias;
+    a.b2 = r.bias + DH;
+    a.b3 = r.bias + 2 * DH;
+    a.x = r.feat;
+    a.m = 2 * N;
+    a.y = r.y;
+    a.status = r.status;
+    const int tiles = (2 * N + TM - 1) / TM;
+    k_mlp_fwd<<<tiles < 2 * r.n_sm ? tiles : 2 * r.n_sm, TM, (size_t)F_END + 1024, s>>>(a);
+    k_frames<<<(N + 127) / 128, 128, 0, s>>>(r.pos, N, r.box[0], r.box[1], r.box[2], r.frames);
+    k_apply_correction<<<(N + 127) / 128, 128, 0, s>>>(r.frames, r.y, N, r.out_scale, r.f);
+    if (launches) *launches += 5;
+}
+
+void init_surrogate_kernel_attributes() {
+    cudaFuncSetAttribute(k_mlp_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(F_END + 1024));
+}
+
+}  // namespace qtg
+
 // ---- C ABI -----------------------------------------------------------------------
 namespace {
 __device__ unsigned g_surrogate_status;  // error bits of the surrogate kernels (bounded waits, overflows)
