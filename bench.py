@@ -146,10 +146,12 @@ def count_pairs(q, box, rc2, n_mols):
     return nreal / 2.0 / nb, nlj / nb
 
 
-def make_system(q_mod, precision, propagator, st):
+def make_system(q_mod, precision, propagator, st, autotune=False):
     s = q_mod.System.create(N_MOLS, N_BEADS, st.box_bohr, precision=precision, temp_K=TEMP, dt_fs=DT_FS,
                             propagator=propagator, thermostat=q_mod.PILE_G, seed=SEED)
     s.set_state(st.q, st.p)
+    if autotune:
+        s.ctx.autotune(10)  # the library's launch-shape autotuner (chunk counts of the force kernels)
     s.ctx.init_forces()
     return s
 
@@ -196,7 +198,8 @@ def run_gpu(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     # ---- headline: mixed precision, Trotter -----------------------------------------------
-    mix = make_system(q, q.MIXED, q.TROTTER, st)
+    mix = make_system(q, q.MIXED, q.TROTTER, st, autotune=True)
+    tuned = mix.ctx.tuning()
     sampler = ClockSampler(local)
     sampler.start()
     if dist:
@@ -243,6 +246,7 @@ def run_gpu(args):
         "config": {"workload": WORKLOAD, "precision": "mixed", "propagator": "trotter", "thermostat": "pile_g",
                    "n_mols": N_MOLS, "n_beads": N_BEADS, "dt_fs": DT_FS,
                    "l2": "flushed (256 MiB write) before every timed step; flush not timed",
+                   "launch_shapes": "autotuned chunks (real, structure factor, k-force) = %d, %d, %d" % tuned,
                    "parallelism": "replicas only" if world > 1 else "single GPU"},
         "bead_steps_per_s": N_BEADS * args.steps / t_mix,
         "fp64_ns_day": ns_per_day(t64 / k2), "fp64_ms_per_step": t64 / k2 * 1e3,

@@ -281,8 +281,8 @@ qtg_status qtg_surrogate_status(unsigned *bits, int clear);
 
 /* ---- launch-shape autotuner (no reference counterpart) ---------------------- */
 /* The three dominant force kernels split their work into chunks whose counts
- * set the grid sizes: real-space j-chunks (k_real), structure-factor site
- * chunks (k_ksk) and k-vector chunks (k_kforce), each in [1, 8]. By default a
+ * set the grid sizes: real-space j-chunks (k_real, 1..16), structure-factor
+ * site chunks (k_ksk, 1..32) and k-vector chunks (k_kforce, 1..16). By default a
  * heuristic sizes each grid for about 12 blocks per SM over all of the
  * context's systems. qtg_autotune times every candidate count of each kernel
  * on the context's own batch (iters launches each), then keeps the tuned

@@ -253,6 +253,7 @@ struct qtg_ctx {
         float out_scale = 1.f;
         __nv_bfloat16 *wbf = nullptr, *feat = nullptr;
         float *bias = nullptr, *norm = nullptr, *desc = nullptr, *y = nullptr, *frames = nullptr;
+        float4 *wrapped = nullptr;
     };
     std::vector<Surrogate> surrogates;
     int n_sm = 148;
@@ -460,6 +461,7 @@ void enqueue_forces(qtg_ctx *c, int sys, bool force_sc) {
         r.y = g.y;
         r.frames = g.frames;
         r.feat = g.feat;
+        r.wrapped = g.wrapped;
         r.status = c->status;
         launch_surrogate_correction(r, c->stream, &c->launches);
     }
@@ -608,7 +610,7 @@ void drop_graphs(qtg_ctx *ctx) {
 }
 
 void free_surrogate(qtg_ctx::Surrogate &g) {
-    void *ptrs[] = {g.wbf, g.feat, g.bias, g.norm, g.desc, g.y, g.frames};
+    void *ptrs[] = {g.wbf, g.feat, g.bias, g.norm, g.desc, g.y, g.frames, g.wrapped};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     g = qtg_ctx::Surrogate();
@@ -1176,6 +1178,7 @@ qtg_status qtg_attach_surrogate(qtg_ctx *ctx, int sys, const qtg_mlp_weights *w,
     al((void **)&g.feat, sizeof(__nv_bfloat16) * 2 * N * QTG_MLP_IN);
     al((void **)&g.y, sizeof(float) * 2 * N * QTG_MLP_OUT_PAD);
     al((void **)&g.frames, sizeof(float) * 9 * N);
+    al((void **)&g.wrapped, sizeof(float4) * 3 * N);
     auto cp = [&](void *dst, const void *src, size_t bytes, cudaMemcpyKind k) {
         if (e == cudaSuccess) e = cudaMemcpy(dst, src, bytes, k);
     };
@@ -1652,7 +1655,7 @@ qtg_status qtg_time_kernel(qtg_ctx *ctx, const char *name, int iters, double *av
 
 qtg_status qtg_set_tuning(qtg_ctx *ctx, int n_rj, int n_sc, int n_kc) {
     if (!ctx || n_rj < 0 || n_sc < 0 || n_kc < 0 || n_rj > MAX_RJ || n_sc > MAX_SC || n_kc > MAX_KC)
-        return fail(ctx, QTG_ERR_ARG, "chunk counts must lie in [0, 8] (0: heuristic)");
+        return fail(ctx, QTG_ERR_ARG, "chunk counts must lie in [0, 16], [0, 32], [0, 16] (0: heuristic)");
     ctx->tune[0] = n_rj;
     ctx->tune[1] = n_sc;
     ctx->tune[2] = n_kc;
@@ -1682,7 +1685,8 @@ qtg_status qtg_autotune(qtg_ctx *ctx, int iters, double *ms_heuristic, double *m
         return time_on_stream(ctx, iters, [&] { launch_eval(ctx, a); }, ms);
     };
     // each count governs one kernel: k_real (n_rj), k_ksk (n_sc), k_kforce (n_kc)
-    static const int cand[] = {1, 2, 3, 4, 5, 6, 8};
+    static const int cand_rk[] = {1, 2, 3, 4, 6, 8, 12, 16};          // k_real, k_kforce
+    static const int cand_sc[] = {1, 2, 4, 6, 8, 12, 16, 24, 32};     // k_ksk
     static const char *kname[3] = {"real", "ksk", "kforce"};
     int best[3] = {0, 0, 0};
     {
@@ -1692,7 +1696,10 @@ qtg_status qtg_autotune(qtg_ctx *ctx, int iters, double *ms_heuristic, double *m
     }
     for (int k = 0; k < 3; ++k) {
         double best_ms = 1e30;
-        for (int c : cand) {
+        const int *cand = k == 1 ? cand_sc : cand_rk;
+        const int n_cand = k == 1 ? (int)(sizeof(cand_sc) / sizeof(int)) : (int)(sizeof(cand_rk) / sizeof(int));
+        for (int ci = 0; ci < n_cand; ++ci) {
+            const int c = cand[ci];
             int t[3] = {0, 0, 0};
             t[k] = c;
             for (int q = 0; q < 3; ++q) ctx->tune[q] = t[q];

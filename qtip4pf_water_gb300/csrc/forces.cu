@@ -1082,7 +1082,8 @@ __global__ void __launch_bounds__(128) k_lj(EvalArgs a) {
 // the list loop of forces.cpp:489-515. This kernel forms that sum without going
 // through the list: the bead's wrapped oxygen positions are staged through
 // shared memory, LJD_SUB lanes share a row and split its j's (each warp reads
-// LJD_SUB consecutive positions per step: one shared-memory wavefront), and the
+// LJD_SUB consecutive positions per step: at most one shared-memory wavefront
+// for eight lanes a row), and the
 // row's sums are reduced over those lanes in FP32 with shuffles. Each pair is
 // seen from both ends; the energy is halved.
 //
@@ -1091,8 +1092,6 @@ __global__ void __launch_bounds__(128) k_lj(EvalArgs a) {
 // arithmetic (as in k_lj). They are rare, and that FP64 code is kept out of the
 // main loop: the loop skips them and raises a block flag, and only blocks that
 // saw one run a second pass that evaluates exactly those pairs.
-constexpr int LJD_SUB = 8;                  // lanes per row
-constexpr int LJD_ROWS = 128 / LJD_SUB;     // rows per 128-thread block
 constexpr int LJD_CH = 1024;                // oxygens per shared-memory chunk
 
 struct LjdConst {
@@ -1129,7 +1128,9 @@ __device__ __forceinline__ void ljd_pair(const float *r, float rr, const LjdCons
     fz = fmaf(ff, r[2], fz);
 }
 
+template <int LJD_SUB>  // lanes per row: 8, or 32 when there are too few rows to fill the GPU
 __global__ void __launch_bounds__(128) k_lj_dense(EvalArgs a) {
+    constexpr int LJD_ROWS = 128 / LJD_SUB;  // rows per 128-thread block
     const int jb = blockIdx.y;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
@@ -1281,6 +1282,12 @@ int chunks_or(int tuned, long long base_blocks, int maxc) {
     return tuned > 0 ? std::min(tuned, maxc) : chunks_for(base_blocks, maxc);
 }
 
+void launch_lj_dense(const EvalArgs &a, cudaStream_t s) {
+    const long long blocks8 = (long long)((a.max_mols + 15) / 16) * a.n_jobs;
+    if (blocks8 >= 2LL * 152) k_lj_dense<8><<<dim3((a.max_mols + 15) / 16, a.n_jobs), 128, 0, s>>>(a);
+    else k_lj_dense<32><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
+}
+
 template <typename R>
 void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n) {
     const int ns = 3 * a.max_mols;
@@ -1307,7 +1314,7 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n) {
     if (n) *n += 6;
     if (a.mode == 0) {
         if (sizeof(R) == 4 && a.lj_full)
-            k_lj_dense<<<dim3((a.max_mols + LJD_ROWS - 1) / LJD_ROWS, a.n_jobs), 128, 0, s>>>(a);
+            launch_lj_dense(a, s);
         else if (a.lj_full) k_lj<R, 1><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
         else k_lj<R, 0><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
         if (n) *n += 1;
@@ -1351,7 +1358,7 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
         else k_combine<double><<<gm, 128, 0, s>>>(a);
     } else if (n == "lj") {
         if (mixed) {
-            if (a.lj_full) k_lj_dense<<<dim3((a.max_mols + LJD_ROWS - 1) / LJD_ROWS, a.n_jobs), 128, 0, s>>>(a);
+            if (a.lj_full) launch_lj_dense(a, s);
             else k_lj<float, 0><<<gl, 128, 0, s>>>(a);
         } else {
             if (a.lj_full) k_lj<double, 1><<<gl, 128, 0, s>>>(a);

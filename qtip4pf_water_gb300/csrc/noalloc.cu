@@ -32,6 +32,7 @@ constexpr int NA_COLS = (NA_MAX_KMAX + 1) * (2 * NA_MAX_KMAX + 1);  // every (kx
 constexpr int NA_MAX_K = NA_COLS * (2 * NA_MAX_KMAX + 1);          // every kz of every column
 constexpr int NA_MAX_GRP = NA_COLS * ((NA_MAX_KMAX + 1 + 3) / 4);
 constexpr int NA_MAX_BATCH = NA_COLS;
+constexpr int NA_SC = 8, NA_KC = 8;  // structure-factor site chunks and k-chunks the scratch holds
 
 constexpr size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr size_t OFF_SYS = 0;
@@ -43,9 +44,9 @@ constexpr size_t OFF_KBATCH = OFF_KGRP + al256(sizeof(KGroup) * NA_MAX_GRP);
 constexpr size_t OFF_SITES = OFF_KBATCH + al256(sizeof(KBatch) * NA_MAX_BATCH);
 constexpr size_t OFF_PHASE = OFF_SITES + al256(4 * sizeof(double) * NA_MAX_SITES);
 constexpr size_t OFF_SKP = OFF_PHASE + al256(2 * sizeof(double) * 3 * (NA_MAX_KMAX + 1) * NA_MAX_SITES);
-constexpr size_t OFF_WSK = OFF_SKP + al256(2 * sizeof(double) * MAX_SC * NA_MAX_K);
+constexpr size_t OFF_WSK = OFF_SKP + al256(2 * sizeof(double) * NA_SC * NA_MAX_K);
 constexpr size_t OFF_PART = OFF_WSK + al256(2 * sizeof(double) * NA_MAX_K);
-constexpr size_t OFF_STATUS = OFF_PART + al256(3 * sizeof(double) * MAX_KC * NA_MAX_SITES);
+constexpr size_t OFF_STATUS = OFF_PART + al256(3 * sizeof(double) * NA_KC * NA_MAX_SITES);
 constexpr size_t NA_BYTES = OFF_STATUS + 256;
 
 // All scratch of qtg_kwald_noalloc. In host code this name is only a host-side
@@ -303,6 +304,8 @@ extern "C" qtg_status qtg_kwald_noalloc(const double *sites, const double *charg
     a.energy = energy;
     a.status = reinterpret_cast<unsigned *>(base + OFF_STATUS);
     a.sites_are_input = 1;
+    a.tune_sc = NA_SC;  // the scratch holds this many partial planes
+    a.tune_kc = NA_KC;
     launch_kwald_only(a, false, s, nullptr);
     return cudaGetLastError() == cudaSuccess ? QTG_OK : QTG_ERR_CUDA;
 }

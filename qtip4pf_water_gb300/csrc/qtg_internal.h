@@ -302,9 +302,9 @@ void launch_nm_energy(const SysDev *sys, int sysi, int P, int n_dof, const doubl
                       unsigned long long *n);
 
 // Chunking limits of the force kernels' second grid dimension.
-constexpr int MAX_RJ = 8;    // real-space j-chunks
-constexpr int MAX_KC = 8;    // reciprocal-space k-chunks
-constexpr int MAX_SC = 8;    // structure-factor site chunks
+constexpr int MAX_RJ = 16;   // real-space j-chunks
+constexpr int MAX_KC = 16;   // reciprocal-space k-chunks
+constexpr int MAX_SC = 32;   // structure-factor site chunks
 constexpr int MAX_PART = MAX_RJ + MAX_KC + 1;  // partial site-force planes
 
 struct EvalArgs {
@@ -360,6 +360,7 @@ struct SurrogateRun {
     const float *norm;            // input mean [96] | inverse standard deviation [96]
     float out_scale;
     float *desc, *y, *frames;     // scratch: [3N][32], [2N][16], [N][9]
+    float4 *wrapped;              // scratch: [3N] atoms wrapped into the box (A, FP32)
     __nv_bfloat16 *feat;          // scratch: [2N][96]
     unsigned *status;
 };

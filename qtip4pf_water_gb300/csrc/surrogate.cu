@@ -6,7 +6,7 @@
 // molecule's own frame. This file holds its device side:
 //
 //   k_descriptors   Behler-Parrinello radial (G2) and angular (G4) symmetry
-//                   functions within 6 A, 32 per atom, one warp per atom
+//                   functions within 6 A, 32 per atom, one warp per molecule
 //   k_mlp_fwd       the network's forward pass on the tensor cores: BF16
 //                   operands in shared memory, tcgen05.mma into FP32
 //                   accumulators in tensor memory, bias + SiLU epilogues
@@ -38,16 +38,15 @@ namespace {
 // Layout of the 32 values of an atom:
 //   0..7    G2, neighbours O, eta = G2_ETA[0..7]
 //   8..15   G2, neighbours H
-//   16..23  G4, neighbour pair of one species (OO or HH), (zeta, lambda, eta) = G4_SET[0..7]
+//   16..23  G4, neighbour pair of one species (OO or HH), the eight G4 sets below
 //   24..31  G4, mixed neighbour pair (OH)
 // Atoms are O, H1, H2 of each molecule in the reference's order; every atom
 // within R_c counts, the atom's own molecule included.
 constexpr int ND = QTG_DESC_PER_ATOM;
 constexpr int NB_MAX = 256;  // neighbours within R_c kept per atom
 __constant__ float G2_ETA[8] = {0.001f, 0.01f, 0.03f, 0.06f, 0.15f, 0.3f, 0.7f, 1.5f};  // 1/A^2
-__constant__ float G4_ZETA[8] = {1.f, 1.f, 2.f, 2.f, 1.f, 1.f, 2.f, 2.f};
-__constant__ float G4_LAMBDA[8] = {1.f, -1.f, 1.f, -1.f, 1.f, -1.f, 1.f, -1.f};
-__constant__ float G4_ETA[8] = {0.005f, 0.005f, 0.005f, 0.005f, 0.02f, 0.02f, 0.02f, 0.02f};  // 1/A^2
+// G4 sets, in this order: (zeta, lambda) = (1, +1), (1, -1), (2, +1), (2, -1) with
+// eta = 0.005 / A^2, then the same four with eta = 0.02 / A^2
 
 constexpr float BOHR_A = 0.529177210903f;
 
@@ -57,101 +56,170 @@ struct DescArgs {
     const double *pos;  // [n_conf][9N] bohr
     int n_conf, n_mols;
     double box[3];      // bohr
+    float4 *wrapped;    // scratch [n_conf][3N]: atoms wrapped into the box, A
     float *desc;        // [n_conf][3N][32]
     float rc_ang;       // cutoff, A
     unsigned *status;
 };
 
-// One warp per atom: the lanes scan every atom of the configuration and compact
-// the neighbours within R_c into shared memory (ballot + prefix), then sum G2
-// over neighbours and G4 over neighbour pairs, and reduce over the warp.
-constexpr int DW = 4;  // warps per block
+// Atoms wrapped into [0, L) and converted to FP32 Angstrom once, so that the
+// neighbour scan runs in FP32 (w = species: 0 = O, 1 = H).
+__global__ void k_wrap_atoms(DescArgs a) {
+    const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int na = 3 * a.n_mols;
+    if (g >= (long long)a.n_conf * na) return;
+    const double *r = a.pos + 3 * g;
+    float v[3];
+    for (int d = 0; d < 3; ++d) {
+        const double L = a.box[d], t = r[d] / L;
+        v[d] = (float)((t - floor(t)) * L) * BOHR_A;
+    }
+    a.wrapped[g] = make_float4(v[0], v[1], v[2], (g % na) % 3 ? 1.f : 0.f);
+}
+
+// One warp per molecule. The lanes first scan the molecules' oxygens and keep
+// the molecules whose O lies within R_c + CAND_MARGIN of this molecule's O
+// (an atom within R_c of one of this molecule's atoms belongs to such a
+// molecule: every H lies within CAND_MARGIN / 2 of its O); then, for each of
+// the three atoms in turn, the candidates' atoms within R_c are compacted into
+// shared memory (ballot + prefix), G2 is summed over them and G4 over their
+// pairs, and the sums are reduced over the warp. The G4 sets share one
+// Gaussian per pair (exp(-0.02 s) = exp(-0.005 s)^4) and two angular bases
+// (1 +- cos theta).
+constexpr int DW = 4;            // warps per block
+constexpr int CAND_MAX = 256;    // candidate molecules kept per molecule
+constexpr float CAND_MARGIN = 3.2f;  // A
 __global__ void __launch_bounds__(32 * DW) k_descriptors(DescArgs a) {
+    __shared__ int cand[DW][CAND_MAX];
     __shared__ float4 nb[DW][NB_MAX];   // (dx, dy, dz, r) in A, minimum image
+    __shared__ float nfc[DW][NB_MAX];   // f_c(r)
     __shared__ unsigned char sp[DW][NB_MAX];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int na = 3 * a.n_mols;
-    const long long g = (long long)blockIdx.x * DW + warp;  // global atom index over configurations
-    if (g >= (long long)a.n_conf * na) return;
-    const int conf = (int)(g / na), i = (int)(g - (long long)conf * na);
-    const double *q = a.pos + (size_t)conf * 3 * na;
-    const double L[3] = {a.box[0], a.box[1], a.box[2]};
-    const float rc = a.rc_ang, rc2 = rc * rc;
-    const double xi = q[3 * i], yi = q[3 * i + 1], zi = q[3 * i + 2];
-    int n = 0;
-    for (int j0 = 0; j0 < na; j0 += 32) {
+    const int N = a.n_mols, na = 3 * N;
+    const long long g = (long long)blockIdx.x * DW + warp;  // global molecule index over configurations
+    if (g >= (long long)a.n_conf * N) return;
+    const int conf = (int)(g / N), mol = (int)(g - (long long)conf * N);
+    const float4 *w = a.wrapped + (size_t)conf * na;
+    const float L[3] = {(float)a.box[0] * BOHR_A, (float)a.box[1] * BOHR_A, (float)a.box[2] * BOHR_A};
+    const float IL[3] = {1.f / L[0], 1.f / L[1], 1.f / L[2]};
+    const float rc = a.rc_ang, rc2 = rc * rc, irc = 1.f / rc;
+    const float rcand = rc + CAND_MARGIN, rcand2 = rcand * rcand;
+    auto disp = [&](const float4 &x, const float4 &y) {  // minimum-image y - x
+        float3 d;
+        d.x = y.x - x.x;
+        d.y = y.y - x.y;
+        d.z = y.z - x.z;
+        d.x = fmaf(-L[0], rintf(d.x * IL[0]), d.x);
+        d.y = fmaf(-L[1], rintf(d.y * IL[1]), d.y);
+        d.z = fmaf(-L[2], rintf(d.z * IL[2]), d.z);
+        return d;
+    };
+    // candidate molecules
+    const float4 om = w[3 * mol];
+    int nc = 0;
+    for (int j0 = 0; j0 < N; j0 += 32) {
         const int j = j0 + lane;
-        float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
         bool in = false;
-        if (j < na && j != i) {
-            double dx = q[3 * j] - xi, dy = q[3 * j + 1] - yi, dz = q[3 * j + 2] - zi;
-            dx -= L[0] * rint(dx / L[0]);
-            dy -= L[1] * rint(dy / L[1]);
-            dz -= L[2] * rint(dz / L[2]);
-            d = make_float4((float)dx * BOHR_A, (float)dy * BOHR_A, (float)dz * BOHR_A, 0.f);
-            const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
-            in = r2 < rc2;
-            d.w = sqrtf(r2);
+        if (j < N) {
+            const float3 d = disp(om, w[3 * j]);
+            in = d.x * d.x + d.y * d.y + d.z * d.z < rcand2;
         }
         const unsigned m = __ballot_sync(0xffffffffu, in);
-        const int at = n + __popc(m & ((1u << lane) - 1u));
-        if (in && at < NB_MAX) {
-            nb[warp][at] = d;
-            sp[warp][at] = (unsigned char)((j % 3) != 0);  // 0 = O, 1 = H
-        }
-        n += __popc(m);
+        const int at = nc + __popc(m & ((1u << lane) - 1u));
+        if (in && at < CAND_MAX) cand[warp][at] = j;
+        nc += __popc(m);
     }
-    if (n > NB_MAX) {
+    if (nc > CAND_MAX) {
         if (lane == 0) atomicOr(a.status, (unsigned)ST_DESC_OVERFLOW);
-        n = NB_MAX;
+        nc = CAND_MAX;
     }
     __syncwarp();
-    float acc[ND];
-#pragma unroll
-    for (int k = 0; k < ND; ++k) acc[k] = 0.f;
-    for (int jj = lane; jj < n; jj += 32) {
-        const float4 d = nb[warp][jj];
-        const float r2 = d.w * d.w, fc = fcut(d.w, rc);
-        const int o = sp[warp][jj] ? 8 : 0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const float v = __expf(-G2_ETA[k] * r2) * fc;
-            if (o) acc[8 + k] += v;
-            else acc[k] += v;
+    for (int atom = 0; atom < 3; ++atom) {
+        const int i = 3 * mol + atom;
+        const float4 xi = w[i];
+        int n = 0;
+        for (int c0 = 0; c0 < 3 * nc; c0 += 32) {
+            const int c = c0 + lane;
+            bool in = false;
+            float4 d4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            float spj = 0.f;
+            if (c < 3 * nc) {
+                const int j = 3 * cand[warp][c / 3] + c % 3;
+                if (j != i) {
+                    const float4 xj = w[j];
+                    const float3 d = disp(xi, xj);
+                    const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+                    in = r2 < rc2;
+                    d4 = make_float4(d.x, d.y, d.z, sqrtf(r2));
+                    spj = xj.w;
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, in);
+            const int at = n + __popc(m & ((1u << lane) - 1u));
+            if (in && at < NB_MAX) {
+                nb[warp][at] = d4;
+                nfc[warp][at] = fcut(d4.w, rc);
+                sp[warp][at] = (unsigned char)(spj > 0.5f);
+            }
+            n += __popc(m);
         }
-    }
-    for (int jj = lane; jj < n; jj += 32) {
-        const float4 dj = nb[warp][jj];
-        const float fj = fcut(dj.w, rc), rj2 = dj.w * dj.w;
-        for (int kk = jj + 1; kk < n; ++kk) {
-            const float4 dk = nb[warp][kk];
-            const float ex = dj.x - dk.x, ey = dj.y - dk.y, ez = dj.z - dk.z;
-            const float rjk2 = ex * ex + ey * ey + ez * ez;
-            if (rjk2 >= rc2) continue;
-            const float fk = fcut(dk.w, rc), fjk = fcut(sqrtf(rjk2), rc);
-            const float cs = (dj.x * dk.x + dj.y * dk.y + dj.z * dk.z) / (dj.w * dk.w);
-            const float s2 = rj2 + dk.w * dk.w + rjk2, f3 = fj * fk * fjk;
-            const bool same = sp[warp][jj] == sp[warp][kk];
+        if (n > NB_MAX) {
+            if (lane == 0) atomicOr(a.status, (unsigned)ST_DESC_OVERFLOW);
+            n = NB_MAX;
+        }
+        __syncwarp();
+        float acc[ND];
+#pragma unroll
+        for (int k = 0; k < ND; ++k) acc[k] = 0.f;
+        for (int jj = lane; jj < n; jj += 32) {
+            const float4 d = nb[warp][jj];
+            const float r2 = d.w * d.w, fc = nfc[warp][jj];
+            const bool h = sp[warp][jj];
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-                const float b = 1.0f + G4_LAMBDA[k] * cs;
-                const float ang = G4_ZETA[k] == 1.f ? b : 0.5f * b * b;  // 2^(1-zeta) (1 + lambda cos)^zeta
-                const float v = ang * __expf(-G4_ETA[k] * s2) * f3;
-                if (same) acc[16 + k] += v;
-                else acc[24 + k] += v;
+                const float v = __expf(-G2_ETA[k] * r2) * fc;
+                if (h) acc[8 + k] += v;
+                else acc[k] += v;
             }
         }
-    }
+        for (int jj = lane; jj < n; jj += 32) {
+            const float4 dj = nb[warp][jj];
+            const float fj = nfc[warp][jj], rj2 = dj.w * dj.w, ij = 1.f / dj.w;
+            const unsigned char sj = sp[warp][jj];
+            for (int kk = jj + 1; kk < n; ++kk) {
+                const float4 dk = nb[warp][kk];
+                const float ex = dj.x - dk.x, ey = dj.y - dk.y, ez = dj.z - dk.z;
+                const float rjk2 = ex * ex + ey * ey + ez * ez;
+                if (rjk2 >= rc2) continue;
+                const float fjk = 0.5f * (__cosf(3.14159265358979f * sqrtf(rjk2) * irc) + 1.0f);
+                const float cs = (dj.x * dk.x + dj.y * dk.y + dj.z * dk.z) * ij / dk.w;
+                const float f3 = fj * nfc[warp][kk] * fjk;
+                const float e1 = __expf(-0.005f * (rj2 + dk.w * dk.w + rjk2)), e2 = e1 * e1;
+                const float ga = e1 * f3, gb = e2 * e2 * f3;  // eta = 0.005 and 0.02 / A^2
+                const float bp = 1.f + cs, bm = 1.f - cs;
+                // (zeta, lambda) = (1, +1), (1, -1), (2, +1), (2, -1); 2^(1-zeta) (1 + lambda cos)^zeta
+                const float t0 = bp, t1 = bm, t2 = 0.5f * bp * bp, t3 = 0.5f * bm * bm;
+                if (sj == sp[warp][kk]) {
+                    acc[16] += t0 * ga; acc[17] += t1 * ga; acc[18] += t2 * ga; acc[19] += t3 * ga;
+                    acc[20] += t0 * gb; acc[21] += t1 * gb; acc[22] += t2 * gb; acc[23] += t3 * gb;
+                } else {
+                    acc[24] += t0 * ga; acc[25] += t1 * ga; acc[26] += t2 * ga; acc[27] += t3 * ga;
+                    acc[28] += t0 * gb; acc[29] += t1 * gb; acc[30] += t2 * gb; acc[31] += t3 * gb;
+                }
+            }
+        }
 #pragma unroll
-    for (int k = 0; k < ND; ++k) {
-        float v = acc[k];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        acc[k] = v;
-    }
-    if (lane == 0) {
-        float *out = a.desc + ((size_t)conf * na + i) * ND;
+        for (int k = 0; k < ND; ++k) {
+            float v = acc[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            acc[k] = v;
+        }
+        if (lane == 0) {
+            float *out = a.desc + ((size_t)conf * na + i) * ND;
 #pragma unroll
-        for (int k = 0; k < ND; ++k) out[k] = acc[k];
+            for (int k = 0; k < ND; ++k) out[k] = acc[k];
+        }
+        __syncwarp();
     }
 }
 
@@ -742,9 +810,11 @@ void launch_surrogate_correction(const SurrogateRun &r, cudaStream_t s, unsigned
     d.n_mols = N;
     for (int k = 0; k < 3; ++k) d.box[k] = r.box[k];
     d.desc = r.desc;
+    d.wrapped = r.wrapped;
     d.rc_ang = 6.0f;
     d.status = r.status;
-    k_descriptors<<<(3 * N + DW - 1) / DW, 32 * DW, 0, s>>>(d);
+    k_wrap_atoms<<<(3 * N + 255) / 256, 256, 0, s>>>(d);
+    k_descriptors<<<(N + DW - 1) / DW, 32 * DW, 0, s>>>(d);
     const long long nf = 2LL * N * DIN;
     k_mol_features<<<(unsigned)((nf + 255) / 256), 256, 0, s>>>(r.desc, N, r.norm, r.feat);
     MlpArgs a;
@@ -762,7 +832,7 @@ void launch_surrogate_correction(const SurrogateRun &r, cudaStream_t s, unsigned
     k_mlp_fwd<<<tiles < 2 * r.n_sm ? tiles : 2 * r.n_sm, TM, (size_t)F_END + 1024, s>>>(a);
     k_frames<<<(N + 127) / 128, 128, 0, s>>>(r.pos, N, r.box[0], r.box[1], r.box[2], r.frames);
     k_apply_correction<<<(N + 127) / 128, 128, 0, s>>>(r.frames, r.y, N, r.out_scale, r.f);
-    if (launches) *launches += 5;
+    if (launches) *launches += 6;
 }
 
 void init_surrogate_kernel_attributes() {
@@ -814,10 +884,17 @@ qtg_status qtg_sym_descriptors(const double *pos, int n_conf, int n_mols, const 
     a.rc_ang = 6.0f;
     a.status = st;
     const long long atoms = (long long)n_conf * 3 * n_mols;
-    const long long blocks = (atoms + qtg::DW - 1) / qtg::DW;
+    const long long blocks = ((long long)n_conf * n_mols + qtg::DW - 1) / qtg::DW;
     if (blocks > 0x7fffffffLL) return QTG_ERR_ARG;
-    qtg::k_descriptors<<<(unsigned)blocks, 32 * qtg::DW, 0, (cudaStream_t)stream>>>(a);
-    return cudaGetLastError() == cudaSuccess ? QTG_OK : QTG_ERR_CUDA;
+    cudaStream_t s = (cudaStream_t)stream;
+    void *wrapped = nullptr;  // stream-ordered scratch: the wrapped FP32 atoms
+    if (cudaMallocAsync(&wrapped, sizeof(float4) * (size_t)atoms, s) != cudaSuccess) return QTG_ERR_CUDA;
+    a.wrapped = static_cast<float4 *>(wrapped);
+    qtg::k_wrap_atoms<<<(unsigned)((atoms + 255) / 256), 256, 0, s>>>(a);
+    qtg::k_descriptors<<<(unsigned)blocks, 32 * qtg::DW, 0, s>>>(a);
+    const cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(wrapped, s);
+    return e == cudaSuccess ? QTG_OK : QTG_ERR_CUDA;
 }
 
 qtg_status qtg_mlp_forward(const qtg_mlp_weights *w, const void *x_bf16, int m, float *y, void *stream) {

@@ -170,6 +170,27 @@ def seeded_start(n_mols: int, n_beads: int = 1, temp_K: float = 298.0, seed: int
                       np.ascontiguousarray(p), temp_K, seed)
 
 
+def spread_beads(centroid: np.ndarray, n_beads: int, temp_K: float = 298.0, seed: int = 1):
+    """Beads around a given centroid configuration (double[9N]): the centroid
+    normal mode is the given centroid, modes k >= 1 are free-ring-polymer
+    Gaussian displacements at temp_K, bead momenta Maxwell-Boltzmann at the bead
+    temperature. Returns (q, p), each double[P][9N]."""
+    rng = SplitMix64(seed)
+    c = np.asarray(centroid, dtype=np.float64).reshape(-1)
+    n_mols = c.size // 9
+    P = n_beads
+    beta_n = 1.0 / (K2AU * temp_K) / P
+    mass = np.tile(np.repeat(np.array([MO, MH, MH]), 3), n_mols)
+    Q = np.zeros((P, c.size))
+    Q[0] = math.sqrt(P) * c
+    for k in range(1, P):
+        wk = (2.0 / beta_n) * math.sin(k * math.pi / P)
+        Q[k] = rng.normal(c.size) / np.sqrt(beta_n * mass * wk * wk)
+    q = nm_matrix(P).T @ Q
+    p = rng.normal(P * c.size).reshape(P, c.size) * np.sqrt(mass / beta_n)[None, :]
+    return np.ascontiguousarray(q), np.ascontiguousarray(p)
+
+
 def default_charges(n_mols: int) -> np.ndarray:
     """Per-site charges (M, H1, H2) as simulation.cpp:811-816 sets them."""
     qo = -1.1128

@@ -18,6 +18,11 @@ reference names no dataset):
   sc512         512 waters, P = 16, Suzuki-Chin, 298 K, dt = 0.25 fs: NVE
                 energy drift per ns of the conserved quantity (mixed over
                 --steps, FP64 over a shorter run), ns/day of both, force error.
+  cmd           learned centroid correction: constrained-PIMD training data
+                (216 waters, P = 32), training on the tensor cores, held-out
+                error; surrogate CMD of 4096 waters (L = 49.7 A) against plain
+                P = 32 PIMD centroid sampling, and the surrogate's error against
+                fresh constrained-PIMD samples of that system.
   replicas48    48 independent replicas, N from {64, 128, 216, 343, 512},
                 P from {8, 16, 32}, T uniform in [250, 350] K (seeded choice),
                 Trotter + PILE-G, mixed: all replicas in one context (one
@@ -224,6 +229,94 @@ def replicas48(steps=200, seed=48, warm=10):
             "launches_per_step": launches_per_step}
 
 
+def cmd(n_configs=4096, constrained_steps=2000, replicas=64, fit_steps=2000, deploy_mols=4096, deploy_beads=32,
+        fresh_configs=2, fresh_steps=1000, timing_steps=50, seed=5, train_mols=216, train_beads=32, held_out=256):
+    """Learned centroid correction: training data from constrained PIMD of
+    train_mols waters (train_beads beads), training on the tensor cores, held-out
+    error; then surrogate CMD of deploy_mols waters against plain PIMD centroid
+    sampling (deploy_beads beads), and the surrogate's centroid-force error
+    judged against fresh constrained-PIMD samples of the deployed system."""
+    from . import surrogate as sg
+    from .start import spread_beads
+
+    rep = {"workload": "cmd", "train": {"n_mols": train_mols, "n_beads": train_beads, "configs": n_configs,
+                                        "constrained_steps": constrained_steps, "replicas": replicas,
+                                        "fit_steps": fit_steps}}
+    t0 = time.perf_counter()
+    ds = sg.generate(n_mols=train_mols, n_beads=train_beads, n_configs=n_configs, replicas=replicas,
+                     equil_steps=2000, sample_every=200, constrained_steps=constrained_steps, seed=seed)
+    rep["train"]["generate_s"] = time.perf_counter() - t0
+    n_ho = min(held_out, max(1, n_configs // 8))
+    train, test = ds.split(n_configs - n_ho)
+    X, T = sg.features(train)
+    model = sg.Correction(seed=seed)
+    t0 = time.perf_counter()
+    rep["train"]["final_loss"] = model.fit(X, T, steps=fit_steps)
+    rep["train"]["fit_s"] = time.perf_counter() - t0
+    rep["train"]["rows"] = int(len(X))
+    rep["train"]["fit_ms_per_step"] = rep["train"]["fit_s"] / fit_steps * 1e3
+    rep["held_out"] = model.evaluate(test)
+    rep["held_out"]["on"] = f"{len(test)} configurations of {train_mols} waters not used in training"
+
+    # deployment: surrogate CMD (P = 1 + correction) against plain PIMD centroid sampling
+    st = seeded_start(deploy_mols, deploy_beads, 298.0, seed=seed + 7)
+    box = st.box_bohr
+    cents = st.q.reshape(deploy_beads, -1).mean(axis=0)
+    c_ctx = Context([system_desc(deploy_mols, 1, box, dt_fs=0.25, propagator=TROTTER, thermostat=PILE_L,
+                                 seed=seed)], MIXED)
+    cs = c_ctx.systems[0]
+    cs.set_state(cents)
+    model.attach(cs)
+    c_ctx.init_forces()
+    c_ctx.run_steps(2000, is_nvt=True)  # equilibrate the centroids with the surrogate
+    c_ctx.sync()
+    t0 = time.perf_counter()
+    c_ctx.run_steps(timing_steps * 10, is_nvt=True)
+    c_ctx.sync()
+    t_cmd = (time.perf_counter() - t0) / (timing_steps * 10)
+    snaps = []
+    for k in range(fresh_configs):
+        c_ctx.run_steps(400, is_nvt=True)
+        c_ctx.sync()
+        snaps.append(cs.get_state()["q"].copy())
+    c_ctx.close()
+    p_ctx = Context([system_desc(deploy_mols, deploy_beads, box, dt_fs=0.25, propagator=TROTTER, thermostat=PILE_G,
+                                 seed=seed)], MIXED)
+    ps = p_ctx.systems[0]
+    ps.set_state(st.q, st.p)
+    p_ctx.init_forces()
+    p_ctx.run_steps(5, is_nvt=True)
+    p_ctx.sync()
+    t0 = time.perf_counter()
+    p_ctx.run_steps(timing_steps, is_nvt=True)
+    p_ctx.sync()
+    t_pimd = (time.perf_counter() - t0) / timing_steps
+    # fresh constrained-PIMD mean centroid forces at the surrogate-CMD centroids
+    fmean, fclass = [], []
+    for k, c in enumerate(snaps):
+        q, p = spread_beads(c, deploy_beads, 298.0, seed=seed * 100 + k)
+        ps.set_state(q, p)
+        ps.set_centroid_fixed(True)
+        p_ctx.init_forces()
+        p_ctx.run_steps(200, is_nvt=True)  # internal modes relax around the fixed centroid
+        ps.reset_centroid_force()
+        p_ctx.run_steps(fresh_steps, is_nvt=True)
+        p_ctx.sync()
+        f, n = ps.centroid_force()
+        fmean.append(f)
+        ps.set_centroid_fixed(False)
+    p_ctx.close()
+    snaps, fmean = np.array(snaps), np.array(fmean)
+    fclass = sg.classical_forces(snaps, deploy_mols, box)
+    fresh = sg.Dataset(deploy_mols, box, snaps, fmean, fclass, {})
+    rep["deploy"] = {"n_mols": deploy_mols, "box_angstrom": float(box[0] * 0.529177210903),
+                     "surrogate_cmd_ms_per_step": t_cmd * 1e3, "surrogate_cmd_ns_day": ns_per_day(t_cmd, 0.25),
+                     "pimd_ms_per_step": t_pimd * 1e3, "pimd_beads": deploy_beads,
+                     "pimd_ns_day": ns_per_day(t_pimd, 0.25), "speedup_over_pimd": t_pimd / t_cmd,
+                     "fresh_constrained_pimd": dict(model.evaluate(fresh), steps=fresh_steps, beads=deploy_beads)}
+    return rep
+
+
 def headline(steps=200, seed=2024):
     st = seeded_start(512, 32, 298.0, seed=seed)
     d = system_desc(512, 32, st.box_bohr, dt_fs=0.25, propagator=TROTTER, thermostat=PILE_G, seed=seed)
@@ -239,7 +332,7 @@ def headline(steps=200, seed=2024):
 
 
 WORKLOADS = {"headline": headline, "classical216": classical216, "trotter216": trotter216, "sc512": sc512,
-             "replicas48": replicas48}
+             "replicas48": replicas48, "cmd": cmd}
 
 
 def main(argv=None):
@@ -247,8 +340,13 @@ def main(argv=None):
     ap.add_argument("name", choices=sorted(WORKLOADS))
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--seed", type=int, default=None)
+    ap.add_argument("--arg", action="append", default=[], metavar="KEY=VALUE",
+                    help="any other keyword of the workload function (numbers)")
     a = ap.parse_args(argv)
     kw = {}
+    for item in a.arg:
+        k, v = item.split("=", 1)
+        kw[k] = float(v) if any(ch in v for ch in ".e") else int(v)
     if a.steps is not None:
         kw["steps"] = a.steps
     if a.seed is not None:

@@ -43,7 +43,8 @@ def test_autotuned_shapes_keep_the_forces(gpu_lib, precision, tol):
         if tuned:
             t_heur, t_best = ctx.autotune(3)
             assert 0.0 < t_best <= t_heur
-            assert all(0 <= c <= 8 for c in ctx.tuning())
+            n_rj, n_sc, n_kc = ctx.tuning()
+            assert 0 <= n_rj <= 16 and 0 <= n_sc <= 32 and 0 <= n_kc <= 16
         ctx.init_forces()
         forces.append(ctx.systems[0].get_state()["fphys"])
         ctx.close()
@@ -59,7 +60,7 @@ def test_fixed_tuning_is_checked_and_used(gpu_lib):
     ctx = q.Context([q.system_desc(64, 4, st.box_bohr, propagator=q.TROTTER)], q.MIXED)
     ctx.systems[0].set_state(st.q, st.p)
     with pytest.raises(q.QtgError):
-        ctx.set_tuning(9, 1, 1)
+        ctx.set_tuning(17, 1, 1)
     ctx.set_tuning(1, 8, 3)
     assert ctx.tuning() == (1, 8, 3)
     ctx.init_forces()
