@@ -279,6 +279,13 @@ qtg_status qtg_detach_surrogate(qtg_ctx *ctx, int sys);
  * wait ran out), clearing them when `clear` is set. */
 qtg_status qtg_surrogate_status(unsigned *bits, int clear);
 
+/* Bytes the context has copied host -> device and device -> host since it was
+ * created (every entry that takes host arrays counts what it moves). The
+ * per-call steps skip what is provably unchanged: masses and charges equal to
+ * the last ones uploaded, and the Verlet list on the way back unless the skin
+ * test rebuilt it during the call (no reference counterpart). */
+qtg_status qtg_transfer_bytes(qtg_ctx *ctx, unsigned long long *h2d, unsigned long long *d2h);
+
 /* ---- launch-shape autotuner (no reference counterpart) ---------------------- */
 /* The three dominant force kernels split their work into chunks whose counts
  * set the grid sizes: real-space j-chunks (k_real, 1..16), structure-factor

@@ -106,6 +106,7 @@ def load(build_if_missing: bool = True):
         "qtg_time_kernel": ([V, C.c_char_p, C.c_int, D], C.c_int),
         "qtg_fp32_peak": ([D], C.c_int),
         "qtg_autotune": ([V, C.c_int, D, D], C.c_int),
+        "qtg_transfer_bytes": ([V, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], C.c_int),
         "qtg_sym_descriptors": ([V, C.c_int, C.c_int, D, V, V], C.c_int),
         "qtg_mlp_forward": ([C.POINTER(MlpWeights), V, C.c_int, V, V], C.c_int),
         "qtg_surrogate_status": ([C.POINTER(C.c_uint), C.c_int], C.c_int),
@@ -183,6 +184,12 @@ class Context:
 
     def init_forces(self):
         self.check(self.L.qtg_init_forces(self.h))
+
+    def transfer_bytes(self):
+        """(host -> device, device -> host) bytes moved by this context so far."""
+        a, b = C.c_uint64(0), C.c_uint64(0)
+        self.check(self.L.qtg_transfer_bytes(self.h, C.byref(a), C.byref(b)))
+        return int(a.value), int(b.value)
 
     def autotune(self, iters=10):
         """Pick the chunk counts of k_real / k_ksk / k_kforce for this batch

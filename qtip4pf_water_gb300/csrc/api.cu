@@ -257,6 +257,8 @@ struct qtg_ctx {
     };
     std::vector<Surrogate> surrogates;
     int n_sm = 148;
+    unsigned long long h2d_bytes = 0, d2h_bytes = 0;  // host <-> device traffic of the per-call entries
+    std::vector<std::vector<double>> last_mass, last_charge;  // per system: the arrays last uploaded
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     unsigned long long graph_kernels[2] = {0, 0};
     unsigned long long launches = 0;
@@ -425,6 +427,7 @@ ListArgs list_args(qtg_ctx *c, int first_job, int n_jobs, int force) {
     l.point_full = c->point_full;
     l.list_full = c->list_full;
     l.acc = c->acc;
+    l.run = c->run;
     l.status = c->status;
     l.force_rebuild = force;
     l.max_mols = c->max_mols;
@@ -557,9 +560,11 @@ qtg_status sync_status(qtg_ctx *ctx) {
     } while (0)
 
 cudaError_t up(qtg_ctx *c, void *dst, const void *src, size_t bytes) {
+    c->h2d_bytes += bytes;
     return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
 }
 cudaError_t down(qtg_ctx *c, void *dst, const void *src, size_t bytes) {
+    c->d2h_bytes += bytes;
     return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
 }
 
@@ -571,6 +576,11 @@ qtg_status refresh_sys(qtg_ctx *ctx, int sys) {
 // masses, their inverses and square roots (the kernels multiply instead of dividing)
 qtg_status upload_masses(qtg_ctx *ctx, int sys, const double *mass) {
     const SysDev &S = ctx->sys_h[sys];
+    if (ctx->last_mass.size() != ctx->sys_h.size()) ctx->last_mass.resize(ctx->sys_h.size());
+    std::vector<double> &last = ctx->last_mass[sys];
+    if (last.size() == (size_t)S.n_dof && memcmp(last.data(), mass, sizeof(double) * S.n_dof) == 0) return QTG_OK;
+    last.assign(mass, mass + S.n_dof);
+    ctx->h2d_bytes += 2 * sizeof(double) * S.n_dof;  // 1/m and sqrt(m)
     std::vector<double> im(S.n_dof), sm(S.n_dof);
     for (int k = 0; k < S.n_dof; ++k) {
         im[k] = 1.0 / mass[k];
@@ -587,6 +597,11 @@ qtg_status upload_masses(qtg_ctx *ctx, int sys, const double *mass) {
 
 qtg_status upload_charges(qtg_ctx *ctx, int sys, const double *charge) {
     SysDev &S = ctx->sys_h[sys];
+    if (ctx->last_charge.size() != ctx->sys_h.size()) ctx->last_charge.resize(ctx->sys_h.size());
+    std::vector<double> &last = ctx->last_charge[sys];
+    if (last.size() == (size_t)S.n_sites && memcmp(last.data(), charge, sizeof(double) * S.n_sites) == 0)
+        return QTG_OK;
+    last.assign(charge, charge + S.n_sites);
     double self = 0.0;
     for (int i = 0; i < S.n_sites; ++i) self += 0.5 * S.ewald_pref * charge[i] * charge[i];
     S.self_energy = self;
@@ -1038,7 +1053,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         for (auto &r : runs) {
             r.heat = 0.0;
             r.alpha = 1.0;
-            r.cf_samples = r.pad = 0.0;
+            r.cf_samples = r.list_builds = 0.0;
         }
         cp(ctx->run, runs.data(), sizeof(SysRun) * n_systems);
         if (e == cudaSuccess) e = cudaMemset(ctx->cf_acc, 0, sizeof(double) * ctx->n_cf);
@@ -1450,7 +1465,21 @@ static qtg_status download_dynamic(qtg_ctx *ctx, int sys, double *q, double *p, 
     if (fphys) CK(down(ctx, fphys, ctx->fphys + S.q_off, sizeof(double) * nt));
     CK(down(ctx, disp, ctx->disp + S.d_off, sizeof(double) * S.n_beads * 3 * S.n_mols));
     CK(down(ctx, point, ctx->point + S.pt_off, sizeof(int) * S.n_beads * S.n_mols));
+    if (list) CK(down(ctx, list, ctx->list + S.ls_off, sizeof(int) * (size_t)S.n_beads * S.list_size));
+    return QTG_OK;
+}
+
+// The list entries of a per-call step go back to the caller only when the skin
+// test rebuilt a list during the call: otherwise the device copy is the one the
+// call uploaded, which the caller's array already holds (the reference's
+// neighbour_list likewise writes the list only when it rebuilds).
+// builds0 / builds1: the system's rebuild count read (asynchronously) before and
+// after the step, both resolved by the time this runs.
+static qtg_status download_list_if_rebuilt(qtg_ctx *ctx, int sys, int *list, double builds0, double builds1) {
+    const SysDev &S = ctx->sys_h[sys];
+    if (builds1 == builds0) return QTG_OK;
     CK(down(ctx, list, ctx->list + S.ls_off, sizeof(int) * (size_t)S.n_beads * S.list_size));
+    CK(cudaStreamSynchronize(ctx->stream));
     return QTG_OK;
 }
 
@@ -1460,6 +1489,8 @@ qtg_status qtg_update_class(qtg_ctx *ctx, int sys, double *q, double *p, const d
     const SysDev &S = ctx->sys_h[sys];
     if (S.n_beads != 1 || !q || !p || !f || !point || !list || !disp) return fail(ctx, QTG_ERR_ARG, "bad argument");
     CKS(upload_dynamic(ctx, sys, q, p, mass, f, nullptr, charge, point, list, disp));
+    double builds0 = 0.0, builds = 0.0;
+    CK(down(ctx, &builds0, &ctx->run[sys].list_builds, sizeof(double)));
     CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
     launch_ring(ring_args(ctx, sys, RF_KICK | RF_VV | RF_DISP), ctx->stream, &ctx->launches);
     launch_skin_rebuild(list_args(ctx, S.job_base, 1, 0), ctx->stream, &ctx->launches);
@@ -1470,10 +1501,12 @@ qtg_status qtg_update_class(qtg_ctx *ctx, int sys, double *q, double *p, const d
     RingArgs e = ring_args(ctx, sys, 0);
     e.kick = 1;
     launch_end_step(e, ctx->stream, &ctx->launches);
-    CKS(download_dynamic(ctx, sys, q, p, f, nullptr, point, list, disp));
+    CKS(download_dynamic(ctx, sys, q, p, f, nullptr, point, nullptr, disp));
     double en = 0.0;
     CK(down(ctx, &en, ctx->energy + S.job_base, sizeof(double)));
+    CK(down(ctx, &builds, &ctx->run[sys].list_builds, sizeof(double)));
     CKS(sync_status(ctx));
+    CKS(download_list_if_rebuilt(ctx, sys, list, builds0, builds));
     CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
     if (energy) *energy = en;
     return sync_status(ctx);
@@ -1486,6 +1519,8 @@ qtg_status qtg_update_pimd(qtg_ctx *ctx, int sys, double *q, double *p, const do
     const SysDev &S = ctx->sys_h[sys];
     if (!q || !p || !f || !fphys || !point || !list || !disp) return fail(ctx, QTG_ERR_ARG, "bad argument");
     CKS(upload_dynamic(ctx, sys, q, p, mass, f, fphys, charge, point, list, disp));
+    double builds0 = 0.0, builds = 0.0;
+    CK(down(ctx, &builds0, &ctx->run[sys].list_builds, sizeof(double)));
     if (noise) CK(up(ctx, ctx->noise, noise, sizeof(double) * (2 + (size_t)(S.n_beads - 1) * S.n_dof)));
     const double h0 = heat ? *heat : 0.0;
     CK(up(ctx, &ctx->run[sys].heat, &h0, sizeof(double)));
@@ -1510,11 +1545,13 @@ qtg_status qtg_update_pimd(qtg_ctx *ctx, int sys, double *q, double *p, const do
     RingArgs e = ring_args(ctx, sys, 0);
     e.kick = 1;
     launch_end_step(e, ctx->stream, &ctx->launches);
-    CKS(download_dynamic(ctx, sys, q, p, f, fphys, point, list, disp));
+    CKS(download_dynamic(ctx, sys, q, p, f, fphys, point, nullptr, disp));
     double h = 0.0;
     CK(down(ctx, &h, &ctx->run[sys].heat, sizeof(double)));
+    CK(down(ctx, &builds, &ctx->run[sys].list_builds, sizeof(double)));
     double vs, ve, extra;
-    CKS(read_energies(ctx, sys, &vs, &ve, &extra));
+    CKS(read_energies(ctx, sys, &vs, &ve, &extra));  // synchronises
+    CKS(download_list_if_rebuilt(ctx, sys, list, builds0, builds));
     if (heat) *heat = h;
     if (S.propagator == QTG_SUZUKI_CHIN) {
         if (pot) *pot = 2.0 * ve / S.n_beads;
@@ -1668,6 +1705,13 @@ qtg_status qtg_get_tuning(qtg_ctx *ctx, int *n_rj, int *n_sc, int *n_kc) {
     *n_rj = ctx->tune[0];
     *n_sc = ctx->tune[1];
     *n_kc = ctx->tune[2];
+    return QTG_OK;
+}
+
+qtg_status qtg_transfer_bytes(qtg_ctx *ctx, unsigned long long *h2d, unsigned long long *d2h) {
+    if (!ctx || !h2d || !d2h) return QTG_ERR_ARG;
+    *h2d = ctx->h2d_bytes;
+    *d2h = ctx->d2h_bytes;
     return QTG_OK;
 }
 

@@ -383,6 +383,123 @@ __global__ void __launch_bounds__(RT) k_real_f32(EvalArgs a) {
     if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
 }
 
+// Half-interaction form of k_real_f32 (energies and forces, beads of at most
+// HALF_MAX_TILES tiles of 32 sites): every site pair is evaluated once. A warp
+// holds tile J of a bead in registers (one site a lane) and visits the tiles at
+// ring distances d = 1 .. T/2 from it (distance T/2 of an even ring only from
+// the first half of the tiles); the visited tile's sites and their force
+// accumulators rotate through the lanes by shuffles, 32 steps bringing them
+// back home. The stationary tile's own pairs (d = 0) are taken from both sides.
+// Forces are written as partial planes, deterministic: plane `ch` holds the
+// stationary-side sums of chunk ch of the distances, plane n_ch + d - 1 the
+// visited-side sums of distance d (zero where that visit is not made).
+constexpr int HW = 4;  // warps per block
+__global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ch = blockIdx.y, jb = blockIdx.z;
+    const Job J = a.jobs[jb];
+    const SysDev &S = a.sys[J.sys];
+    const int ns = S.n_sites, T = (ns + 31) / 32;
+    const int tJ = blockIdx.x * HW + warp;
+    if (tJ >= T) return;
+    const int maxd = T / 2;
+    const int d0 = chunk_lo(maxd + 1, ch, n_ch), d1 = chunk_lo(maxd + 1, ch + 1, n_ch);
+    const float4 *sites = reinterpret_cast<const float4 *>(a.sites) + J.site_off;
+    const float L0 = S.boxf[0], L1 = S.boxf[1], L2 = S.boxf[2];
+    const float I0 = S.inv_boxf[0], I1 = S.inv_boxf[1], I2 = S.inv_boxf[2];
+    const float rc2 = (float)S.rc_sq, ka = (float)(0.3275911 * S.kappa);
+    const float cex = (float)(-S.kappa * S.kappa * 1.4426950408889634), pref = (float)S.ewald_pref;
+    const int s = tJ * 32 + lane, ms = s / 3;
+    const bool vs = s < ns;
+    float4 ps = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (vs) ps = sites[s];
+    // w = q_s q_m (A + B) / r^2 along d = r_s - r_m; returns q_s q_m A (the pair energy)
+    auto pair = [&](const float4 &pm, float &dx, float &dy, float &dz, float &w) -> float {
+        dx = ps.x - pm.x;
+        dy = ps.y - pm.y;
+        dz = ps.z - pm.z;
+        dx = fmaf(-L0, rintf(dx * I0), dx);
+        dy = fmaf(-L1, rintf(dy * I1), dy);
+        dz = fmaf(-L2, rintf(dz * I2), dz);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        w = 0.f;
+        if (!(r2 < rc2)) return 0.f;
+        const float iv = rsqrt_approx(r2);
+        const float ex = ex2_approx(cex * r2);
+        const float t = rcp_approx(fmaf(ka, r2 * iv, 1.0f));
+        const float A = (t * as_poly(t)) * ex * iv;
+        const float qq = ps.w * pm.w;
+        w = qq * fmaf(pref, ex, A) * (iv * iv);
+        return qq * A;
+    };
+    float Sx = 0.f, Sy = 0.f, Sz = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f, e = 0.f;
+    const size_t ts = (size_t)a.total_sites;
+    for (int d = d0; d < d1; ++d) {
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        if (d == 0) {  // the tile's own pairs, from both sides
+            for (int r = 1; r < 32; ++r) {
+                const int src = (lane + r) & 31;
+                float4 pm;
+                pm.x = __shfl_sync(0xffffffffu, ps.x, src);
+                pm.y = __shfl_sync(0xffffffffu, ps.y, src);
+                pm.z = __shfl_sync(0xffffffffu, ps.z, src);
+                pm.w = __shfl_sync(0xffffffffu, ps.w, src);
+                const int m = tJ * 32 + src;
+                if (!vs || m >= ns || m / 3 == ms) continue;
+                float dx, dy, dz, w;
+                e += 0.5f * pair(pm, dx, dy, dz, w);
+                fx = fmaf(w, dx, fx);
+                fy = fmaf(w, dy, fy);
+                fz = fmaf(w, dz, fz);
+            }
+        } else {
+            const int tI = (tJ + d) % T;
+            const bool active = !((T % 2 == 0) && d == maxd && tJ >= maxd);
+            const int m0 = tI * 32;
+            float4 pm = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (active && m0 + lane < ns) pm = sites[m0 + lane];
+            float mx = 0.f, my = 0.f, mz = 0.f;
+            if (active) {
+                for (int r = 0; r < 32; ++r) {
+                    const int m = m0 + ((lane + r) & 31);
+                    if (vs && m < ns && m / 3 != ms) {
+                        float dx, dy, dz, w;
+                        e += pair(pm, dx, dy, dz, w);
+                        fx = fmaf(w, dx, fx);
+                        fy = fmaf(w, dy, fy);
+                        fz = fmaf(w, dz, fz);
+                        mx = fmaf(-w, dx, mx);
+                        my = fmaf(-w, dy, my);
+                        mz = fmaf(-w, dz, mz);
+                    }
+                    // hand the visited site and its force one lane down
+                    const int nx = (lane + 1) & 31;
+                    pm.x = __shfl_sync(0xffffffffu, pm.x, nx);
+                    pm.y = __shfl_sync(0xffffffffu, pm.y, nx);
+                    pm.z = __shfl_sync(0xffffffffu, pm.z, nx);
+                    pm.w = __shfl_sync(0xffffffffu, pm.w, nx);
+                    mx = __shfl_sync(0xffffffffu, mx, nx);
+                    my = __shfl_sync(0xffffffffu, my, nx);
+                    mz = __shfl_sync(0xffffffffu, mz, nx);
+                }
+            }
+            if (m0 + lane < ns)
+                store_plane<float>(a.part, 3 * ((size_t)(n_ch + d - 1) * ts + J.site_off + m0 + lane), mx, my, mz);
+        }
+        kahan_add(Sx, Cx, fx);
+        kahan_add(Sy, Cy, fy);
+        kahan_add(Sz, Cz, fz);
+    }
+    if (vs) store_plane<float>(a.part, 3 * ((size_t)ch * ts + J.site_off + s), Sx - Cx, Sy - Cy, Sz - Cz);
+    // a bead with fewer tiles than the largest of the batch: its sites get zero
+    // planes for the distances it does not have
+    if (ch == 0 && vs)
+        for (int d = maxd + 1; d <= a.n_rj - n_ch; ++d)
+            store_plane<float>(a.part, 3 * ((size_t)(n_ch + d - 1) * ts + J.site_off + s), 0.f, 0.f, 0.f);
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+    if (lane == 0) atomicAdd(&a.energy[J.slot], (double)e);
+}
+
 // ---- k_ksk: structure factors ---------------------------------------------------
 // One thread per group of <= 4 consecutive |kz| of one (kx, ky) column, each
 // |kz| covering the pair kz = +|kz|, -|kz|; the column factor X(kx) Y(ky) of a
@@ -1288,6 +1405,21 @@ void launch_lj_dense(const EvalArgs &a, cudaStream_t s) {
     else k_lj_dense<32><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
 }
 
+// The half-interaction real-space kernel applies to beads of at most
+// HALF_MAX_TILES tiles; its plane count is n_ch + T / 2 (n_ch from the
+// autotuner's real-space count, else sized for ~12 warps' blocks per SM).
+bool half_ok(const EvalArgs &a) { return (3 * a.max_mols + 31) / 32 <= HALF_MAX_TILES; }
+int half_chunks(const EvalArgs &a) {
+    const int T = (3 * a.max_mols + 31) / 32;
+    const long long blocks = (long long)((T + HW - 1) / HW) * a.n_jobs;
+    return chunks_or(a.tune_rj, blocks, HALF_MAX_CH);
+}
+void launch_real_half(EvalArgs &a, cudaStream_t s) {
+    const int T = (3 * a.max_mols + 31) / 32, n_ch = half_chunks(a);
+    a.n_rj = n_ch + T / 2;  // the planes the combine sums
+    k_real_half<<<dim3((T + HW - 1) / HW, n_ch, a.n_jobs), 32 * HW, 0, s>>>(a, n_ch);
+}
+
 template <typename R>
 void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n) {
     const int ns = 3 * a.max_mols;
@@ -1297,7 +1429,8 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n) {
     a.n_kc = chunks_or(a.tune_kc, (long long)tiles * a.n_jobs, MAX_KC);
     k_prep<R><<<dim3((ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
     if (a.mode == 0) {
-        if (sizeof(R) == 4) k_real_f32<<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
+        if (sizeof(R) == 4 && half_ok(a)) launch_real_half(a, s);
+        else if (sizeof(R) == 4) k_real_f32<<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         else k_real<R, 0><<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         k_ksk<R, 0><<<dim3(ktiles, a.n_sc, a.n_jobs), KT, ksk_smem<R>(a.max_kmax), s>>>(a);
         k_sk_reduce<R, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
@@ -1342,7 +1475,8 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
         if (mixed) k_prep<float><<<gs, 128, 0, s>>>(a);
         else k_prep<double><<<gs, 128, 0, s>>>(a);
     } else if (n == "real") {
-        if (mixed) k_real_f32<<<gr, RT, 0, s>>>(a);
+        if (mixed && half_ok(a)) launch_real_half(a, s);
+        else if (mixed) k_real_f32<<<gr, RT, 0, s>>>(a);
         else k_real<double, 0><<<gr, RT, 0, s>>>(a);
     } else if (n == "ksk") {
         if (mixed) k_ksk<float, 0><<<gk, KT, ksk_smem<float>(a.max_kmax), s>>>(a);

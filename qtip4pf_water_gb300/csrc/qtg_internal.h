@@ -108,7 +108,7 @@ struct SysRun {
     double heat;        // accumulated thermostat heat (update.cpp:325)
     double alpha;       // centroid rescale factor for the next O step (PILE-G)
     double cf_samples;  // steps accumulated into the mean centroid force
-    double pad;
+    double list_builds; // Verlet-list rebuilds of any bead since creation (never reset)
 };
 
 // Status word written by kernels (bit flags), read by the host after a sync.
@@ -305,7 +305,10 @@ void launch_nm_energy(const SysDev *sys, int sysi, int P, int n_dof, const doubl
 constexpr int MAX_RJ = 16;   // real-space j-chunks
 constexpr int MAX_KC = 16;   // reciprocal-space k-chunks
 constexpr int MAX_SC = 32;   // structure-factor site chunks
-constexpr int MAX_PART = MAX_RJ + MAX_KC + 1;  // partial site-force planes
+constexpr int HALF_MAX_TILES = 64;  // half-interaction real space: beads of at most 64 x 32 sites
+constexpr int HALF_MAX_CH = 8;      // its stationary-side chunks
+constexpr int MAX_RPLANES = HALF_MAX_CH + HALF_MAX_TILES / 2 > MAX_RJ ? HALF_MAX_CH + HALF_MAX_TILES / 2 : MAX_RJ;
+constexpr int MAX_PART = MAX_RPLANES + MAX_KC + 1;  // partial site-force planes
 
 struct EvalArgs {
     const SysDev *sys;     // device array
@@ -391,6 +394,7 @@ struct ListArgs {
     int *point, *list;
     int *point_full, *list_full;  // may be null: only the half list is built
     SysAcc *acc;
+    SysRun *run;        // cumulative rebuild count per system (may be null)
     unsigned *status;
     int force_rebuild;  // 1: rebuild unconditionally (initial build / per-call API)
     int max_mols;

@@ -1,0 +1,57 @@
+"""Per-call stepping (the update_sc_nospline drop-in): the Verlet list goes back
+to the caller only when the skin test rebuilt it (and then whole, cleared past
+the new list as the reference clears it), masses and charges are uploaded only
+when they change, and the transfer counters see exactly that."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(q, N=64, P=4):
+    st = q.seeded_start(N, P, 298.0, seed=41)
+    s = q.System.create(N, P, st.box_bohr, precision=q.MIXED, propagator=q.TROTTER, thermostat=q.PILE_G, seed=41)
+    qq, pp = st.q.reshape(-1).copy(), st.p.reshape(-1).copy()
+    point, lst, disp = s.build_lists(qq)
+    f = np.zeros_like(qq)
+    s.force_eval_trotter(qq, f, s.charges(), point, lst)
+    return s, qq, pp, point, lst, disp, f, f.copy()
+
+
+def _used_mask(s, point):
+    P, N, cap = s.P, s.N, s.info.list_size
+    mask = np.zeros(P * cap, bool)
+    for b in range(P):
+        mask[b * cap: b * cap + point[b * N + N - 1]] = True
+    return mask
+
+
+def test_list_comes_back_only_after_a_rebuild(gpu_lib):
+    q = gpu_lib
+    s, qq, pp, point, lst, disp, f, fp = _setup(q)
+    mass, chg = s.masses(), s.charges()
+    used = _used_mask(s, point)
+    lst[~used] = -7  # entries past each bead's list: never read, and untouched without a rebuild
+    before = lst.copy()
+    h0 = s.ctx.transfer_bytes()
+    _, heat, _ = s.update_sc_nospline(qq, pp, mass, f, fp, chg, point, lst, disp, True, 0.0)
+    h1 = s.ctx.transfer_bytes()
+    assert np.array_equal(lst, before)  # no rebuild: untouched
+    assert h1[1] - h0[1] < lst.nbytes  # and the list was not downloaded
+    # a second call with the same masses and charges uploads neither
+    _, heat, _ = s.update_sc_nospline(qq, pp, mass, f, fp, chg, point, lst, disp, True, heat)
+    h2 = s.ctx.transfer_bytes()
+    assert (h2[0] - h1[0]) <= (h1[0] - h0[0])
+    # displacements beyond the skin force a rebuild on the next call
+    disp[:] = 0.0
+    disp[0::3] = 10.0  # |disp| = 10 bohr for every molecule: beyond any skin margin
+    _, heat, _ = s.update_sc_nospline(qq, pp, mass, f, fp, chg, point, lst, disp, True, heat)
+    h3 = s.ctx.transfer_bytes()
+    assert h3[1] - h2[1] >= lst.nbytes
+    ref_point, ref_list, _ = s.build_lists(qq)
+    assert np.array_equal(point, ref_point)
+    new_used = _used_mask(s, point)
+    assert np.array_equal(lst[new_used], ref_list[new_used])
+    # a rebuild clears the whole list first, as the reference's neighbour_list does
+    # (neighbour.cpp:23-25): past the new list the caller's array now reads zero
+    assert np.all(lst[~new_used] == 0)
