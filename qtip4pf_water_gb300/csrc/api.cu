@@ -258,6 +258,8 @@ struct qtg_ctx {
     std::vector<Surrogate> surrogates;
     int n_sm = 148;
     unsigned long long h2d_bytes = 0, d2h_bytes = 0;  // host <-> device traffic of the per-call entries
+    // per-call ring-polymer steps captured as graphs, by (system, NVT, caller noise): graph, kernels in it
+    std::map<int, std::pair<cudaGraphExec_t, unsigned long long>> call_graphs;
     std::vector<std::vector<double>> last_mass, last_charge;  // per system: the arrays last uploaded
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     unsigned long long graph_kernels[2] = {0, 0};
@@ -622,6 +624,8 @@ void drop_graphs(qtg_ctx *ctx) {
         ctx->graph[i] = nullptr;
         ctx->graph_kernels[i] = 0;
     }
+    for (auto &g : ctx->call_graphs) cudaGraphExecDestroy(g.second.first);
+    ctx->call_graphs.clear();
 }
 
 void free_surrogate(qtg_ctx::Surrogate &g) {
@@ -1083,6 +1087,7 @@ void qtg_destroy(qtg_ctx *ctx) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (auto &g : ctx->surrogates) free_surrogate(g);
+    for (auto &g : ctx->call_graphs) cudaGraphExecDestroy(g.second.first);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -1524,27 +1529,52 @@ qtg_status qtg_update_pimd(qtg_ctx *ctx, int sys, double *q, double *p, const do
     if (noise) CK(up(ctx, ctx->noise, noise, sizeof(double) * (2 + (size_t)(S.n_beads - 1) * S.n_dof)));
     const double h0 = heat ? *heat : 0.0;
     CK(up(ctx, &ctx->run[sys].heat, &h0, sizeof(double)));
-    CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
-    if (is_nvt) {
-        // centroid kinetic energy after the opening kick, then the centroid draw
+    // the step's device work (update.cpp:271-401), the same for every call of this
+    // (system, NVT, caller noise): captured once as a graph and replayed
+    auto step = [&]() -> cudaError_t {
+        cudaError_t err = cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream);
+        if (is_nvt) {
+            // centroid kinetic energy after the opening kick, then the centroid draw
+            RingArgs e = ring_args(ctx, sys, 0);
+            e.kick = 0;
+            launch_end_step(e, ctx->stream, &ctx->launches);
+            FinalizeArgs fa = fin_args(ctx, sys, 0, 1);
+            fa.pile_g = 1;
+            fa.noise = noise ? ctx->noise : nullptr;
+            launch_finalize(fa, ctx->stream, &ctx->launches);
+        }
+        RingArgs r = ring_args(ctx, sys, RF_KICK | RF_FWD | RF_CAYLEY | RF_BACK | RF_DISP | (is_nvt ? RF_THERMO : 0));
+        r.noise = noise ? ctx->noise : nullptr;
+        r.pile_g = 1;
+        launch_ring(r, ctx->stream, &ctx->launches);
+        launch_skin_rebuild(list_args(ctx, S.job_base, S.n_beads, 0), ctx->stream, &ctx->launches);
+        if (err == cudaSuccess) err = cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream);
+        enqueue_forces(ctx, sys, false);
         RingArgs e = ring_args(ctx, sys, 0);
-        e.kick = 0;
+        e.kick = 1;
         launch_end_step(e, ctx->stream, &ctx->launches);
-        FinalizeArgs fa = fin_args(ctx, sys, 0, 1);
-        fa.pile_g = 1;
-        fa.noise = noise ? ctx->noise : nullptr;
-        launch_finalize(fa, ctx->stream, &ctx->launches);
+        return err;
+    };
+    const int key = sys * 4 + (is_nvt ? 2 : 0) + (noise ? 1 : 0);
+    auto it = ctx->call_graphs.find(key);
+    if (it == ctx->call_graphs.end()) {
+        cudaGraph_t graph;
+        const unsigned long long before = ctx->launches;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        const cudaError_t se = step();
+        const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+        if (se != cudaSuccess || ce != cudaSuccess)
+            return fail(ctx, QTG_ERR_CUDA, std::string("step capture: ") + cudaGetErrorString(se != cudaSuccess ? se : ce));
+        const unsigned long long kernels = ctx->launches - before;
+        ctx->launches = before;
+        cudaGraphExec_t exec;
+        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return fail(ctx, QTG_ERR_CUDA, std::string("step graph: ") + cudaGetErrorString(ie));
+        it = ctx->call_graphs.emplace(key, std::make_pair(exec, kernels)).first;
     }
-    RingArgs r = ring_args(ctx, sys, RF_KICK | RF_FWD | RF_CAYLEY | RF_BACK | RF_DISP | (is_nvt ? RF_THERMO : 0));
-    r.noise = noise ? ctx->noise : nullptr;
-    r.pile_g = 1;
-    launch_ring(r, ctx->stream, &ctx->launches);
-    launch_skin_rebuild(list_args(ctx, S.job_base, S.n_beads, 0), ctx->stream, &ctx->launches);
-    CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
-    enqueue_forces(ctx, sys, false);
-    RingArgs e = ring_args(ctx, sys, 0);
-    e.kick = 1;
-    launch_end_step(e, ctx->stream, &ctx->launches);
+    CK(cudaGraphLaunch(it->second.first, ctx->stream));
+    ctx->launches += it->second.second;
     CKS(download_dynamic(ctx, sys, q, p, f, fphys, point, nullptr, disp));
     double h = 0.0;
     CK(down(ctx, &h, &ctx->run[sys].heat, sizeof(double)));
