@@ -53,6 +53,12 @@ Consts make_consts() {
     K.ktheta = 87.85 * kcal2au;
     K.qo = -1.1128;
     K.qh = -0.5 * K.qo;
+    K.ljf[0] = (float)K.sigmalj6;
+    K.ljf[1] = (float)K.sigmalj12;
+    K.ljf[2] = (float)(4.0 * K.epslj);
+    K.ljf[3] = (float)(24.0 * K.epslj);
+    K.ljf[4] = (float)K.e_cut;
+    K.ljf[5] = (float)K.r_cut_sq;
     return K;
 }
 
@@ -731,6 +737,12 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
             S.boxf[k] = (float)S.box[k];
             S.inv_boxf[k] = (float)S.inv_box[k];
         }
+        // two images of an O-O pair tied in dimension d are both L_d / 2 away in d: the
+        // tie can change the Lennard-Jones cutoff decision only when (L_d / 2)^2 is not
+        // clearly above r_cut^2
+        S.lj_tie_mask = 0;
+        for (int k = 0; k < 3; ++k)
+            if (0.25 * S.box[k] * S.box[k] < 1.001 * K.r_cut_sq) S.lj_tie_mask |= 1 << k;
         // water.cpp:76-157 with the box given directly
         S.beta = 1.0 / (K.K2au * d.temp_K);
         S.beta_n = S.beta / P;

@@ -636,7 +636,11 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
                     if (h == 1 && az == 0) continue;  // kz = 0 has one entry
                     const int kz = h ? -az : az;
                     const size_t at = (size_t)sc * a.total_k + J.sk_off + C.k_begin + (kz + C.m);
-                    a.skp[at] = make_double2((double)Sr[g][h] - (double)Cr[g][h], (double)Si[g][h] - (double)Ci[g][h]);
+                    if (sizeof(R) == 4 && MODE == 0)  // FP32 form: the compensated pair (S, C) itself
+                        reinterpret_cast<float4 *>(a.skp)[at] =
+                            make_float4((float)Sr[g][h], (float)Si[g][h], (float)Cr[g][h], (float)Ci[g][h]);
+                    else
+                        a.skp[at] = make_double2((double)Sr[g][h] - (double)Cr[g][h], (double)Si[g][h] - (double)Ci[g][h]);
                     if (MODE == 1)
                         a.dskp[at] = make_double2((double)dSr[g][h] - (double)dCr[g][h],
                                                   (double)dSi[g][h] - (double)dCi[g][h]);
@@ -661,6 +665,23 @@ __global__ void __launch_bounds__(128) k_sk_reduce(EvalArgs a) {
     if (k < S.n_kvec) {
         const double w = 2.0 * a.kvec[S.kvec_off + k].coef;
         double sr = 0.0, si = 0.0, dr = 0.0, di = 0.0;
+        if (sizeof(R) == 4 && MODE == 0) {
+            // FP32 form: the site chunks' compensated pairs (S, C), summed in chunk
+            // order with compensation in FP32; FP64 only for the energy
+            const float4 *pk = reinterpret_cast<const float4 *>(a.skp) + J.sk_off + k;
+            float xs = 0.f, xc = 0.f, ys = 0.f, yc = 0.f;
+            for (int sc = 0; sc < a.n_sc; ++sc) {
+                const float4 p = pk[(size_t)sc * a.total_k];
+                kahan_add(xs, xc, p.x - p.z);
+                kahan_add(ys, yc, p.y - p.w);
+            }
+            const float fr = xs - xc, fi = ys - yc, wf = (float)w;
+            e = 0.5 * w * ((double)fr * fr + (double)fi * fi);
+            V2<R> v;
+            v.x = (R)(wf * fr);
+            v.y = (R)(wf * fi);
+            reinterpret_cast<V2<R> *>(a.wsk)[J.sk_off + k] = v;
+        } else {
         for (int sc = 0; sc < a.n_sc; ++sc) {
             const size_t at = (size_t)sc * a.total_k + J.sk_off + k;
             const double2 p = a.skp[at];
@@ -683,6 +704,7 @@ __global__ void __launch_bounds__(128) k_sk_reduce(EvalArgs a) {
             v.x = (R)(w * dr);
             v.y = (R)(w * di);
             wd[k] = v;
+        }
         }
     }
     if (MODE == 0) {
@@ -1265,19 +1287,16 @@ __global__ void __launch_bounds__(128) k_lj_dense(EvalArgs a) {
         K.L[d] = S.boxf[d];
         K.I[d] = S.inv_boxf[d];
     }
-    K.rc2 = (float)rc2;
+    // FP32 constants and the tie mask come prepared from the host (no FP64 work per thread)
+    K.rc2 = C.ljf[5];
     K.band = 1e-5f * K.rc2;
     K.tie = 1e-5f;
-    K.s6 = (float)C.sigmalj6;
-    K.s12 = (float)C.sigmalj12;
-    K.eps4 = (float)(4.0 * C.epslj);
-    K.eps24 = (float)(24.0 * C.epslj);
-    K.ecut = (float)C.e_cut;
-    // two images of a pair tied in dimension d are both L_d / 2 away in d: the tie
-    // can change the cutoff decision only when (L_d / 2)^2 is not clearly above r_cut^2
-    K.tie_mask = 0;
-    for (int d = 0; d < 3; ++d)
-        if (0.25 * S.box[d] * S.box[d] < 1.001 * rc2) K.tie_mask |= 1 << d;
+    K.s6 = C.ljf[0];
+    K.s12 = C.ljf[1];
+    K.eps4 = C.ljf[2];
+    K.eps24 = C.ljf[3];
+    K.ecut = C.ljf[4];
+    K.tie_mask = S.lj_tie_mask;
     const float4 *opos = reinterpret_cast<const float4 *>(a.opos) + J.site_off / 3;
     float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
     if (act) oi = opos[i];

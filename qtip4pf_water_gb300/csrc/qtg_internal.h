@@ -18,6 +18,7 @@ struct Consts {
     double r_cut, r_cut_sq, r_skin, r_skin_sq;
     double gamma_vs, epslj, sigmalj6, sigmalj12, e_cut;
     double roheq, ar2, ar3, ar4fac, Dr, theta_eq, ktheta, qo, qh;
+    float ljf[6];  // FP32 Lennard-Jones constants: sigma^6, sigma^12, 4 eps, 24 eps, e_cut, r_cut^2
 };
 
 // Per-system constants (one per replica), resident in device memory.
@@ -27,6 +28,7 @@ struct SysDev {
     int n_kvec_ref;              // the reference's k-vector count (n_kvec includes c_k = 0 fillers)
     int col_off, n_col, grp_off, n_grp, batch_off, n_batch;
     int centroid_fixed;          // 1: the centroid is held fixed (centroid-constrained PIMD)
+    int lj_tie_mask;             // bit d: half of box side d lies within r_cut (a half-box tie can matter)
     long long nm_off;   // doubles: P x P bead->normal-mode matrix C (y = C x)
     long long mode_off; // ModeCoef entries: P per system
     long long q_off;    // doubles: system block [P][9N] in q/p/f/fphys/aux arrays
