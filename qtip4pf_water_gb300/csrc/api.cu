@@ -378,6 +378,7 @@ RingArgs ring_args(qtg_ctx *c, int sys, int flags) {
     r.kcv_all_beads = -1;
     r.max_p = c->max_p;
     r.cf_acc = c->cf_acc;
+    r.status = c->status;
     return r;
 }
 
@@ -526,6 +527,10 @@ void enqueue_step(qtg_ctx *c, int sys, int nvt, int ext_noise, bool pile_g) {
     RingArgs r = ring_args(c, sys, RF_KICK | RF_FWD | RF_CAYLEY | RF_BACK | RF_DISP | (nvt ? RF_THERMO : 0));
     r.noise = ext_noise ? c->noise : nullptr;
     r.pile_g = pile_g ? 1 : 0;
+    // the finalize below draws from (seed, system, step) only: its draws are made
+    // here by extra ring blocks, off the step's critical path
+    const bool ahead = nvt && sys < 0 && !ext_noise;
+    r.n_draw = ahead ? c->n_sys : 0;
     launch_ring(r, c->stream, &c->launches);
     const int jb = sys < 0 ? 0 : c->sys_h[sys].job_base;
     const int nj = sys < 0 ? (int)c->base.h.size() : c->sys_h[sys].n_beads;
@@ -537,6 +542,7 @@ void enqueue_step(qtg_ctx *c, int sys, int nvt, int ext_noise, bool pile_g) {
     FinalizeArgs fa = fin_args(c, sys, 1, nvt);
     fa.noise = nullptr;
     fa.pile_g = pile_g ? 1 : 0;
+    fa.pre_drawn = ahead ? 1 : 0;
     launch_finalize(fa, c->stream, &c->launches);
 }
 
@@ -1069,7 +1075,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         for (auto &r : runs) {
             r.heat = 0.0;
             r.alpha = 1.0;
-            r.cf_samples = r.list_builds = 0.0;
+            r.cf_samples = r.list_builds = r.R_draw = r.g2_draw = 0.0;
         }
         cp(ctx->run, runs.data(), sizeof(SysRun) * n_systems);
         if (e == cudaSuccess) e = cudaMemset(ctx->cf_acc, 0, sizeof(double) * ctx->n_cf);

@@ -32,8 +32,65 @@ __device__ __forceinline__ double normal_f32(const Philox4 &r) {
     return (double)(sqrtf(-2.0f * logf(u1)) * c);
 }
 
+// Gamma(shape) by Marsaglia & Tsang, "A simple method for generating gamma
+// variables" (ACM TOMS 26, 2000), for shape >= 1, with a bounded number of
+// candidates. Candidate `it` is drawn from Philox counters (2 it, 2 it + 1), so
+// the candidates are independent of one another: the 32 lanes of a warp test
+// 32 of them at once and the first accepted one (lowest `it`, found by ballot)
+// is the value the sequential loop would return. Called by a whole warp.
+__device__ double gamma_mt_warp(double shape, const SysDev &S, int sys, unsigned long long st, bool *ok) {
+    const int lane = threadIdx.x & 31;
+    const double d = shape - 1.0 / 3.0, cc = 1.0 / sqrt(9.0 * d);
+    uint32_t k0, k1;
+    philox_key(S, sys, RNG_GAMMA, &k0, &k1);
+    for (uint32_t base = 0; base < 64; base += 32) {
+        const uint32_t it = base + (uint32_t)lane;
+        const double x = normal2(philox4x32_10(2 * it, 0u, (uint32_t)st, (uint32_t)(st >> 32), k0, k1)).x;
+        double v = 1.0 + cc * x;
+        bool acc = false;
+        if (v > 0.0) {
+            v = v * v * v;
+            const Philox4 r = philox4x32_10(2 * it + 1, 0u, (uint32_t)st, (uint32_t)(st >> 32), k0, k1);
+            const double u = u01_from(r.v[0], r.v[1]);
+            acc = (u < 1.0 - 0.0331 * x * x * x * x) || (log(u) < 0.5 * x * x + d * (1.0 - v + log(v)));
+        }
+        const unsigned hit = __ballot_sync(0xffffffffu, acc);
+        if (hit) return __shfl_sync(0xffffffffu, d * v, __ffs(hit) - 1);
+    }
+    *ok = false;
+    return shape;
+}
+
+// The PILE-G centroid draws of a step (called by a whole warp): R ~ N(0, 1) and
+// g2 ~ chi^2 with (n_dof - 1) degrees of freedom -- both branches of
+// thermostat.cpp:102-110 draw exactly this distribution -- from Philox counters
+// of (seed, system, step), so they do not depend on where they are made.
+__device__ void centroid_draw(const SysDev &S, int sys, unsigned long long st, double *R, double *g2,
+                              unsigned *status) {
+    uint32_t k0, k1;
+    philox_key(S, sys, RNG_CENTROID, &k0, &k1);
+    *R = normal2(philox4x32_10(0u, 0u, (uint32_t)st, (uint32_t)(st >> 32), k0, k1)).x;
+    bool ok = true;
+    *g2 = 2.0 * gamma_mt_warp(0.5 * (S.n_dof - 1), S, sys, st, &ok);
+    if (!ok && (threadIdx.x & 31) == 0) atomicOr(status, (unsigned)ST_GAMMA_LIMIT);
+}
+
 __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
-    const ColWork W = a.work[blockIdx.x];
+    if ((int)blockIdx.x < a.n_draw) {
+        // draw blocks (the first ones, so that they start with the first wave): this
+        // step's PILE-G centroid draws, made while the ring work runs
+        const int sys = blockIdx.x;
+        const SysDev &S = a.sys[sys];
+        if (threadIdx.x >= 32 || !(S.thermostat == 1 || a.pile_g)) return;
+        double R, g2;
+        centroid_draw(S, sys, *a.step, &R, &g2, a.status);
+        if (threadIdx.x == 0) {
+            a.run[sys].R_draw = R;
+            a.run[sys].g2_draw = g2;
+        }
+        return;
+    }
+    const ColWork W = a.work[blockIdx.x - a.n_draw];
     const SysDev &S = a.sys[W.sys];
     const int P = S.n_beads, C = S.cols_per_block;
     const int k = threadIdx.x / C, c = threadIdx.x - k * C;
@@ -315,35 +372,6 @@ __global__ void k_centroid_ke(RingArgs a) {
     if (threadIdx.x == 0) atomicAdd(&a.acc[W.sys].k0, t);
 }
 
-// Gamma(shape) by Marsaglia & Tsang, "A simple method for generating gamma
-// variables" (ACM TOMS 26, 2000), for shape >= 1, with a bounded number of
-// candidates. Candidate `it` is drawn from Philox counters (2 it, 2 it + 1), so
-// the candidates are independent of one another: the 32 lanes of a warp test
-// 32 of them at once and the first accepted one (lowest `it`, found by ballot)
-// is the value the sequential loop would return. Called by a whole warp.
-__device__ double gamma_mt_warp(double shape, const SysDev &S, int sys, unsigned long long st, bool *ok) {
-    const int lane = threadIdx.x & 31;
-    const double d = shape - 1.0 / 3.0, cc = 1.0 / sqrt(9.0 * d);
-    uint32_t k0, k1;
-    philox_key(S, sys, RNG_GAMMA, &k0, &k1);
-    for (uint32_t base = 0; base < 64; base += 32) {
-        const uint32_t it = base + (uint32_t)lane;
-        const double x = normal2(philox4x32_10(2 * it, 0u, (uint32_t)st, (uint32_t)(st >> 32), k0, k1)).x;
-        double v = 1.0 + cc * x;
-        bool acc = false;
-        if (v > 0.0) {
-            v = v * v * v;
-            const Philox4 r = philox4x32_10(2 * it + 1, 0u, (uint32_t)st, (uint32_t)(st >> 32), k0, k1);
-            const double u = u01_from(r.v[0], r.v[1]);
-            acc = (u < 1.0 - 0.0331 * x * x * x * x) || (log(u) < 0.5 * x * x + d * (1.0 - v + log(v)));
-        }
-        const unsigned hit = __ballot_sync(0xffffffffu, acc);
-        if (hit) return __shfl_sync(0xffffffffu, d * v, __ffs(hit) - 1);
-    }
-    *ok = false;
-    return shape;
-}
-
 // One warp per system: the step's estimator record and the next centroid
 // draw for PILE-G. One block, so the step counters advance after every system.
 __global__ void k_finalize(FinalizeArgs a) {
@@ -390,15 +418,11 @@ __global__ void k_finalize(FinalizeArgs a) {
             if (a.noise && s == 0) {
                 R = a.noise[0];
                 g2 = a.noise[1];
+            } else if (a.pre_drawn) {
+                R = run->R_draw;
+                g2 = run->g2_draw;
             } else {
-                uint32_t k0, k1;
-                philox_key(S, s, RNG_CENTROID, &k0, &k1);
-                R = normal2(philox4x32_10(0u, 0u, (uint32_t)st, (uint32_t)(st >> 32), k0, k1)).x;
-                // g2 ~ chi^2 with (n_dof - 1) degrees of freedom: both branches of
-                // thermostat.cpp:102-110 draw exactly this distribution
-                bool ok = true;
-                g2 = 2.0 * gamma_mt_warp(0.5 * (S.n_dof - 1), S, s, st, &ok);
-                if (!ok && lane == 0) atomicOr(a.status, (unsigned)ST_GAMMA_LIMIT);
+                centroid_draw(S, s, st, &R, &g2, a.status);
             }
             if (lane == 0) run->alpha = sqrt((R * R + g2) / (2.0 * S.beta_n * ac->k0));
         }
@@ -538,7 +562,7 @@ void launch_ring(const RingArgs &a, cudaStream_t s, unsigned long long *n) {
     if (a.n_work <= 0) return;
     // shared memory: P^2 + 4 P C doubles, with P C <= 256
     size_t smem = (size_t)(a.max_p * a.max_p + 4 * 256) * sizeof(double);
-    k_ring<<<a.n_work, 256, smem, s>>>(a);
+    k_ring<<<a.n_work + a.n_draw, 256, smem, s>>>(a);
     if (n) ++*n;
 }
 

@@ -111,6 +111,7 @@ struct SysRun {
     double alpha;       // centroid rescale factor for the next O step (PILE-G)
     double cf_samples;  // steps accumulated into the mean centroid force
     double list_builds; // Verlet-list rebuilds of any bead since creation (never reset)
+    double R_draw, g2_draw;  // the step's PILE-G centroid draws, made ahead by k_ring's draw blocks
 };
 
 // Status word written by kernels (bit flags), read by the host after a sync.
@@ -244,6 +245,9 @@ struct RingArgs {
     int pile_g;              // 1: O step is PILE-G whatever the system's thermostat
     double *cf_acc;          // end step: sum over steps of the bead-averaged force, per dof
                              // (systems with a fixed centroid; indexed like mass)
+    unsigned *status;        // ring draw blocks: ST_GAMMA_LIMIT
+    int n_draw;              // ring: extra blocks that make the step's PILE-G centroid draws of
+                             // systems 0 .. n_draw-1 while the ring work runs (0: none)
 };
 
 struct FinalizeArgs {
@@ -262,6 +266,7 @@ struct FinalizeArgs {
     int draw_alpha;          // 1: draw the next PILE-G centroid factor
     int sys_begin, sys_end;  // systems handled
     int pile_g;              // 1: draw alpha whatever the system's thermostat
+    int pre_drawn;           // 1: this step's k_ring already made the centroid draws (SysRun)
 };
 
 struct ScArgs {
