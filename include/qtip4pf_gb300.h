@@ -135,14 +135,22 @@ qtg_status qtg_get_kcv(qtg_ctx *ctx, int sys, const double *q, const double *f, 
 qtg_status qtg_get_conserved(qtg_ctx *ctx, int sys, double *q, double *p, const double *mass,
                              double energy, double *out);
 /* update.cpp:78-137  double update_trajectory_class_nospline(q, p, mass, f, charge,
- *                                                           point, list, disp) */
+ *                                                           point, list, disp)
+ * Per-call steps (this and qtg_update_pimd): q, p, f and disp are read and written
+ * back; point and list are written back only for the beads whose lists the skin
+ * test rebuilt during the call, as the reference's neighbour_list writes them.
+ * In QTG_MIXED the Lennard-Jones term of the physical forces runs over every O-O
+ * pair inside r_cut (the pairs a valid Verlet list holds), so a mixed Trotter or
+ * classical step does not read the caller's point and list; QTG_FP64 steps and
+ * the Suzuki-Chin finite-difference terms read them as the reference does. */
 qtg_status qtg_update_class(qtg_ctx *ctx, int sys, double *q, double *p, const double *mass,
                             double *f, const double *charge, int *point, int *list, double *disp,
                             double *energy);
 /* update.cpp:271-401  double update_sc_nospline(q, p, mass, f, fphys, charge, point, list,
  *                                               disp, rng, is_nvt, heat, sc_pot)
  * The system's propagator decides the force assembly (SC or Trotter). noise as for
- * qtg_pile_g (NULL = counter-based generator). *heat is updated in place. */
+ * qtg_pile_g (NULL = counter-based generator). *heat is updated in place. fphys is
+ * output only: the reference's step overwrites it before reading it. */
 qtg_status qtg_update_pimd(qtg_ctx *ctx, int sys, double *q, double *p, const double *mass,
                            double *f, double *fphys, const double *charge, int *point,
                            int *list, double *disp, int is_nvt, const double *noise,

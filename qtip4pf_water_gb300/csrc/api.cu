@@ -210,6 +210,17 @@ struct qtg_ctx {
     // state
     double *q = nullptr, *p = nullptr, *f = nullptr, *fphys = nullptr, *disp = nullptr;
     int *point = nullptr, *list = nullptr, *point_full = nullptr, *list_full = nullptr;
+    int *rebuilt = nullptr;  // per base job: 1 after a rebuild of that bead's lists (per-call steps clear it)
+    // pinned mailbox of the per-call steps: the step's small results arrive here by
+    // asynchronous copies and resolve with one stream synchronisation
+    struct Mailbox {
+        double heat_in, heat_out;
+        SysAcc acc;
+        unsigned status;
+        int pad;
+    } *box = nullptr;
+    double *box_energy = nullptr;  // [max_p] per-bead energies of the step
+    int *box_rebuilt = nullptr;    // [max_p] per-bead rebuild flags of the step
     size_t total_point_full = 0, total_list_full = 0;
     double *charge = nullptr, *mass = nullptr, *inv_mass = nullptr, *sqrt_mass = nullptr;
     double *cf_acc = nullptr;  // mean-centroid-force sums of constrained systems, per dof (like mass)
@@ -437,6 +448,7 @@ ListArgs list_args(qtg_ctx *c, int first_job, int n_jobs, int force) {
     l.list_full = c->list_full;
     l.acc = c->acc;
     l.run = c->run;
+    l.rebuilt = c->rebuilt;
     l.status = c->status;
     l.force_rebuild = force;
     l.max_mols = c->max_mols;
@@ -450,10 +462,13 @@ void enqueue_forces(qtg_ctx *c, int sys, bool force_sc) {
     const int jb = sys < 0 ? 0 : c->sys_h[sys].job_base;
     const int nj = sys < 0 ? (int)c->base.h.size() : c->sys_h[sys].n_beads;
     // the device-resident stepper (sys < 0) maintains the symmetric lists itself;
-    // per-call entries work on the caller's half lists
+    // per-call entries work on the caller's half lists, except that the mixed
+    // evaluation of the physical forces takes the dense Lennard-Jones kernel as
+    // the stepper does (every O-O pair inside r_cut: the pairs a valid Verlet list
+    // holds). The Suzuki-Chin finite-difference terms stay FP64 and list-based.
     const int full = sys < 0 ? 1 : 0;
     EvalArgs base = eval_args(c, c->base.d + jb, nj, c->q, c->fphys, 0, 0);
-    base.lj_full = full;
+    base.lj_full = (full || c->mixed) ? 1 : 0;
     launch_eval(c, base);
     // learned centroid corrections of the systems that carry one (P = 1)
     for (const auto &g : c->surrogates) {
@@ -552,12 +567,9 @@ qtg_status check_sys(qtg_ctx *ctx, int sys) {
     return QTG_OK;
 }
 
-qtg_status sync_status(qtg_ctx *ctx) {
-    CK(cudaStreamSynchronize(ctx->stream));
-    unsigned st = 0;
-    CK(cudaMemcpy(&st, ctx->status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+// the error a nonzero device status word stands for
+qtg_status status_error(qtg_ctx *ctx, unsigned st) {
     if (st) {
-        CK(cudaMemset(ctx->status, 0, sizeof(unsigned)));
         if (st & ST_LIST_OVERFLOW) return fail(ctx, QTG_ERR_LIST_OVERFLOW, "Verlet list exceeded list_size");
         if (st & ST_NONFINITE) return fail(ctx, QTG_ERR_NONFINITE, "non-finite energy or force");
         if (st & ST_GAMMA_LIMIT) return fail(ctx, QTG_ERR_NONFINITE, "gamma variate iteration limit reached");
@@ -565,6 +577,14 @@ qtg_status sync_status(qtg_ctx *ctx) {
         if (st & ST_MMA_TIMEOUT) return fail(ctx, QTG_ERR_CUDA, "tensor-core completion wait ran out");
     }
     return QTG_OK;
+}
+
+qtg_status sync_status(qtg_ctx *ctx) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    unsigned st = 0;
+    CK(cudaMemcpy(&st, ctx->status, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (st) CK(cudaMemset(ctx->status, 0, sizeof(unsigned)));
+    return status_error(ctx, st);
 }
 
 #define CKS(expr)                            \
@@ -1018,6 +1038,18 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->energy, ctx->total_slots);
     AL(ctx->energy_aux, ctx->total_slots);
     AL(ctx->base.d, ctx->base.h.size());
+    AL(ctx->rebuilt, ctx->base.h.size());
+    if (e == cudaSuccess) {
+        void *pin = nullptr;
+        const size_t bytes = sizeof(qtg_ctx::Mailbox) + (sizeof(double) + sizeof(int)) * ctx->max_p;
+        e = cudaHostAlloc(&pin, bytes, cudaHostAllocDefault);
+        if (e == cudaSuccess) {
+            memset(pin, 0, bytes);
+            ctx->box = static_cast<qtg_ctx::Mailbox *>(pin);
+            ctx->box_energy = reinterpret_cast<double *>(ctx->box + 1);
+            ctx->box_rebuilt = reinterpret_cast<int *>(ctx->box_energy + ctx->max_p);
+        }
+    }
     AL(ctx->fd.d, ctx->fd.h.size());
     AL(ctx->tan.d, ctx->tan.h.size());
     AL(ctx->fd_sc.d, ctx->fd_sc.h.size());
@@ -1101,9 +1133,10 @@ void qtg_destroy(qtg_ctx *ctx) {
                     ctx->phase, ctx->opos, ctx->part, ctx->skp, ctx->dskp, ctx->wsk, ctx->wdsk, ctx->energy, ctx->energy_aux,
                     ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
-                    ctx->status, ctx->red_out};
+                    ctx->status, ctx->red_out, ctx->rebuilt};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    if (ctx->box) cudaFreeHost(ctx->box);
     for (auto &g : ctx->surrogates) free_surrogate(g);
     for (auto &g : ctx->call_graphs) cudaGraphExecDestroy(g.second.first);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -1463,9 +1496,19 @@ qtg_status qtg_get_conserved(qtg_ctx *ctx, int sys, double *q, double *p, const 
     return QTG_OK;
 }
 
+// Inputs of a per-call step. The physical forces are not among them: the
+// reference's step overwrites fphys whole before reading it (force_eval_sc_nospline,
+// forces.cpp:721, through get_forces_nospline, which zeroes its output at
+// forces.cpp:483). The caller's Verlet lists go up only when a kernel of the step
+// reads them (lists_read): the list-based Lennard-Jones of FP64 evaluations and of
+// the Suzuki-Chin finite-difference terms, not the dense kernel of a mixed
+// evaluation. A rebuild rewrites a bead's lists whole on the device either way.
+static bool step_reads_lists(const qtg_ctx *ctx, int sys) {
+    return !ctx->mixed || ctx->sys_h[sys].propagator == QTG_SUZUKI_CHIN;
+}
 static qtg_status upload_dynamic(qtg_ctx *ctx, int sys, const double *q, const double *p, const double *mass,
-                                 const double *f, const double *fphys, const double *charge, const int *point,
-                                 const int *list, const double *disp) {
+                                 const double *f, const double *charge, const int *point, const int *list,
+                                 const double *disp) {
     const SysDev &S = ctx->sys_h[sys];
     const size_t nt = (size_t)S.n_beads * S.n_dof;
     if (charge) CKS(upload_charges(ctx, sys, charge));
@@ -1473,8 +1516,8 @@ static qtg_status upload_dynamic(qtg_ctx *ctx, int sys, const double *q, const d
     CK(up(ctx, ctx->q + S.q_off, q, sizeof(double) * nt));
     CK(up(ctx, ctx->p + S.q_off, p, sizeof(double) * nt));
     CK(up(ctx, ctx->f + S.q_off, f, sizeof(double) * nt));
-    CK(up(ctx, ctx->fphys + S.q_off, fphys ? fphys : f, sizeof(double) * nt));
     CK(up(ctx, ctx->disp + S.d_off, disp, sizeof(double) * S.n_beads * 3 * S.n_mols));
+    if (!step_reads_lists(ctx, sys)) return QTG_OK;
     return upload_lists(ctx, sys, point, list, 0, S.n_beads);
 }
 
@@ -1487,23 +1530,57 @@ static qtg_status download_dynamic(qtg_ctx *ctx, int sys, double *q, double *p, 
     CK(down(ctx, f, ctx->f + S.q_off, sizeof(double) * nt));
     if (fphys) CK(down(ctx, fphys, ctx->fphys + S.q_off, sizeof(double) * nt));
     CK(down(ctx, disp, ctx->disp + S.d_off, sizeof(double) * S.n_beads * 3 * S.n_mols));
-    CK(down(ctx, point, ctx->point + S.pt_off, sizeof(int) * S.n_beads * S.n_mols));
+    if (point) CK(down(ctx, point, ctx->point + S.pt_off, sizeof(int) * S.n_beads * S.n_mols));
     if (list) CK(down(ctx, list, ctx->list + S.ls_off, sizeof(int) * (size_t)S.n_beads * S.list_size));
     return QTG_OK;
 }
 
-// The list entries of a per-call step go back to the caller only when the skin
-// test rebuilt a list during the call: otherwise the device copy is the one the
-// call uploaded, which the caller's array already holds (the reference's
-// neighbour_list likewise writes the list only when it rebuilds).
-// builds0 / builds1: the system's rebuild count read (asynchronously) before and
-// after the step, both resolved by the time this runs.
-static qtg_status download_list_if_rebuilt(qtg_ctx *ctx, int sys, int *list, double builds0, double builds1) {
+// The point and list arrays of a per-call step go back to the caller bead by
+// bead, for the beads whose skin test rebuilt them during the call (the
+// reference's neighbour_list writes a bead's point and list only when it
+// rebuilds them, update.cpp:380-383); the caller's arrays of the other beads stay
+// as they are. Reads the flags that the mailbox received before the stream was
+// last synchronised.
+static qtg_status download_rebuilt_lists(qtg_ctx *ctx, int sys, int *point, int *list) {
     const SysDev &S = ctx->sys_h[sys];
-    if (builds1 == builds0) return QTG_OK;
-    CK(down(ctx, list, ctx->list + S.ls_off, sizeof(int) * (size_t)S.n_beads * S.list_size));
-    CK(cudaStreamSynchronize(ctx->stream));
+    bool any = false;
+    for (int b = 0; b < S.n_beads; ++b) {
+        if (!ctx->box_rebuilt[b]) continue;
+        any = true;
+        CK(down(ctx, point + (size_t)b * S.n_mols, ctx->point + S.pt_off + (size_t)b * S.n_mols,
+                sizeof(int) * S.n_mols));
+        CK(down(ctx, list + (size_t)b * S.list_size, ctx->list + S.ls_off + (size_t)b * S.list_size,
+                sizeof(int) * S.list_size));
+    }
+    if (any) CK(cudaStreamSynchronize(ctx->stream));
     return QTG_OK;
+}
+
+// clear the per-bead rebuild flags of a per-call step
+static cudaError_t clear_rebuilt(qtg_ctx *ctx, int sys) {
+    const SysDev &S = ctx->sys_h[sys];
+    return cudaMemsetAsync(ctx->rebuilt + S.job_base, 0, sizeof(int) * S.n_beads, ctx->stream);
+}
+
+// The small results of a per-call step -- the heat (heat: PIMD steps), per-bead
+// energies and rebuild flags, the step's accumulators and the status word -- go
+// to the pinned mailbox by asynchronous copies, after which the accumulators and
+// the status word are cleared on the device. One stream synchronisation then
+// resolves them all.
+static cudaError_t post_small_results(qtg_ctx *ctx, int sys, bool heat) {
+    const SysDev &S = ctx->sys_h[sys];
+    cudaError_t e = cudaSuccess;
+    auto chk = [&e](cudaError_t r) {
+        if (e == cudaSuccess) e = r;
+    };
+    if (heat) chk(down(ctx, &ctx->box->heat_out, &ctx->run[sys].heat, sizeof(double)));
+    chk(down(ctx, ctx->box_energy, ctx->energy + S.job_base, sizeof(double) * S.n_beads));
+    chk(down(ctx, ctx->box_rebuilt, ctx->rebuilt + S.job_base, sizeof(int) * S.n_beads));
+    chk(down(ctx, &ctx->box->acc, ctx->acc + sys, sizeof(SysAcc)));
+    chk(down(ctx, &ctx->box->status, ctx->status, sizeof(unsigned)));
+    chk(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
+    chk(cudaMemsetAsync(ctx->status, 0, sizeof(unsigned), ctx->stream));
+    return e;
 }
 
 qtg_status qtg_update_class(qtg_ctx *ctx, int sys, double *q, double *p, const double *mass, double *f,
@@ -1511,28 +1588,27 @@ qtg_status qtg_update_class(qtg_ctx *ctx, int sys, double *q, double *p, const d
     CKS(check_sys(ctx, sys));
     const SysDev &S = ctx->sys_h[sys];
     if (S.n_beads != 1 || !q || !p || !f || !point || !list || !disp) return fail(ctx, QTG_ERR_ARG, "bad argument");
-    CKS(upload_dynamic(ctx, sys, q, p, mass, f, nullptr, charge, point, list, disp));
-    double builds0 = 0.0, builds = 0.0;
-    CK(down(ctx, &builds0, &ctx->run[sys].list_builds, sizeof(double)));
+    CKS(upload_dynamic(ctx, sys, q, p, mass, f, charge, point, list, disp));
+    CK(clear_rebuilt(ctx, sys));
     CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
     launch_ring(ring_args(ctx, sys, RF_KICK | RF_VV | RF_DISP), ctx->stream, &ctx->launches);
     launch_skin_rebuild(list_args(ctx, S.job_base, 1, 0), ctx->stream, &ctx->launches);
-    launch_eval(ctx, eval_args(ctx, ctx->base.d + S.job_base, 1, ctx->q, ctx->fphys, 0, 0));
+    EvalArgs ea = eval_args(ctx, ctx->base.d + S.job_base, 1, ctx->q, ctx->fphys, 0, 0);
+    ea.lj_full = ctx->mixed ? 1 : 0;  // mixed: the dense Lennard-Jones, as in enqueue_forces
+    launch_eval(ctx, ea);
     // P = 1: the propagating force is the physical force
     CK(cudaMemcpyAsync(ctx->f + S.q_off, ctx->fphys + S.q_off, sizeof(double) * S.n_dof, cudaMemcpyDeviceToDevice,
                        ctx->stream));
     RingArgs e = ring_args(ctx, sys, 0);
     e.kick = 1;
     launch_end_step(e, ctx->stream, &ctx->launches);
-    CKS(download_dynamic(ctx, sys, q, p, f, nullptr, point, nullptr, disp));
-    double en = 0.0;
-    CK(down(ctx, &en, ctx->energy + S.job_base, sizeof(double)));
-    CK(down(ctx, &builds, &ctx->run[sys].list_builds, sizeof(double)));
-    CKS(sync_status(ctx));
-    CKS(download_list_if_rebuilt(ctx, sys, list, builds0, builds));
-    CK(cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream));
-    if (energy) *energy = en;
-    return sync_status(ctx);
+    CKS(download_dynamic(ctx, sys, q, p, f, nullptr, nullptr, nullptr, disp));
+    CK(post_small_results(ctx, sys, false));
+    CK(cudaStreamSynchronize(ctx->stream));
+    CKS(status_error(ctx, ctx->box->status));
+    CKS(download_rebuilt_lists(ctx, sys, point, list));
+    if (energy) *energy = ctx->box_energy[0];
+    return QTG_OK;
 }
 
 qtg_status qtg_update_pimd(qtg_ctx *ctx, int sys, double *q, double *p, const double *mass, double *f, double *fphys,
@@ -1541,16 +1617,15 @@ qtg_status qtg_update_pimd(qtg_ctx *ctx, int sys, double *q, double *p, const do
     CKS(check_sys(ctx, sys));
     const SysDev &S = ctx->sys_h[sys];
     if (!q || !p || !f || !fphys || !point || !list || !disp) return fail(ctx, QTG_ERR_ARG, "bad argument");
-    CKS(upload_dynamic(ctx, sys, q, p, mass, f, fphys, charge, point, list, disp));
-    double builds0 = 0.0, builds = 0.0;
-    CK(down(ctx, &builds0, &ctx->run[sys].list_builds, sizeof(double)));
+    CKS(upload_dynamic(ctx, sys, q, p, mass, f, charge, point, list, disp));
     if (noise) CK(up(ctx, ctx->noise, noise, sizeof(double) * (2 + (size_t)(S.n_beads - 1) * S.n_dof)));
-    const double h0 = heat ? *heat : 0.0;
-    CK(up(ctx, &ctx->run[sys].heat, &h0, sizeof(double)));
+    ctx->box->heat_in = heat ? *heat : 0.0;  // the previous call's synchronisation freed the slot
+    CK(up(ctx, &ctx->run[sys].heat, &ctx->box->heat_in, sizeof(double)));
     // the step's device work (update.cpp:271-401), the same for every call of this
     // (system, NVT, caller noise): captured once as a graph and replayed
     auto step = [&]() -> cudaError_t {
         cudaError_t err = cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream);
+        if (err == cudaSuccess) err = clear_rebuilt(ctx, sys);
         if (is_nvt) {
             // centroid kinetic energy after the opening kick, then the centroid draw
             RingArgs e = ring_args(ctx, sys, 0);
@@ -1593,14 +1668,18 @@ qtg_status qtg_update_pimd(qtg_ctx *ctx, int sys, double *q, double *p, const do
     }
     CK(cudaGraphLaunch(it->second.first, ctx->stream));
     ctx->launches += it->second.second;
-    CKS(download_dynamic(ctx, sys, q, p, f, fphys, point, nullptr, disp));
-    double h = 0.0;
-    CK(down(ctx, &h, &ctx->run[sys].heat, sizeof(double)));
-    CK(down(ctx, &builds, &ctx->run[sys].list_builds, sizeof(double)));
-    double vs, ve, extra;
-    CKS(read_energies(ctx, sys, &vs, &ve, &extra));  // synchronises
-    CKS(download_list_if_rebuilt(ctx, sys, list, builds0, builds));
-    if (heat) *heat = h;
+    CKS(download_dynamic(ctx, sys, q, p, f, fphys, nullptr, nullptr, disp));
+    CK(post_small_results(ctx, sys, true));
+    CK(cudaStreamSynchronize(ctx->stream));
+    CKS(status_error(ctx, ctx->box->status));
+    CKS(download_rebuilt_lists(ctx, sys, point, list));
+    double vs = 0.0, ve = 0.0;
+    for (int b = 0; b < S.n_beads; ++b) {
+        vs += ctx->box_energy[b];
+        if (b % 2 == 0) ve += ctx->box_energy[b];
+    }
+    const double extra = ctx->box->acc.sc_extra;
+    if (heat) *heat = ctx->box->heat_out;
     if (S.propagator == QTG_SUZUKI_CHIN) {
         if (pot) *pot = 2.0 * ve / S.n_beads;
         if (energy) *energy = (2.0 * ve + 4.0 * (vs - ve) + extra) / 3.0;

@@ -210,6 +210,7 @@ __global__ void __launch_bounds__(512) k_skin_rebuild(ListArgs a) {
     for (int k = threadIdx.x; k < 3 * N; k += blockDim.x) disp[k] = 0.0;
     if (threadIdx.x == 0 && a.acc) atomicAdd(&a.acc[sid].rebuilds, 1.0);
     if (threadIdx.x == 0 && a.run) atomicAdd(&a.run[sid].list_builds, 1.0);
+    if (threadIdx.x == 0) a.rebuilt[S.job_base + bead] = 1;
 }
 
 }  // namespace

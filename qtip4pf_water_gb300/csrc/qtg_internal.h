@@ -402,6 +402,7 @@ struct ListArgs {
     int *point_full, *list_full;  // may be null: only the half list is built
     SysAcc *acc;
     SysRun *run;        // cumulative rebuild count per system (may be null)
+    int *rebuilt;       // per base job (system's job_base + bead): set to 1 by a rebuild
     unsigned *status;
     int force_rebuild;  // 1: rebuild unconditionally (initial build / per-call API)
     int max_mols;

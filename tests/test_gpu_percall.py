@@ -55,3 +55,54 @@ def test_list_comes_back_only_after_a_rebuild(gpu_lib):
     # a rebuild clears the whole list first, as the reference's neighbour_list does
     # (neighbour.cpp:23-25): past the new list the caller's array now reads zero
     assert np.all(lst[~new_used] == 0)
+
+
+def test_mixed_step_reads_neither_list_nor_fphys(gpu_lib):
+    """Mixed precision takes the dense Lennard-Jones kernel, and fphys is output
+    only: a step with the caller's point/list/fphys overwritten by junk gives the
+    same state as one with the real arrays, and leaves the junk in place."""
+    q = gpu_lib
+    runs = []
+    for junk in (False, True):
+        s, qq, pp, point, lst, disp, f, fp = _setup(q)
+        if junk:
+            point[:] = -3
+            lst[:] = -7
+            fp[:] = np.nan
+        _, heat, _ = s.update_sc_nospline(qq, pp, s.masses(), f, fp, s.charges(), point, lst, disp, True, 0.0)
+        runs.append((qq.copy(), pp.copy(), f.copy(), fp.copy(), heat))
+        if junk:
+            assert np.all(point == -3) and np.all(lst == -7)  # no rebuild: neither written
+    for a, b in zip(runs[0][:4], runs[1][:4]):
+        assert np.array_equal(a, b)
+    assert runs[0][4] == runs[1][4]
+
+
+def test_only_rebuilt_beads_come_back(gpu_lib):
+    q = gpu_lib
+    s, qq, pp, point, lst, disp, f, fp = _setup(q)
+    P, N, cap = s.P, s.N, s.info.list_size
+    point0, lst0 = point.copy(), lst.copy()
+    # a step without a rebuild: the downloads every step makes
+    disp[:] = 0.0
+    h0 = s.ctx.transfer_bytes()
+    s.update_sc_nospline(qq, pp, s.masses(), f, fp, s.charges(), point, lst, disp, True, 0.0)
+    h1 = s.ctx.transfer_bytes()
+    assert np.array_equal(point, point0) and np.array_equal(lst, lst0)
+    disp[:] = 0.0
+    b = 2
+    disp[b * 3 * N: (b + 1) * 3 * N: 3] = 10.0  # bead b only: beyond the skin margin
+    s.update_sc_nospline(qq, pp, s.masses(), f, fp, s.charges(), point, lst, disp, True, 0.0)
+    h2 = s.ctx.transfer_bytes()
+    ref_point, ref_list, _ = s.build_lists(qq)
+    for k in range(P):
+        sl_p, sl_l = slice(k * N, (k + 1) * N), slice(k * cap, (k + 1) * cap)
+        if k == b:
+            assert np.array_equal(point[sl_p], ref_point[sl_p])
+            assert np.array_equal(lst[sl_l], ref_list[sl_l])
+        else:
+            assert np.array_equal(point[sl_p], point0[sl_p])
+            assert np.array_equal(lst[sl_l], lst0[sl_l])
+    # exactly one bead's point and list came down on top of the every-step downloads
+    assert (h2[1] - h1[1]) - (h1[1] - h0[1]) == 4 * (N + cap)
+    assert np.all(disp[b * 3 * N: (b + 1) * 3 * N] == 0.0)
