@@ -233,7 +233,7 @@ def run_gpu(args):
     del f_mix0
 
     # ---- end to end through the drop-in C-ABI call with pinned host buffers --------------
-    e2e = run_e2e(q, st, min(args.steps, 20), flush)
+    e2e = run_e2e(q, st, min(args.steps, 200), flush)
 
     # ---- roofline of the dominant kernel -----------------------------------------------------
     roof = roofline(q, st, mix)
@@ -289,7 +289,7 @@ def run_e2e(q, st, steps, flush):
     fp[:] = f
     heat = 0.0
     nbytes = sum(a.nbytes for a in (qq, pp, f, fp, point, lst, disp)) + mass.nbytes + charge.nbytes
-    for _ in range(3):
+    for _ in range(10):
         _, heat, _ = s.update_sc_nospline(qq, pp, mass, f, fp, charge, point, lst, disp, True, heat)
     tot = 0.0
     b0 = s.ctx.transfer_bytes()

@@ -195,6 +195,10 @@ struct qtg_ctx {
     int device = 0;
     int precision = QTG_FP64;
     cudaStream_t own_stream = nullptr, stream = nullptr;
+    // a second stream and fork / join events: inside the captured per-call step, the
+    // stage-out of arrays that are final early runs beside the later kernels
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join = nullptr;
     std::string err;
     Consts K;
     std::vector<qtg_system_desc> desc;
@@ -211,16 +215,13 @@ struct qtg_ctx {
     double *q = nullptr, *p = nullptr, *f = nullptr, *fphys = nullptr, *disp = nullptr;
     int *point = nullptr, *list = nullptr, *point_full = nullptr, *list_full = nullptr;
     int *rebuilt = nullptr;  // per base job: 1 after a rebuild of that bead's lists (per-call steps clear it)
-    // pinned mailbox of the per-call steps: the step's small results arrive here by
-    // asynchronous copies and resolve with one stream synchronisation
-    struct Mailbox {
-        double heat_in, heat_out;
-        SysAcc acc;
-        unsigned status;
-        int pad;
-    } *box = nullptr;
-    double *box_energy = nullptr;  // [max_p] per-bead energies of the step
-    int *box_rebuilt = nullptr;    // [max_p] per-bead rebuild flags of the step
+    // mapped, page-locked mailbox of the per-call steps: the caller's array
+    // pointers for the stage kernels, and the step's small results, which arrive
+    // by asynchronous copies or stage-kernel stores and resolve with one stream
+    // synchronisation (host addresses; *_d: the same memory seen from the device)
+    CallBox *box = nullptr, *box_d = nullptr;
+    double *box_energy = nullptr, *box_energy_d = nullptr;  // [max_p] per-bead energies
+    int *box_rebuilt = nullptr, *box_rebuilt_d = nullptr;    // [max_p] per-bead rebuild flags
     size_t total_point_full = 0, total_list_full = 0;
     double *charge = nullptr, *mass = nullptr, *inv_mass = nullptr, *sqrt_mass = nullptr;
     double *cf_acc = nullptr;  // mean-centroid-force sums of constrained systems, per dof (like mass)
@@ -255,6 +256,8 @@ struct qtg_ctx {
     int n_sc_odd = 0;
     ColWork *colwork = nullptr;
     int n_colwork = 0;
+    double *cw_part = nullptr;    // [n_colwork][4] block partials of the ordered system sums
+    unsigned *cw_ticket = nullptr;  // [n_sys] arrival tickets of those sums
     // run state
     SysAcc *acc = nullptr;
     SysRun *run = nullptr;
@@ -390,6 +393,8 @@ RingArgs ring_args(qtg_ctx *c, int sys, int flags) {
     r.max_p = c->max_p;
     r.cf_acc = c->cf_acc;
     r.status = c->status;
+    r.cw_part = c->cw_part;
+    r.cw_ticket = c->cw_ticket;
     return r;
 }
 
@@ -958,17 +963,19 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     ctx->n_sc_odd = (int)scs.size();
     std::vector<ColWork> cw;
     for (int s = 0; s < n_systems; ++s) {
-        const SysDev &S = ctx->sys_h[s];
+        SysDev &S = ctx->sys_h[s];
         ctx->cw_begin.push_back((int)cw.size());
         for (int c0 = 0; c0 < S.n_dof; c0 += S.cols_per_block) {
             ColWork w;
             w.sys = s;
             w.col0 = c0;
             w.ncols = std::min(S.cols_per_block, S.n_dof - c0);
-            w.pad = 0;
+            w.slot = (int)cw.size();
             cw.push_back(w);
         }
         ctx->cw_count.push_back((int)cw.size() - ctx->cw_begin[s]);
+        S.cw_begin = ctx->cw_begin[s];
+        S.cw_count = ctx->cw_count[s];
     }
     ctx->n_colwork = (int)cw.size();
     ctx->noise_len = 2 + (size_t)(ctx->max_p - 1) * ctx->max_dof;
@@ -982,6 +989,9 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     }
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
     ctx->stream = ctx->own_stream;
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&ctx->ev_fork[k], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
 #define AL(ptr, n)                                  \
     if (e == cudaSuccess) e = dalloc(&(ptr), (n));
     AL(ctx->sys_d, n_systems);
@@ -1041,13 +1051,18 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->rebuilt, ctx->base.h.size());
     if (e == cudaSuccess) {
         void *pin = nullptr;
-        const size_t bytes = sizeof(qtg_ctx::Mailbox) + (sizeof(double) + sizeof(int)) * ctx->max_p;
-        e = cudaHostAlloc(&pin, bytes, cudaHostAllocDefault);
+        const size_t bytes = sizeof(CallBox) + (sizeof(double) + sizeof(int)) * ctx->max_p;
+        e = cudaHostAlloc(&pin, bytes, cudaHostAllocMapped);
+        void *pin_d = nullptr;
+        if (e == cudaSuccess) e = cudaHostGetDevicePointer(&pin_d, pin, 0);
         if (e == cudaSuccess) {
             memset(pin, 0, bytes);
-            ctx->box = static_cast<qtg_ctx::Mailbox *>(pin);
+            ctx->box = static_cast<CallBox *>(pin);
             ctx->box_energy = reinterpret_cast<double *>(ctx->box + 1);
             ctx->box_rebuilt = reinterpret_cast<int *>(ctx->box_energy + ctx->max_p);
+            ctx->box_d = static_cast<CallBox *>(pin_d);
+            ctx->box_energy_d = reinterpret_cast<double *>(ctx->box_d + 1);
+            ctx->box_rebuilt_d = reinterpret_cast<int *>(ctx->box_energy_d + ctx->max_p);
         }
     }
     AL(ctx->fd.d, ctx->fd.h.size());
@@ -1061,6 +1076,8 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->sc_sys, scs.size());
     AL(ctx->sc_bead, scb.size());
     AL(ctx->colwork, cw.size());
+    AL(ctx->cw_part, 4 * cw.size());
+    AL(ctx->cw_ticket, n_systems);
     AL(ctx->acc, n_systems);
     AL(ctx->run, n_systems);
     AL(ctx->est, (size_t)ctx->max_records * n_systems * 8);
@@ -1108,6 +1125,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
             r.heat = 0.0;
             r.alpha = 1.0;
             r.cf_samples = r.list_builds = r.R_draw = r.g2_draw = 0.0;
+            r.draw_step_plus1 = 0ull;
         }
         cp(ctx->run, runs.data(), sizeof(SysRun) * n_systems);
         if (e == cudaSuccess) e = cudaMemset(ctx->cf_acc, 0, sizeof(double) * ctx->n_cf);
@@ -1133,13 +1151,16 @@ void qtg_destroy(qtg_ctx *ctx) {
                     ctx->phase, ctx->opos, ctx->part, ctx->skp, ctx->dskp, ctx->wsk, ctx->wdsk, ctx->energy, ctx->energy_aux,
                     ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
-                    ctx->status, ctx->red_out, ctx->rebuilt};
+                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->box) cudaFreeHost(ctx->box);
     for (auto &g : ctx->surrogates) free_surrogate(g);
     for (auto &g : ctx->call_graphs) cudaGraphExecDestroy(g.second.first);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
+    for (cudaEvent_t ev : {ctx->ev_fork[0], ctx->ev_fork[1], ctx->ev_join})
+        if (ev) cudaEventDestroy(ev);
     delete ctx;
 }
 
@@ -1535,6 +1556,38 @@ static qtg_status download_dynamic(qtg_ctx *ctx, int sys, double *q, double *p, 
     return QTG_OK;
 }
 
+// Whether the five state arrays of a per-call step can move by stage-kernel
+// loads and stores: each must start in page-locked host memory that the device
+// can address and that was not registered read-only, and no two may overlap (the
+// copy path writes them back in a fixed order, the stage kernel all at once).
+// The device addresses go to d*. The callers' arrays hold nt doubles (q, p, f,
+// fphys) and nd (disp), as the reference's do.
+static bool stageable(qtg_ctx *ctx, double *q, double *p, double *f, double *fphys, double *disp, size_t nt,
+                      size_t nd, double **dq, double **dp, double **df, double **dfp, double **dd) {
+    if (!ctx->box_d) return false;
+    double *h[5] = {q, p, f, fphys, disp};
+    double **d[5] = {dq, dp, df, dfp, dd};
+    const size_t n[5] = {nt, nt, nt, nt, nd};
+    for (int k = 0; k < 5; ++k) {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, h[k]) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (at.type != cudaMemoryTypeHost || !at.devicePointer) return false;
+        unsigned flags = 0;
+        if (cudaHostGetFlags(&flags, h[k]) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (flags & cudaHostRegisterReadOnly) return false;
+        *d[k] = static_cast<double *>(at.devicePointer);
+        for (int j = 0; j < k; ++j)
+            if (h[j] < h[k] + n[k] && h[k] < h[j] + n[j]) return false;
+    }
+    return true;
+}
+
 // The point and list arrays of a per-call step go back to the caller bead by
 // bead, for the beads whose skin test rebuilt them during the call (the
 // reference's neighbour_list writes a bead's point and list only when it
@@ -1617,38 +1670,114 @@ qtg_status qtg_update_pimd(qtg_ctx *ctx, int sys, double *q, double *p, const do
     CKS(check_sys(ctx, sys));
     const SysDev &S = ctx->sys_h[sys];
     if (!q || !p || !f || !fphys || !point || !list || !disp) return fail(ctx, QTG_ERR_ARG, "bad argument");
-    CKS(upload_dynamic(ctx, sys, q, p, mass, f, charge, point, list, disp));
-    if (noise) CK(up(ctx, ctx->noise, noise, sizeof(double) * (2 + (size_t)(S.n_beads - 1) * S.n_dof)));
+    const size_t nt = (size_t)S.n_beads * S.n_dof, nd = (size_t)S.n_beads * 3 * S.n_mols;
+    // q, p, f, fphys and disp in page-locked, mapped, writable and disjoint host
+    // memory move inside the step's graph by the stage kernels; anything else by
+    // copy calls
+    double *dq = nullptr, *dp = nullptr, *df = nullptr, *dfp = nullptr, *dd = nullptr;
+    const bool staged = !noise && stageable(ctx, q, p, f, fphys, disp, nt, nd, &dq, &dp, &df, &dfp, &dd);
     ctx->box->heat_in = heat ? *heat : 0.0;  // the previous call's synchronisation freed the slot
-    CK(up(ctx, &ctx->run[sys].heat, &ctx->box->heat_in, sizeof(double)));
+    if (staged) {
+        if (charge) CKS(upload_charges(ctx, sys, charge));
+        if (mass) CKS(upload_masses(ctx, sys, mass));
+        if (step_reads_lists(ctx, sys)) CKS(upload_lists(ctx, sys, point, list, 0, S.n_beads));
+        ctx->box->q = dq;
+        ctx->box->p = dp;
+        ctx->box->f = df;
+        ctx->box->fphys = dfp;
+        ctx->box->disp = dd;
+        ctx->h2d_bytes += sizeof(double) * (3 * nt + nd + 1);
+        ctx->d2h_bytes += sizeof(double) * (4 * nt + nd + 1 + S.n_beads) + sizeof(int) * S.n_beads +
+                          sizeof(SysAcc) + sizeof(unsigned);
+    } else {
+        CKS(upload_dynamic(ctx, sys, q, p, mass, f, charge, point, list, disp));
+        if (noise) CK(up(ctx, ctx->noise, noise, sizeof(double) * (2 + (size_t)(S.n_beads - 1) * S.n_dof)));
+        CK(up(ctx, &ctx->run[sys].heat, &ctx->box->heat_in, sizeof(double)));
+    }
+    StageArgs sg;
+    memset(&sg, 0, sizeof(sg));
+    sg.box = ctx->box_d;
+    sg.box_energy = ctx->box_energy_d;
+    sg.box_rebuilt = ctx->box_rebuilt_d;
+    sg.q = ctx->q + S.q_off;
+    sg.p = ctx->p + S.q_off;
+    sg.f = ctx->f + S.q_off;
+    sg.fphys = ctx->fphys + S.q_off;
+    sg.disp = ctx->disp + S.d_off;
+    sg.nt = (long long)nt;
+    sg.nd = (long long)nd;
+    sg.run = ctx->run + sys;
+    sg.energy = ctx->energy + S.job_base;
+    sg.rebuilt = ctx->rebuilt + S.job_base;
+    sg.acc = ctx->acc + sys;
+    sg.status = ctx->status;
+    sg.n_beads = S.n_beads;
+    sg.blocks = std::max(1, std::min(8 * ctx->n_sm, (int)((4 * nt + nd + 255) / 256)));
     // the step's device work (update.cpp:271-401), the same for every call of this
-    // (system, NVT, caller noise): captured once as a graph and replayed
+    // (system, NVT, caller noise, staging): captured once as a graph and replayed
     auto step = [&]() -> cudaError_t {
-        cudaError_t err = cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream);
+        cudaError_t err = cudaSuccess;
+        // staged NVT: the centroid-alpha kernel moves p and f in as it reads them,
+        // while q and disp come in on the side stream
+        const bool split_in = staged && is_nvt;
+        if (staged && !split_in) {
+            StageArgs si = sg;
+            si.mask = STAGE_Q | STAGE_P | STAGE_F | STAGE_DISP;
+            launch_stage_in(si, ctx->stream, &ctx->launches);
+        }
+        if (split_in) {
+            err = cudaEventRecord(ctx->ev_fork[0], ctx->stream);
+            if (err == cudaSuccess) err = cudaStreamWaitEvent(ctx->side_stream, ctx->ev_fork[0], 0);
+            StageArgs si = sg;
+            si.mask = STAGE_Q | STAGE_DISP;
+            launch_stage_in(si, ctx->side_stream, &ctx->launches);
+            if (err == cudaSuccess) err = cudaEventRecord(ctx->ev_join, ctx->side_stream);
+        }
+        if (err == cudaSuccess) err = cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream);
         if (err == cudaSuccess) err = clear_rebuilt(ctx, sys);
         if (is_nvt) {
-            // centroid kinetic energy after the opening kick, then the centroid draw
+            // centroid kinetic energy after the opening kick, the centroid draws and alpha
             RingArgs e = ring_args(ctx, sys, 0);
-            e.kick = 0;
-            launch_end_step(e, ctx->stream, &ctx->launches);
-            FinalizeArgs fa = fin_args(ctx, sys, 0, 1);
-            fa.pile_g = 1;
-            fa.noise = noise ? ctx->noise : nullptr;
-            launch_finalize(fa, ctx->stream, &ctx->launches);
+            e.noise = noise ? ctx->noise : nullptr;
+            e.box = split_in ? ctx->box_d : nullptr;
+            launch_centroid_alpha(e, sys, ctx->stream, &ctx->launches);
         }
+        if (split_in && err == cudaSuccess) err = cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0);
         RingArgs r = ring_args(ctx, sys, RF_KICK | RF_FWD | RF_CAYLEY | RF_BACK | RF_DISP | (is_nvt ? RF_THERMO : 0));
         r.noise = noise ? ctx->noise : nullptr;
         r.pile_g = 1;
+        // one extra block draws the next call's centroid variates beside the ring work
+        r.n_draw = noise ? 0 : 1;
+        r.draw_sys0 = sys;
         launch_ring(r, ctx->stream, &ctx->launches);
         launch_skin_rebuild(list_args(ctx, S.job_base, S.n_beads, 0), ctx->stream, &ctx->launches);
+        // staged: q and disp are final here, f and fphys after the forces; each goes
+        // back on the side stream beside the kernels that follow
+        auto side = [&](int k, unsigned mask) {
+            if (err == cudaSuccess) err = cudaEventRecord(ctx->ev_fork[k], ctx->stream);
+            if (err == cudaSuccess) err = cudaStreamWaitEvent(ctx->side_stream, ctx->ev_fork[k], 0);
+            StageArgs so = sg;
+            so.mask = mask;
+            so.blocks = std::min(sg.blocks, 2 * ctx->n_sm);
+            launch_stage_out(so, ctx->side_stream, &ctx->launches);
+        };
+        if (staged) side(0, STAGE_Q | STAGE_DISP);
         if (err == cudaSuccess) err = cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream);
         enqueue_forces(ctx, sys, false);
+        if (staged) side(1, STAGE_F | STAGE_FPHYS);
         RingArgs e = ring_args(ctx, sys, 0);
         e.kick = 1;
         launch_end_step(e, ctx->stream, &ctx->launches);
+        if (staged) {
+            if (err == cudaSuccess) err = cudaEventRecord(ctx->ev_join, ctx->side_stream);
+            if (err == cudaSuccess) err = cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0);
+            StageArgs so = sg;
+            so.mask = STAGE_P | STAGE_SMALL;
+            launch_stage_out(so, ctx->stream, &ctx->launches);
+        }
         return err;
     };
-    const int key = sys * 4 + (is_nvt ? 2 : 0) + (noise ? 1 : 0);
+    const int key = sys * 8 + (staged ? 4 : 0) + (is_nvt ? 2 : 0) + (noise ? 1 : 0);
     auto it = ctx->call_graphs.find(key);
     if (it == ctx->call_graphs.end()) {
         cudaGraph_t graph;
@@ -1668,8 +1797,10 @@ qtg_status qtg_update_pimd(qtg_ctx *ctx, int sys, double *q, double *p, const do
     }
     CK(cudaGraphLaunch(it->second.first, ctx->stream));
     ctx->launches += it->second.second;
-    CKS(download_dynamic(ctx, sys, q, p, f, fphys, nullptr, nullptr, disp));
-    CK(post_small_results(ctx, sys, true));
+    if (!staged) {
+        CKS(download_dynamic(ctx, sys, q, p, f, fphys, nullptr, nullptr, disp));
+        CK(post_small_results(ctx, sys, true));
+    }
     CK(cudaStreamSynchronize(ctx->stream));
     CKS(status_error(ctx, ctx->box->status));
     CKS(download_rebuilt_lists(ctx, sys, point, list));

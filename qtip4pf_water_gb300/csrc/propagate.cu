@@ -77,16 +77,18 @@ __device__ void centroid_draw(const SysDev &S, int sys, unsigned long long st, d
 
 __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
     if ((int)blockIdx.x < a.n_draw) {
-        // draw blocks (the first ones, so that they start with the first wave): this
-        // step's PILE-G centroid draws, made while the ring work runs
-        const int sys = blockIdx.x;
+        // draw blocks (the first ones, so that they start with the first wave): the
+        // PILE-G centroid draws at the current step, made while the ring work runs
+        const int sys = a.draw_sys0 + blockIdx.x;
         const SysDev &S = a.sys[sys];
         if (threadIdx.x >= 32 || !(S.thermostat == 1 || a.pile_g)) return;
         double R, g2;
-        centroid_draw(S, sys, *a.step, &R, &g2, a.status);
+        const unsigned long long st = *a.step;
+        centroid_draw(S, sys, st, &R, &g2, a.status);
         if (threadIdx.x == 0) {
             a.run[sys].R_draw = R;
             a.run[sys].g2_draw = g2;
+            a.run[sys].draw_step_plus1 = st + 1;
         }
         return;
     }
@@ -261,15 +263,20 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
             a.disp[S.d_off + (long long)k * 3 * S.n_mols + 3 * (col / 9) + (col % 9)] += qn - q_old;
     }
     if (flags & RF_THERMO) {
-        // one warp sums the block's values (8 a lane), then one 5-level shuffle reduction
+        // one warp sums the block's values (8 a lane), then one 5-level shuffle
+        // reduction; the blocks' sums go to the system's heat in slot order
+        __shared__ double bsum;
         hred[threadIdx.x] = heat;
         __syncthreads();
         if (threadIdx.x < 32) {
             double t = 0.0;
             for (int k = threadIdx.x; k < (int)blockDim.x; k += 32) t += hred[k];
             t = warp_sum(t);
-            if (threadIdx.x == 0) atomicAdd(&a.run[W.sys].heat, t);
+            if (threadIdx.x == 0) bsum = t;
         }
+        __syncthreads();
+        double *const dst[1] = {&a.run[W.sys].heat};
+        ordered_system_sum<1>(&bsum, W.slot, S.cw_begin, S.cw_count, a.cw_part, a.cw_ticket + W.sys, dst);
     }
 }
 
@@ -345,16 +352,18 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
     red4[3][threadIdx.x] = k0;
     __syncthreads();
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __shared__ double bsum[4];
     if (w < 4) {
         double t = 0.0;
         for (int k = lane; k < (int)blockDim.x; k += 32) t += red4[w][k];
         t = warp_sum(t);
-        if (lane == 0) {
-            SysAcc *ac = &a.acc[W.sys];
-            double *dst = w == 0 ? &ac->kin : w == 1 ? &ac->spring : w == 2 ? &ac->kcv_tq : &ac->k0;
-            atomicAdd(dst, t);
-        }
+        if (lane == 0) bsum[w] = t;
     }
+    __syncthreads();
+    // the blocks' sums go to the system's accumulators in slot order
+    SysAcc *ac = &a.acc[W.sys];
+    double *const dst[4] = {&ac->kin, &ac->spring, &ac->kcv_tq, &ac->k0};
+    ordered_system_sum<4>(bsum, W.slot, S.cw_begin, S.cw_count, a.cw_part, a.cw_ticket + W.sys, dst);
 }
 
 // Centroid normal-mode kinetic energy of normal-mode momenta (row 0 of p).
@@ -368,8 +377,103 @@ __global__ void k_centroid_ke(RingArgs a) {
         const double pv = a.p[S.q_off + col];
         e += 0.5 * pv * pv * a.inv_mass[S.mass_off + col];
     }
-    double t = block_sum(e, red);
-    if (threadIdx.x == 0) atomicAdd(&a.acc[W.sys].k0, t);
+    __shared__ double bsum;
+    const double t = block_sum(e, red);
+    if (threadIdx.x == 0) bsum = t;
+    __syncthreads();
+    double *const dst[1] = {&a.acc[W.sys].k0};
+    ordered_system_sum<1>(&bsum, W.slot, S.cw_begin, S.cw_count, a.cw_part, a.cw_ticket + W.sys, dst);
+}
+
+// The PILE-G centroid rescale factor of one system's per-call step
+// (update.cpp:271-320 with thermostat.cpp:64-100): the centroid kinetic energy
+// after the opening kick, k0 = sum_dof (sqrt(1/P) sum_b (p_b + dt/2 f_b))^2 / 2m
+// (the half Cayley step leaves the centroid momentum alone), and the draws R and
+// g2 (caller noise, else the counter-based generator at the system's step --
+// made ahead by the previous per-call ring launch when it drew for this step).
+// With a mailbox (a staged per-call step) the kernel also moves p and f from the
+// caller's arrays to the device ones as it reads them.
+// Block 0 makes the draws while blocks 1.. sum column blocks of k0; the block
+// that arrives last on the system's ticket adds the column sums in slot order,
+// sets alpha = sqrt((R^2 + g2) / (2 beta_n k0)) and advances the step counter, as
+// the estimator-free finalize of this step did.
+__global__ void __launch_bounds__(256) k_centroid_alpha(RingArgs a, int sys) {
+    const SysDev &S = a.sys[sys];
+    SysRun *run = &a.run[sys];
+    __shared__ double X[256];
+    __shared__ double red[8];
+    __shared__ int last;
+    if (blockIdx.x == 0) {
+        if (threadIdx.x < 32) {
+            double R, g2;
+            const unsigned long long st = *a.step;
+            if (a.noise) {
+                R = a.noise[0];
+                g2 = a.noise[1];
+            } else if (run->draw_step_plus1 == st + 1) {  // made ahead by an earlier ring launch
+                R = run->R_draw;
+                g2 = run->g2_draw;
+            } else {
+                centroid_draw(S, sys, st, &R, &g2, a.status);
+            }
+            if (threadIdx.x == 0) {
+                run->R_draw = R;
+                run->g2_draw = g2;
+            }
+        }
+    } else {
+        const ColWork W = a.work[blockIdx.x - 1];
+        const int P = S.n_beads, C = S.cols_per_block;
+        const int b = threadIdx.x / C, c = threadIdx.x - b * C;
+        const bool act = (b < P) && (c < W.ncols);
+        const int col = W.col0 + c;
+        // staged: p and f come from the caller's arrays and are stored on the device
+        __shared__ const double *src[2];
+        if (threadIdx.x == 0) {
+            src[0] = a.box ? a.box->p : a.p + S.q_off;
+            src[1] = a.box ? a.box->f : a.f + S.q_off;
+        }
+        __syncthreads();
+        if (act) {
+            const long long at = (long long)b * S.n_dof + col;
+            const double pv = src[0][at], fv = src[1][at];
+            if (a.box) {
+                a.p[S.q_off + at] = pv;
+                const_cast<double *>(a.f)[S.q_off + at] = fv;  // the device force array (RingArgs reads it)
+            }
+            X[threadIdx.x] = pv + S.halfdt * fv;
+        }
+        __syncthreads();
+        double k0 = 0.0;
+        if (b == 0 && c < W.ncols) {
+            double sp = 0.0;
+            for (int j = 0; j < P; ++j) sp += X[j * C + c];
+            const double p0 = sqrt(1.0 / P) * sp;
+            k0 = 0.5 * p0 * p0 * a.inv_mass[S.mass_off + col];
+        }
+        const double t = block_sum(k0, red);
+        if (threadIdx.x == 0) a.cw_part[(size_t)W.slot * 4] = t;
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(a.cw_ticket + sys, 1u) == (unsigned)S.cw_count;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double t = 0.0;
+    for (int j = threadIdx.x; j < S.cw_count; j += blockDim.x) t += __ldcg(&a.cw_part[(size_t)(S.cw_begin + j) * 4]);
+    t = block_sum(t, red);
+    if (threadIdx.x == 0) {
+        const double R = __ldcg(&run->R_draw), g2 = __ldcg(&run->g2_draw);
+        a.acc[sys].k0 = t;
+        run->alpha = sqrt((R * R + g2) / (2.0 * S.beta_n * t));
+        // the step counter lives in writable device memory; RingArgs hands it to
+        // the ring kernels read-only
+        unsigned long long *step = const_cast<unsigned long long *>(a.step);
+        *step = *step + 1;
+        a.cw_ticket[sys] = 0u;
+    }
 }
 
 // One warp per system: the step's estimator record and the next centroid
@@ -575,6 +679,12 @@ void launch_end_step(const RingArgs &a, cudaStream_t s, unsigned long long *n) {
 void launch_centroid_ke(const RingArgs &a, cudaStream_t s, unsigned long long *n) {
     if (a.n_work <= 0) return;
     k_centroid_ke<<<a.n_work, 256, 0, s>>>(a);
+    if (n) ++*n;
+}
+
+void launch_centroid_alpha(const RingArgs &a, int sys, cudaStream_t s, unsigned long long *n) {
+    if (a.n_work <= 0) return;
+    k_centroid_alpha<<<a.n_work + 1, 256, 0, s>>>(a, sys);
     if (n) ++*n;
 }
 

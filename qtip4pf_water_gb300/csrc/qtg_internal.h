@@ -25,6 +25,7 @@ struct Consts {
 struct SysDev {
     int n_mols, n_beads, n_sites, n_dof, list_size, k_max, n_kvec, kvec_off;
     int propagator, thermostat, job_base, cols_per_block;
+    int cw_begin, cw_count;  // the system's column-work blocks: slots cw_begin .. cw_begin + cw_count - 1
     int n_kvec_ref;              // the reference's k-vector count (n_kvec includes c_k = 0 fillers)
     int col_off, n_col, grp_off, n_grp, batch_off, n_batch;
     int centroid_fixed;          // 1: the centroid is held fixed (centroid-constrained PIMD)
@@ -111,7 +112,8 @@ struct SysRun {
     double alpha;       // centroid rescale factor for the next O step (PILE-G)
     double cf_samples;  // steps accumulated into the mean centroid force
     double list_builds; // Verlet-list rebuilds of any bead since creation (never reset)
-    double R_draw, g2_draw;  // the step's PILE-G centroid draws, made ahead by k_ring's draw blocks
+    double R_draw, g2_draw;  // PILE-G centroid draws made ahead by k_ring's draw blocks ...
+    unsigned long long draw_step_plus1;  // ... for step draw_step_plus1 - 1 (0: none made)
 };
 
 // Status word written by kernels (bit flags), read by the host after a sync.
@@ -149,6 +151,51 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
         t = warp_sum(t);
     }
     return t;  // valid in warp 0 (lane 0)
+}
+
+// Fixed-order sum of per-block values over the column-work blocks of one system
+// (every thread of the block calls it, after the kernel's last __syncthreads).
+// Each block stores its NV values (v, read by thread 0) at its slot; the block
+// that arrives last on the system's ticket sums all the system's slots in slot
+// order (thread t the slots t, t + blockDim.x, ..., all NV values at once, then a
+// fixed shuffle-and-shared-memory tree), adds the NV totals to dst[k] and re-arms
+// the ticket. The totals therefore do not depend on the order the blocks ran in.
+template <int NV>
+__device__ void ordered_system_sum(const double *v, int slot, int cw_begin, int cw_count, double *part,
+                                   unsigned *ticket, double *const *dst) {
+    __shared__ int last;
+    __shared__ double red[NV][32];
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < NV; ++k) part[(size_t)slot * NV + k] = v[k];
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == (unsigned)(cw_count - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double t[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) t[k] = 0.0;
+    for (int j = threadIdx.x; j < cw_count; j += blockDim.x) {
+        const double *pj = part + (size_t)(cw_begin + j) * NV;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) t[k] += __ldcg(pj + k);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        t[k] = warp_sum(t[k]);
+        if (lane == 0) red[k][w] = t[k];
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const double u = warp_sum(lane < nw ? red[k][lane] : 0.0);
+            if (lane == 0) *dst[k] += u;
+        }
+        if (lane == 0) *ticket = 0u;
+    }
 }
 
 // Philox4x32-10 counter-based generator (Salmon, Moraes, Dror & Shaw,
@@ -208,7 +255,8 @@ enum RngTag : uint32_t { RNG_MODES = 1u, RNG_CENTROID = 2u, RNG_GAMMA = 3u };
 // Column work item of the normal-mode / propagation kernels: a block handles
 // cols_per_block dof columns of one system (all beads of each column).
 struct ColWork {
-    int sys, col0, ncols, pad;
+    int sys, col0, ncols;
+    int slot;  // index of this block in the context's column-work list
 };
 
 enum RingFlags : int {
@@ -246,8 +294,14 @@ struct RingArgs {
     double *cf_acc;          // end step: sum over steps of the bead-averaged force, per dof
                              // (systems with a fixed centroid; indexed like mass)
     unsigned *status;        // ring draw blocks: ST_GAMMA_LIMIT
-    int n_draw;              // ring: extra blocks that make the step's PILE-G centroid draws of
-                             // systems 0 .. n_draw-1 while the ring work runs (0: none)
+    double *cw_part;         // per column-work slot: block partials of the system sums (4 doubles)
+    unsigned *cw_ticket;     // per system: blocks arrived at the system sums of the running kernel
+    const struct CallBox *box;  // centroid alpha: staged per-call step -- p and f come from the
+                                // caller's arrays named in this mailbox (device address)
+    int n_draw;              // ring: extra blocks that make the PILE-G centroid draws at the
+                             // current step of systems draw_sys0 .. draw_sys0 + n_draw - 1
+                             // while the ring work runs (0: none)
+    int draw_sys0;
 };
 
 struct FinalizeArgs {
@@ -303,6 +357,8 @@ void launch_sc_finish(const ScArgs &a, cudaStream_t s, unsigned long long *n);
 void launch_transform(const SysDev *sys, int sysi, int P, const double *nm_sys, double *a, int length,
                       int forwards, cudaStream_t s, unsigned long long *n);
 void launch_centroid_ke(const RingArgs &a, cudaStream_t s, unsigned long long *n);
+// per-call PIMD steps: k0 after the opening kick, the centroid draws and alpha of system sys
+void launch_centroid_alpha(const RingArgs &a, int sys, cudaStream_t s, unsigned long long *n);
 // sum_k sum_j (p_kj^2 / 2 m_j + m_j w_k^2 q_kj^2 / 2) of normal-mode arrays -> out[0], out[1]
 void launch_nm_energy(const SysDev *sys, int sysi, int P, int n_dof, const double *q, const double *p,
                       const double *mass, const ModeCoef *modes, double *out, cudaStream_t s,
@@ -408,5 +464,38 @@ struct ListArgs {
     int max_mols;
 };
 void launch_skin_rebuild(const ListArgs &a, cudaStream_t s, unsigned long long *launches);
+
+// stage.cu: the per-call mailbox and the kernels that move a per-call step's
+// arrays between the caller's page-locked host memory and the device
+struct CallBox {
+    // the caller's arrays of this call (device-accessible host memory; stage kernels)
+    double *q, *p, *f, *fphys, *disp;
+    double heat_in, heat_out;
+    SysAcc acc;
+    unsigned status;
+    int pad;
+    // followed by double energy[max_p] and int rebuilt[max_p]
+};
+struct StageArgs {
+    CallBox *box;            // device address of the mailbox
+    double *box_energy;      // device address of its energy[]
+    int *box_rebuilt;        // device address of its rebuilt[]
+    double *q, *p, *f, *fphys, *disp;  // the system's device arrays
+    long long nt, nd;        // doubles in q (p, f, fphys) and in disp
+    SysRun *run;             // the system's run state (heat)
+    const double *energy;    // the system's per-bead energies
+    const int *rebuilt;      // the system's per-bead rebuild flags
+    SysAcc *acc;             // the system's step accumulators (cleared by stage out)
+    unsigned *status;        // context status word (copied, then cleared, by stage out)
+    int n_beads;
+    int blocks;              // grid size
+    unsigned mask;           // stage out: STAGE_* arrays to write back
+};
+enum StageParts : unsigned {
+    STAGE_Q = 1u, STAGE_P = 2u, STAGE_F = 4u, STAGE_FPHYS = 8u, STAGE_DISP = 16u,
+    STAGE_SMALL = 32u,  // heat, energies, rebuild flags, accumulators, status
+};
+void launch_stage_in(const StageArgs &a, cudaStream_t s, unsigned long long *n);
+void launch_stage_out(const StageArgs &a, cudaStream_t s, unsigned long long *n);
 
 }  // namespace qtg

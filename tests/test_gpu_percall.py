@@ -106,3 +106,30 @@ def test_only_rebuilt_beads_come_back(gpu_lib):
     # exactly one bead's point and list came down on top of the every-step downloads
     assert (h2[1] - h1[1]) - (h1[1] - h0[1]) == 4 * (N + cap)
     assert np.all(disp[b * 3 * N: (b + 1) * 3 * N] == 0.0)
+
+
+def test_staged_and_copied_steps_agree(gpu_lib):
+    """Arrays in page-locked host memory move inside the step's graph by the stage
+    kernels; pageable arrays by copy calls. Both give the same state and heat bits
+    (the per-bead energies are sums of FP64 atomic adds, whose order may vary), and
+    the staged call launches four stage kernels on top of the step's own (stage
+    in; stage out of q and disp beside the forces, of f and fphys beside the
+    closing kick, of p and the small results at the end)."""
+    torch = pytest.importorskip("torch")
+    q = gpu_lib
+    out = []
+    for pinned in (False, True):
+        s, qq, pp, point, lst, disp, f, fp = _setup(q)
+        if pinned:
+            qq, pp, disp, f, fp = (torch.from_numpy(a.copy()).pin_memory().numpy() for a in (qq, pp, disp, f, fp))
+        heat, launches, e = 0.0, [], 0.0
+        for _ in range(3):
+            k0 = s.ctx.kernel_launches()
+            e, heat, _ = s.update_sc_nospline(qq, pp, s.masses(), f, fp, s.charges(), point, lst, disp, True, heat)
+            launches.append(s.ctx.kernel_launches() - k0)
+        out.append((qq.copy(), pp.copy(), f.copy(), fp.copy(), disp.copy(), heat, e, launches))
+    for a, b in zip(out[0][:5], out[1][:5]):
+        assert np.array_equal(a, b)
+    assert out[0][5] == out[1][5] != 0.0
+    assert abs(out[0][6] - out[1][6]) <= 1e-12 * abs(out[0][6])
+    assert all(x == out[0][7][0] + 4 for x in out[1][7]), (out[0][7], out[1][7])
