@@ -131,7 +131,7 @@ void nm_matrix(int P, std::vector<double> &C) {
 // build the structure-factor groups (<= 8 kz of one column) and the force
 // batches (whole columns, <= 128 vectors).
 void build_columns(const std::vector<KVec> &kv, std::vector<KVec> &kord, std::vector<KCol> &cols,
-                   std::vector<KGroup> &grps, std::vector<KBatch> &bats) {
+                   std::vector<KGroup> &grps, std::vector<KBatch> &bats, std::vector<int> &kpk) {
     std::map<std::pair<int, int>, std::map<int, KVec>> by;
     for (const KVec &v : kv) by[{v.kx, v.ky}][v.kz] = v;
     for (auto &col : by) {
@@ -182,6 +182,16 @@ void build_columns(const std::vector<KVec> &kv, std::vector<KVec> &kord, std::ve
         bats.push_back(b);
         c0 = c1;
     }
+    // the FP32 k-force kernel's packing: per batch, the columns' |kz| = 0 .. m in
+    // consecutive slots; the kz >= 0 entry of each pair names its slot and |kz|
+    kpk.assign(kord.size(), -1);
+    for (const KBatch &b : bats) {
+        int slot = 0;
+        for (int c = b.c0; c < b.c1; ++c) {
+            for (int az = 0; az <= cols[c].m; ++az) kpk[cols[c].k_begin + cols[c].m + az] = ((slot + az) << 8) | az;
+            slot += cols[c].m + 1;
+        }
+    }
 }
 
 struct Table {  // a device job table plus its host copy
@@ -231,6 +241,7 @@ struct qtg_ctx {
     double *noise = nullptr;  // per-call noise (2 + (Pmax-1) * 9Nmax)
     size_t noise_len = 0;
     KVec *kvec = nullptr;
+    int *kpk = nullptr;  // FP32 k-force packing code per k (see build_columns)
     KCol *kcol = nullptr;
     KGroup *kgrp = nullptr;
     KBatch *kbatch = nullptr;
@@ -329,6 +340,7 @@ EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, d
     a.kcol = c->kcol;
     a.kgrp = c->kgrp;
     a.kbatch = c->kbatch;
+    a.kpk = c->kpk;
     a.max_grp = c->max_grp;
     a.max_batch = c->max_batch;
     a.sites = c->sites;
@@ -739,6 +751,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     ctx->desc.assign(systems, systems + n_systems);
     const Consts &K = ctx->K;
     std::vector<KVec> kall;
+    std::vector<int> kpk_all;
     std::vector<KCol> call;
     std::vector<KGroup> gall;
     std::vector<KBatch> ball;
@@ -816,7 +829,9 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         std::vector<KGroup> grps;
         std::vector<KBatch> bats;
         enumerate_k(S, kc * kc, kv);
-        build_columns(kv, kord, cols, grps, bats);
+        std::vector<int> kp;
+        build_columns(kv, kord, cols, grps, bats, kp);
+        kpk_all.insert(kpk_all.end(), kp.begin(), kp.end());
         S.n_kvec_ref = (int)kv.size();
         S.n_kvec = (int)kord.size();
         S.kvec_off = (int)kall.size();
@@ -1018,6 +1033,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->sc_scale, ctx->total_slots);
     AL(ctx->noise, ctx->noise_len);
     AL(ctx->kvec, kall.size());
+    AL(ctx->kpk, kpk_all.size());
     AL(ctx->kcol, call.size());
     AL(ctx->kgrp, gall.size());
     AL(ctx->kbatch, ball.size());
@@ -1102,6 +1118,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         cp(ctx->sqrt_mass, sm.data(), sizeof(double) * sm.size());
     }
     cp(ctx->kvec, kall.data(), sizeof(KVec) * kall.size());
+    cp(ctx->kpk, kpk_all.data(), sizeof(int) * kpk_all.size());
     cp(ctx->kcol, call.data(), sizeof(KCol) * call.size());
     cp(ctx->kgrp, gall.data(), sizeof(KGroup) * gall.size());
     cp(ctx->kbatch, ball.data(), sizeof(KBatch) * ball.size());
@@ -1151,7 +1168,7 @@ void qtg_destroy(qtg_ctx *ctx) {
                     ctx->phase, ctx->opos, ctx->part, ctx->skp, ctx->dskp, ctx->wsk, ctx->wdsk, ctx->energy, ctx->energy_aux,
                     ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
-                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket};
+                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->box) cudaFreeHost(ctx->box);

@@ -813,6 +813,117 @@ __global__ void __launch_bounds__(FT) k_kforce(EvalArgs a) {
     if (act) store_plane<R>(a.part, 3 * ((size_t)(a.n_rj + kc) * a.total_sites + J.site_off + i), Fx - Cx, Fy - Cy, Fz - Cz);
 }
 
+// FP32 form of k_kforce<float, 0> with the kz sums rearranged. Per site and
+// column, with A = X(kx) Y(ky) = pr + i pi, Z = Z(|kz|) = zx + i zy and the
+// column's weights W(+kz), W(-kz) (W = 2 c_k S(k)), the value summed above is
+//   vp + vm = pr [zy dx - zx sy] + pi [zx sx + zy dy],
+//   vp - vm = pr [zy sx - zx dy] + pi [zx dx + zy sy],
+// with sx, sy = W(+kz) + W(-kz) and dx, dy = W(+kz) - W(-kz) (x, y: real and
+// imaginary parts). So four per-site sums over |kz| -- U1 = sum (zx sx + zy dy),
+// U2 = sum (zy dx - zx sy), U3 = sum kz (zx dx + zy sy), U4 = sum kz (zy sx - zx dy)
+// -- take eight FMAs per +-kz pair, and A enters once per column:
+// sum v = pi (U1 + W0x) + pr (U2 - W0y), sum kz v = pi U3 + pr U4 (W0: kz = 0).
+// The batch's weights are staged as (sx, dy, dx, sy) and kz (dx, sy, sx, dy);
+// a site's Z(1 .. ZM) stays in registers, its X and Y rows in shared memory.
+template <int ZM>
+__global__ void __launch_bounds__(FT) k_kforce_f32(EvalArgs a) {
+    const int kc = blockIdx.y, jb = blockIdx.z;
+    const Job J = a.jobs[jb];
+    const SysDev &S = a.sys[J.sys];
+    const int nb = S.n_batch, ns = S.n_sites, km1 = S.k_max + 1;
+    if (blockIdx.x * FT >= ns) return;
+    const int i = blockIdx.x * FT + threadIdx.x;
+    const bool act = i < ns;
+    const int ii = act ? i : 0;
+    const int bt0 = chunk_lo(nb, kc, a.n_kc), bt1 = chunk_lo(nb, kc + 1, a.n_kc);
+    __shared__ float4 P1[KB], P2[KB];
+    __shared__ int4 cs[KB];      // kx, ky, m, packed slot of kz = 0
+    __shared__ float2 cb[KB];    // b_x kx, b_y ky
+    extern __shared__ float2 xyrow[];  // [2 km1][FT]: this block's sites' X(0 .. k_max), Y(0 .. k_max)
+    const float2 *ph = reinterpret_cast<const float2 *>(a.phase) + J.phase_off;
+    for (int r = 0; r < 2 * km1; ++r) xyrow[r * FT + threadIdx.x] = ph[(size_t)r * ns + ii];
+    float2 z[ZM];
+#pragma unroll
+    for (int az = 1; az <= ZM; ++az) {
+        z[az - 1] = make_float2(0.f, 0.f);
+        if (act && az < km1) z[az - 1] = ph[(size_t)(2 * km1 + az) * ns + i];
+    }
+    const float bx = (float)(2.0 * PI_REF * S.inv_box[0]), by = (float)(2.0 * PI_REF * S.inv_box[1]),
+                bz = (float)(2.0 * PI_REF * S.inv_box[2]);
+    float Fx = 0.f, Fy = 0.f, Fz = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f;
+    const float2 *wsk = reinterpret_cast<const float2 *>(a.wsk) + J.sk_off;
+    const int *kpk = a.kpk + S.kvec_off;
+    for (int bt = bt0; bt < bt1; ++bt) {
+        const KBatch B = a.kbatch[S.batch_off + bt];
+        const int ncol = B.c1 - B.c0;
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < ncol; idx += FT) {
+            const KCol C = a.kcol[S.col_off + B.c0 + idx];
+            cs[idx] = make_int4(C.kx, C.ky, C.m, kpk[C.k_begin + C.m] >> 8);
+            cb[idx] = make_float2(bx * (float)C.kx, by * (float)C.ky);
+        }
+        for (int idx = threadIdx.x; idx < B.k1 - B.k0; idx += FT) {
+            const int k = B.k0 + idx, code = kpk[k];
+            if (code < 0) continue;
+            const int slot = code >> 8, az = code & 255;
+            const float2 wp = wsk[k];
+            if (az == 0) {
+                P1[slot] = make_float4(wp.x, wp.y, 0.f, 0.f);
+            } else {
+                const float2 wm = wsk[k - 2 * az];
+                const float sx = wp.x + wm.x, sy = wp.y + wm.y, dx = wp.x - wm.x, dy = wp.y - wm.y;
+                const float fa = (float)az;
+                P1[slot] = make_float4(sx, dy, dx, sy);
+                P2[slot] = make_float4(fa * dx, fa * sy, fa * sx, fa * dy);
+            }
+        }
+        __syncthreads();
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        for (int cc = 0; cc < ncol; ++cc) {
+            const int4 C = cs[cc];
+            const float2 x = xyrow[C.x * FT + threadIdx.x];
+            const float2 y = xyrow[(km1 + abs(C.y)) * FT + threadIdx.x];
+            const float yi = C.y < 0 ? -y.y : y.y;
+            const float pr = x.x * y.x - x.y * yi, pi = x.x * yi + x.y * y.x;
+            const float4 w0 = P1[C.w];
+            float u1 = w0.x, u2 = -w0.y, u3 = 0.f, u4 = 0.f;
+#pragma unroll
+            for (int az = 1; az <= ZM; ++az) {
+                if (az > C.z) break;
+                const float4 p1 = P1[C.w + az], p2 = P2[C.w + az];
+                const float zx = z[az - 1].x, zy = z[az - 1].y;
+                u1 = fmaf(zx, p1.x, fmaf(zy, p1.y, u1));
+                u2 = fmaf(zy, p1.z, fmaf(-zx, p1.w, u2));
+                u3 = fmaf(zx, p2.x, fmaf(zy, p2.y, u3));
+                u4 = fmaf(zy, p2.z, fmaf(-zx, p2.w, u4));
+            }
+            const float v = fmaf(pi, u1, pr * u2), vz = fmaf(pi, u3, pr * u4);
+            const float2 b = cb[cc];
+            fx = fmaf(b.x, v, fx);
+            fy = fmaf(b.y, v, fy);
+            fz = fmaf(bz, vz, fz);
+        }
+        kahan_add(Fx, Cx, fx);
+        kahan_add(Fy, Cy, fy);
+        kahan_add(Fz, Cz, fz);
+    }
+    if (act) store_plane<float>(a.part, 3 * ((size_t)(a.n_rj + kc) * a.total_sites + J.site_off + i), Fx - Cx, Fy - Cy, Fz - Cz);
+}
+
+template <typename R>
+size_t kforce_smem(int kmax);
+
+// the FP32 k-force kernel for the largest |kz| of the batch (the general form beyond 32)
+void launch_kforce_f32(const EvalArgs &a, dim3 grid, cudaStream_t s) {
+    const size_t sm = (size_t)2 * (a.max_kmax + 1) * FT * sizeof(float2);
+    if (a.kpk && a.max_kmax <= 8) k_kforce_f32<8><<<grid, FT, sm, s>>>(a);
+    else if (a.kpk && a.max_kmax <= 12) k_kforce_f32<12><<<grid, FT, sm, s>>>(a);
+    else if (a.kpk && a.max_kmax <= 16) k_kforce_f32<16><<<grid, FT, sm, s>>>(a);
+    else if (a.kpk && a.max_kmax <= 24) k_kforce_f32<24><<<grid, FT, sm, s>>>(a);
+    else if (a.kpk && a.max_kmax <= 32) k_kforce_f32<32><<<grid, FT, sm, s>>>(a);
+    else k_kforce<float, 0><<<grid, FT, kforce_smem<float>(a.max_kmax), s>>>(a);
+}
+
 // ---- k_combine: partial sums, short-range terms and the M-site chain rule ---------
 
 // Minimum image of an intramolecular vector. |r / L| is far below 1/2, where
@@ -1400,6 +1511,11 @@ size_t kforce_smem(int kmax) {
 template <typename R>
 void set_attrs() {
     const int big = 200 * 1024;
+    cudaFuncSetAttribute(k_kforce_f32<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_kforce_f32<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_kforce_f32<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_kforce_f32<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_kforce_f32<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_ksk<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_ksk<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_kforce<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
@@ -1453,7 +1569,8 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n) {
         else k_real<R, 0><<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         k_ksk<R, 0><<<dim3(ktiles, a.n_sc, a.n_jobs), KT, ksk_smem<R>(a.max_kmax), s>>>(a);
         k_sk_reduce<R, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
-        k_kforce<R, 0><<<dim3(tiles, a.n_kc, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
+        if (sizeof(R) == 4) launch_kforce_f32(a, dim3(tiles, a.n_kc, a.n_jobs), s);
+        else k_kforce<R, 0><<<dim3(tiles, a.n_kc, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
     } else {
         k_real<R, 1><<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         k_ksk<R, 1><<<dim3(ktiles, a.n_sc, a.n_jobs), KT, ksk_smem<R>(a.max_kmax), s>>>(a);
@@ -1504,7 +1621,7 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
         if (mixed) k_sk_reduce<float, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
         else k_sk_reduce<double, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
     } else if (n == "kforce") {
-        if (mixed) k_kforce<float, 0><<<gf, FT, kforce_smem<float>(a.max_kmax), s>>>(a);
+        if (mixed) launch_kforce_f32(a, gf, s);
         else k_kforce<double, 0><<<gf, FT, kforce_smem<double>(a.max_kmax), s>>>(a);
     } else if (n == "combine") {
         if (mixed) k_combine_f32<<<gm, 128, 0, s>>>(a);
@@ -1564,7 +1681,7 @@ void launch_kwald_only(const EvalArgs &a0, bool mixed, cudaStream_t s, unsigned 
         k_prep<float><<<gs, 128, 0, s>>>(a);
         k_ksk<float, 0><<<gk, KT, ksk_smem<float>(a.max_kmax), s>>>(a);
         k_sk_reduce<float, 0><<<gr, 128, 0, s>>>(a);
-        k_kforce<float, 0><<<gf, FT, kforce_smem<float>(a.max_kmax), s>>>(a);
+        launch_kforce_f32(a, gf, s);
     } else {
         k_prep<double><<<gs, 128, 0, s>>>(a);
         k_ksk<double, 0><<<gk, KT, ksk_smem<double>(a.max_kmax), s>>>(a);

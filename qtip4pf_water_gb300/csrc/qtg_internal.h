@@ -391,6 +391,7 @@ struct EvalArgs {
     const KCol *kcol;
     const KGroup *kgrp;
     const KBatch *kbatch;
+    const int *kpk;        // per k (as kvec): kz >= 0: (packed slot in its force batch) << 8 | kz; kz < 0: -1
     int max_grp, max_batch;
     void *sites;           // 4 reals per site (x, y, z, q), per slot
     void *opos;            // wrapped oxygen positions, 4 reals per molecule, per slot
