@@ -459,7 +459,30 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
             float4 pm = make_float4(0.f, 0.f, 0.f, 0.f);
             if (active && m0 + lane < ns) pm = sites[m0 + lane];
             float mx = 0.f, my = 0.f, mz = 0.f;
-            if (active) {
+            // tiles two or more apart share no molecule (a molecule's three sites lie in
+            // at most two consecutive tiles): between two full tiles every pair counts
+            const bool plain = d >= 2 && (tJ + 1) * 32 <= ns && m0 + 32 <= ns;
+            if (active && plain) {
+#pragma unroll 4
+                for (int r = 0; r < 32; ++r) {
+                    float dx, dy, dz, w;
+                    e += pair(pm, dx, dy, dz, w);
+                    fx = fmaf(w, dx, fx);
+                    fy = fmaf(w, dy, fy);
+                    fz = fmaf(w, dz, fz);
+                    mx = fmaf(-w, dx, mx);
+                    my = fmaf(-w, dy, my);
+                    mz = fmaf(-w, dz, mz);
+                    const int nx = (lane + 1) & 31;
+                    pm.x = __shfl_sync(0xffffffffu, pm.x, nx);
+                    pm.y = __shfl_sync(0xffffffffu, pm.y, nx);
+                    pm.z = __shfl_sync(0xffffffffu, pm.z, nx);
+                    pm.w = __shfl_sync(0xffffffffu, pm.w, nx);
+                    mx = __shfl_sync(0xffffffffu, mx, nx);
+                    my = __shfl_sync(0xffffffffu, my, nx);
+                    mz = __shfl_sync(0xffffffffu, mz, nx);
+                }
+            } else if (active) {
                 for (int r = 0; r < 32; ++r) {
                     const int m = m0 + ((lane + r) & 31);
                     if (vs && m < ns && m / 3 != ms) {
@@ -574,7 +597,7 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
         for (int g = 0; g < KZ; ++g)
 #pragma unroll
             for (int h = 0; h < 2; ++h) sr[g][h] = si[g][h] = dsr[g][h] = dsi[g][h] = (R)0;
-        for (int c = 0; c < nc; ++c) {
+        auto site = [&](int c) {
             const V2<R> x = tab[ax * (CH + 1) + c], y = tab[(km1 + ay) * (CH + 1) + c];
             const R yi = sy * y.y;
             const R pr = x.x * y.x - x.y * yi, pi = x.x * yi + x.y * y.x;
@@ -613,6 +636,12 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
                     dsi[g][1] += kum * erm;
                 }
             }
+        };
+        if (nc == CH) {  // a full chunk: a fixed trip count, unrolled
+#pragma unroll 4
+            for (int c = 0; c < CH; ++c) site(c);
+        } else {
+            for (int c = 0; c < nc; ++c) site(c);
         }
 #pragma unroll
         for (int g = 0; g < KZ; ++g)
