@@ -170,9 +170,33 @@ __global__ void __launch_bounds__(128) k_prep(EvalArgs a) {
     // phase table exp(i 2 pi m frac_d), layout [(d * (kmax+1) + m) * ns + s], by
     // complex recursion from exp(i 2 pi frac_d) (as forces.cpp:233-240 does),
     // reseeded every 4 powers from a directly evaluated phase whose argument
-    // 2 m frac_d is reduced in FP64, so rounding does not accumulate with m
+    // 2 m frac_d is reduced exactly (FP64 tables: in FP64; FP32 tables: in fixed
+    // point), so rounding does not accumulate with m
     const int km1 = S.k_max + 1;
     V2<R> *ph = reinterpret_cast<V2<R> *>(a.phase) + J.phase_off;
+    if (sizeof(R) == 4) {
+        // FP32 tables: frac_d as a 32-bit fixed-point fraction F, so the reseeding
+        // argument 2 m frac_d mod 2 is the wrapped integer product m F, exact,
+        // taken to [-1, 1) as a signed value times 2^-31 (no FP64 per power)
+        for (int d = 0; d < 3; ++d) {
+            const unsigned F = __double2uint_rz(frac[d] * 4294967296.0);
+            float s1, c1;
+            sincospif((float)(int)F * 4.656612873077393e-10f, &s1, &c1);
+            const float qd = (d == 0) ? (float)chg : 1.f;
+            float cr = 1.f, ci = 0.f;
+            for (int m = 0; m < km1; ++m) {
+                if (m > 0 && (m & 3) == 0) sincospif((float)(int)((unsigned)m * F) * 4.656612873077393e-10f, &ci, &cr);
+                V2<R> e;
+                e.x = (R)(cr * qd);
+                e.y = (R)(ci * qd);
+                ph[(size_t)(d * km1 + m) * ns + s] = e;
+                const float nr = cr * c1 - ci * s1;
+                ci = cr * s1 + ci * c1;
+                cr = nr;
+            }
+        }
+        return;
+    }
     for (int d = 0; d < 3; ++d) {
         R s1, c1;
         {
@@ -699,7 +723,18 @@ __global__ void __launch_bounds__(128) k_sk_reduce(EvalArgs a) {
             // order with compensation in FP32; FP64 only for the energy
             const float4 *pk = reinterpret_cast<const float4 *>(a.skp) + J.sk_off + k;
             float xs = 0.f, xc = 0.f, ys = 0.f, yc = 0.f;
-            for (int sc = 0; sc < a.n_sc; ++sc) {
+            int sc = 0;
+            for (; sc + 4 <= a.n_sc; sc += 4) {  // four chunks' loads in flight, then their sums in order
+                float4 p[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) p[u] = pk[(size_t)(sc + u) * a.total_k];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    kahan_add(xs, xc, p[u].x - p[u].z);
+                    kahan_add(ys, yc, p[u].y - p[u].w);
+                }
+            }
+            for (; sc < a.n_sc; ++sc) {
                 const float4 p = pk[(size_t)sc * a.total_k];
                 kahan_add(xs, xc, p.x - p.z);
                 kahan_add(ys, yc, p.y - p.w);
@@ -1105,28 +1140,47 @@ __device__ __forceinline__ float ewald_same_mol_f32(const float *rd, float qiqj,
     return e;
 }
 
+// CMB molecules per 128-thread block: first every thread sums site-force
+// components over the partial planes (one component a thread, plane order,
+// Kahan-compensated: the same sums as one thread per molecule would form, spread
+// over the block), then one thread per molecule adds the short-range terms.
+constexpr int CMB = 32;
 __global__ void __launch_bounds__(128) k_combine_f32(EvalArgs a) {
     const int jb = blockIdx.y;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
     const int N = S.n_mols;
-    if (blockIdx.x * blockDim.x >= N) return;
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m0 = blockIdx.x * CMB;
+    if (m0 >= N) return;
+    const int nm = min(CMB, N - m0);
+    const int m = m0 + threadIdx.x;
     __shared__ double red[4];
+    __shared__ float fsum[CMB * 9];
+    {
+        const int np = a.n_rj + a.n_kc;
+        const size_t stride = 3 * (size_t)a.total_sites;
+        const float *pl = reinterpret_cast<const float *>(a.part) + 3 * ((size_t)J.site_off + 3 * m0);
+        for (int o = threadIdx.x; o < 9 * nm; o += blockDim.x) {
+            float sum = 0.f, comp = 0.f;
+            int p = 0;
+            for (; p + 8 <= np; p += 8) {  // eight planes' loads in flight, then their sums in order
+                float v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) v[u] = pl[(p + u) * stride + o];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) kahan_add(sum, comp, v[u]);
+            }
+            for (; p < np; ++p) kahan_add(sum, comp, pl[p * stride + o]);
+            fsum[o] = sum - comp;
+        }
+    }
+    __syncthreads();
     double e = 0.0;
-    if (m < N) {
+    if ((int)threadIdx.x < nm) {
         const double *q = a.pos + J.pos_off + 9 * m;
         double *f = a.out + J.out_off + 9 * m;
-        float fs[9], cs[9];
-        for (int k = 0; k < 9; ++k) fs[k] = cs[k] = 0.f;
-        {
-            const int np = a.n_rj + a.n_kc;
-            const size_t stride = 3 * (size_t)a.total_sites;
-            const float *pl = reinterpret_cast<const float *>(a.part) + 3 * ((size_t)J.site_off + 3 * m);
-            for (int p = 0; p < np; ++p)
-                for (int k = 0; k < 9; ++k) kahan_add(fs[k], cs[k], pl[p * stride + k]);
-            for (int k = 0; k < 9; ++k) fs[k] -= cs[k];
-        }
+        float fs[9];
+        for (int k = 0; k < 9; ++k) fs[k] = fsum[9 * threadIdx.x + k];
         float fa[9];
         for (int k = 0; k < 9; ++k) fa[k] = 0.f;
         if (J.mode == 0) {
@@ -1607,7 +1661,7 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n) {
         k_kforce<R, 1><<<dim3(tiles, a.n_kc, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
     }
     const dim3 gm((a.max_mols + 127) / 128, a.n_jobs);
-    if (sizeof(R) == 4) k_combine_f32<<<gm, 128, 0, s>>>(a);
+    if (sizeof(R) == 4) k_combine_f32<<<dim3((a.max_mols + CMB - 1) / CMB, a.n_jobs), 128, 0, s>>>(a);
     else k_combine<double><<<gm, 128, 0, s>>>(a);
     if (n) *n += 6;
     if (a.mode == 0) {
@@ -1653,7 +1707,7 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
         if (mixed) launch_kforce_f32(a, gf, s);
         else k_kforce<double, 0><<<gf, FT, kforce_smem<double>(a.max_kmax), s>>>(a);
     } else if (n == "combine") {
-        if (mixed) k_combine_f32<<<gm, 128, 0, s>>>(a);
+        if (mixed) k_combine_f32<<<dim3((a.max_mols + CMB - 1) / CMB, a.n_jobs), 128, 0, s>>>(a);
         else k_combine<double><<<gm, 128, 0, s>>>(a);
     } else if (n == "lj") {
         if (mixed) {
