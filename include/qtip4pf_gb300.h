@@ -142,7 +142,11 @@ qtg_status qtg_get_conserved(qtg_ctx *ctx, int sys, double *q, double *p, const 
  * In QTG_MIXED the Lennard-Jones term of the physical forces runs over every O-O
  * pair inside r_cut (the pairs a valid Verlet list holds), so a mixed Trotter or
  * classical step does not read the caller's point and list; QTG_FP64 steps and
- * the Suzuki-Chin finite-difference terms read them as the reference does. */
+ * the Suzuki-Chin finite-difference terms read them as the reference does.
+ * When q, p, f, (fphys,) disp lie in page-locked host memory the device can
+ * address (cudaHostAlloc / cudaHostRegister without the read-only flag) and do
+ * not overlap, qtg_update_pimd moves them inside its captured step graph (stage
+ * kernels); otherwise by copy calls. Results are the same bits either way. */
 qtg_status qtg_update_class(qtg_ctx *ctx, int sys, double *q, double *p, const double *mass,
                             double *f, const double *charge, int *point, int *list, double *disp,
                             double *energy);
