@@ -209,6 +209,8 @@ struct qtg_ctx {
     // stage-out of arrays that are final early runs beside the later kernels
     cudaStream_t side_stream = nullptr;
     cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join = nullptr;
+    Forks forks{};            // branches of a mixed force evaluation (real | k-space | LJ)
+    float4 *ljf = nullptr;    // dense LJ oxygen forces per molecule and slot
     std::string err;
     Consts K;
     std::vector<qtg_system_desc> desc;
@@ -345,6 +347,7 @@ EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, d
     a.max_batch = c->max_batch;
     a.sites = c->sites;
     a.opos = c->opos;
+    a.ljf = c->ljf;
     a.phase = c->phase;
     a.tan_sites = c->tan_sites;
     a.part = c->part;
@@ -372,7 +375,7 @@ EvalArgs aux_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, do
 }
 
 void launch_eval(qtg_ctx *c, const EvalArgs &a) {
-    if (c->mixed) launch_eval_mixed(a, c->stream, &c->launches);
+    if (c->mixed) launch_eval_mixed(a, c->stream, &c->launches, &c->forks);
     else launch_eval_fp64(a, c->stream, &c->launches);
 }
 
@@ -1007,6 +1010,9 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking);
     for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&ctx->ev_fork[k], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaStreamCreateWithFlags(&ctx->forks.side[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->forks.fork, cudaEventDisableTiming);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&ctx->forks.join[k], cudaEventDisableTiming);
 #define AL(ptr, n)                                  \
     if (e == cudaSuccess) e = dalloc(&(ptr), (n));
     AL(ctx->sys_d, n_systems);
@@ -1056,6 +1062,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         AL(tmp, 4 * (ctx->total_sites / 3));
         ctx->opos = tmp;
     }
+    AL(ctx->ljf, ctx->total_sites / 3);
     AL(ctx->part, (size_t)MAX_PART * 3 * ctx->total_sites);
     AL(ctx->skp, (size_t)MAX_SC * ctx->total_k);
     AL(ctx->dskp, (size_t)MAX_SC * ctx->total_k);
@@ -1168,7 +1175,7 @@ void qtg_destroy(qtg_ctx *ctx) {
                     ctx->phase, ctx->opos, ctx->part, ctx->skp, ctx->dskp, ctx->wsk, ctx->wdsk, ctx->energy, ctx->energy_aux,
                     ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
-                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk};
+                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->box) cudaFreeHost(ctx->box);
@@ -1176,8 +1183,11 @@ void qtg_destroy(qtg_ctx *ctx) {
     for (auto &g : ctx->call_graphs) cudaGraphExecDestroy(g.second.first);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
-    for (cudaEvent_t ev : {ctx->ev_fork[0], ctx->ev_fork[1], ctx->ev_join})
+    for (cudaEvent_t ev : {ctx->ev_fork[0], ctx->ev_fork[1], ctx->ev_join, ctx->forks.fork, ctx->forks.join[0],
+                           ctx->forks.join[1]})
         if (ev) cudaEventDestroy(ev);
+    for (cudaStream_t st : {ctx->forks.side[0], ctx->forks.side[1]})
+        if (st) cudaStreamDestroy(st);
     delete ctx;
 }
 

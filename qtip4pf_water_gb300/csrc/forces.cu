@@ -1259,10 +1259,18 @@ __global__ void __launch_bounds__(128) k_combine_f32(EvalArgs a) {
                 }
             }
         }
-        // M-site chain rule (forces.cpp:613-619)
+        // M-site chain rule (forces.cpp:613-619); the dense Lennard-Jones force of a
+        // forked evaluation joins the oxygen here
         const float g = (float)a.c.gamma_vs, h = 0.5f * (1.0f - g);
+        float lj[3] = {0.f, 0.f, 0.f};
+        if (a.lj_plane && J.mode == 0) {
+            const float4 l = a.ljf[J.site_off / 3 + m];
+            lj[0] = l.x;
+            lj[1] = l.y;
+            lj[2] = l.z;
+        }
         for (int d = 0; d < 3; ++d) {
-            f[d] = (double)(fa[d] + g * fs[d]);
+            f[d] = (double)(fa[d] + g * fs[d]) + (double)lj[d];
             f[3 + d] = (double)(fa[3 + d] + fs[3 + d] + h * fs[d]);
             f[6 + d] = (double)(fa[6 + d] + fs[6 + d] + h * fs[d]);
         }
@@ -1543,10 +1551,14 @@ __global__ void __launch_bounds__(128) k_lj_dense(EvalArgs a) {
     }
     double e = 0.0;
     if (act && sub == 0) {
-        double *f = a.out + J.out_off;
-        f[9 * i] += (double)fx;
-        f[9 * i + 1] += (double)fy;
-        f[9 * i + 2] += (double)fz;
+        if (a.lj_plane) {
+            a.ljf[J.site_off / 3 + i] = make_float4(fx, fy, fz, 0.f);
+        } else {
+            double *f = a.out + J.out_off;
+            f[9 * i] += (double)fx;
+            f[9 * i + 1] += (double)fy;
+            f[9 * i + 2] += (double)fz;
+        }
         e = 0.5 * (double)el;
     }
     const double t = block_sum(e, red);
@@ -1639,12 +1651,34 @@ void launch_real_half(EvalArgs &a, cudaStream_t s) {
 }
 
 template <typename R>
-void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n) {
+void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks *forks = nullptr) {
     const int ns = 3 * a.max_mols;
     const int tiles = (ns + RT - 1) / RT, ktiles = (a.max_grp + KT - 1) / KT;
     a.n_rj = chunks_or(a.tune_rj, (long long)tiles * a.n_jobs, MAX_RJ);
     a.n_sc = chunks_or(a.tune_sc, (long long)ktiles * a.n_jobs, MAX_SC);
     a.n_kc = chunks_or(a.tune_kc, (long long)tiles * a.n_jobs, MAX_KC);
+    if (sizeof(R) == 4 && forks && a.mode == 0 && a.lj_full && a.ljf) {
+        // forked: prep; then real space | reciprocal chain | dense LJ; then combine
+        if (half_ok(a)) a.n_rj = half_chunks(a) + (3 * a.max_mols + 31) / 32 / 2;
+        a.lj_plane = 1;
+        k_prep<R><<<dim3((ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
+        cudaEventRecord(forks->fork, s);
+        cudaStreamWaitEvent(forks->side[0], forks->fork, 0);
+        cudaStreamWaitEvent(forks->side[1], forks->fork, 0);
+        k_ksk<R, 0><<<dim3(ktiles, a.n_sc, a.n_jobs), KT, ksk_smem<R>(a.max_kmax), forks->side[0]>>>(a);
+        k_sk_reduce<R, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, forks->side[0]>>>(a);
+        launch_kforce_f32(a, dim3(tiles, a.n_kc, a.n_jobs), forks->side[0]);
+        cudaEventRecord(forks->join[0], forks->side[0]);
+        launch_lj_dense(a, forks->side[1]);
+        cudaEventRecord(forks->join[1], forks->side[1]);
+        if (half_ok(a)) launch_real_half(a, s);
+        else k_real_f32<<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
+        cudaStreamWaitEvent(s, forks->join[0], 0);
+        cudaStreamWaitEvent(s, forks->join[1], 0);
+        k_combine_f32<<<dim3((a.max_mols + CMB - 1) / CMB, a.n_jobs), 128, 0, s>>>(a);
+        if (n) *n += 7;
+        return;
+    }
     k_prep<R><<<dim3((ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
     if (a.mode == 0) {
         if (sizeof(R) == 4 && half_ok(a)) launch_real_half(a, s);
@@ -1739,13 +1773,13 @@ void launch_eval_fp64(const EvalArgs &a, cudaStream_t s, unsigned long long *n) 
     if (n) *n += 2;
 }
 
-void launch_eval_mixed(const EvalArgs &a, cudaStream_t s, unsigned long long *n) {
+void launch_eval_mixed(const EvalArgs &a, cudaStream_t s, unsigned long long *n, const Forks *forks) {
     if (a.n_jobs <= 0) return;
     if (a.sr_only) {
         launch_eval_fp64(a, s, n);  // the finite-difference short-range terms stay FP64
         return;
     }
-    launch_ewald<float>(a, s, n);
+    launch_ewald<float>(a, s, n, forks);
 }
 
 // Reciprocal space only, on caller-supplied charge sites: out (site forces,

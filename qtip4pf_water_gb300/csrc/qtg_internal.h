@@ -395,6 +395,8 @@ struct EvalArgs {
     int max_grp, max_batch;
     void *sites;           // 4 reals per site (x, y, z, q), per slot
     void *opos;            // wrapped oxygen positions, 4 reals per molecule, per slot
+    float4 *ljf;           // dense Lennard-Jones oxygen forces, per molecule, per slot (lj_plane)
+    int lj_plane;          // 1: k_lj_dense writes ljf and k_combine_f32 adds it to the O force
     void *phase;           // complex phase tables, per slot
     void *tan_sites;       // tangent of the site positions (mode 1), per slot
     double *part;          // partial site forces [MAX_PART][total_sites][3]
@@ -440,7 +442,16 @@ void launch_fp32_probe(float *out, int blocks, int iters, cudaStream_t s);
 
 // forces.cu
 void launch_eval_fp64(const EvalArgs &a, cudaStream_t s, unsigned long long *launches);
-void launch_eval_mixed(const EvalArgs &a, cudaStream_t s, unsigned long long *launches);
+// Side streams and events for a forked mixed evaluation: after k_prep, the
+// reciprocal-space chain (k_ksk, k_sk_reduce, k_kforce_f32) runs on side[0] and
+// the dense Lennard-Jones on side[1] beside the real-space kernel; both join
+// before k_combine_f32. (Captured into a graph, these become parallel branches.)
+struct Forks {
+    cudaStream_t side[2];
+    cudaEvent_t fork, join[2];
+};
+void launch_eval_mixed(const EvalArgs &a, cudaStream_t s, unsigned long long *launches,
+                       const Forks *forks = nullptr);
 void launch_kwald_only(const EvalArgs &a, bool mixed, cudaStream_t s, unsigned long long *launches);
 
 // one-time kernel attribute set-up (shared-memory limits); called at context creation
