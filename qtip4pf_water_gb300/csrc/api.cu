@@ -489,6 +489,14 @@ void enqueue_forces(qtg_ctx *c, int sys, bool force_sc) {
     const int full = sys < 0 ? 1 : 0;
     EvalArgs base = eval_args(c, c->base.d + jb, nj, c->q, c->fphys, 0, 0);
     base.lj_full = (full || c->mixed) ? 1 : 0;
+    // mixed, second-order assembly for every system in the evaluation: the combine
+    // writes the propagating force too, and the assembly kernel is not launched
+    bool all_trotter = c->mixed && !force_sc;
+    for (int k = (sys < 0 ? 0 : sys); all_trotter && k < (sys < 0 ? c->n_sys : sys + 1); ++k)
+        all_trotter = c->sys_h[k].propagator != QTG_SUZUKI_CHIN;
+    for (const auto &g : c->surrogates)  // a learned correction is added to fphys after the combine
+        if (sys < 0 || g.sys == sys) all_trotter = false;
+    if (all_trotter) base.out_prop = c->f;
     launch_eval(c, base);
     // learned centroid corrections of the systems that carry one (P = 1)
     for (const auto &g : c->surrogates) {
@@ -555,7 +563,7 @@ void enqueue_forces(qtg_ctx *c, int sys, bool force_sc) {
     sa.job_sys = c->base_sys + jb;
     sa.job_bead = c->base_bead + jb;
     sa.n_jobs = nj;
-    launch_sc_finish(sa, c->stream, &c->launches);
+    if (!all_trotter) launch_sc_finish(sa, c->stream, &c->launches);
 }
 
 void enqueue_step(qtg_ctx *c, int sys, int nvt, int ext_noise, bool pile_g) {

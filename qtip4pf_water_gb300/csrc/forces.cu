@@ -1269,10 +1269,19 @@ __global__ void __launch_bounds__(128) k_combine_f32(EvalArgs a) {
             lj[1] = l.y;
             lj[2] = l.z;
         }
+        double *f2 = a.out_prop ? a.out_prop + J.out_off + 9 * m : nullptr;
         for (int d = 0; d < 3; ++d) {
-            f[d] = (double)(fa[d] + g * fs[d]) + (double)lj[d];
-            f[3 + d] = (double)(fa[3 + d] + fs[3 + d] + h * fs[d]);
-            f[6 + d] = (double)(fa[6 + d] + fs[6 + d] + h * fs[d]);
+            const double fo = (double)(fa[d] + g * fs[d]) + (double)lj[d];
+            const double f1 = (double)(fa[3 + d] + fs[3 + d] + h * fs[d]);
+            const double f2v = (double)(fa[6 + d] + fs[6 + d] + h * fs[d]);
+            f[d] = fo;
+            f[3 + d] = f1;
+            f[6 + d] = f2v;
+            if (f2) {
+                f2[d] = fo;
+                f2[3 + d] = f1;
+                f2[6 + d] = f2v;
+            }
         }
     }
     if (J.mode == 0) {
@@ -1695,10 +1704,17 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
         k_kforce<R, 1><<<dim3(tiles, a.n_kc, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
     }
     const dim3 gm((a.max_mols + 127) / 128, a.n_jobs);
+    // mixed with the dense Lennard-Jones: its oxygen forces go to their plane first,
+    // so the combine writes the complete force
+    const bool plane = sizeof(R) == 4 && a.mode == 0 && a.lj_full && a.ljf;
+    if (plane) {
+        a.lj_plane = 1;
+        launch_lj_dense(a, s);
+    }
     if (sizeof(R) == 4) k_combine_f32<<<dim3((a.max_mols + CMB - 1) / CMB, a.n_jobs), 128, 0, s>>>(a);
     else k_combine<double><<<gm, 128, 0, s>>>(a);
-    if (n) *n += 6;
-    if (a.mode == 0) {
+    if (n) *n += plane ? 7 : 6;
+    if (a.mode == 0 && !plane) {
         if (sizeof(R) == 4 && a.lj_full)
             launch_lj_dense(a, s);
         else if (a.lj_full) k_lj<R, 1><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);

@@ -382,6 +382,8 @@ struct EvalArgs {
     int max_kmax;
     const double *pos;     // position base (jobs' pos_off are relative to it)
     double *out;           // force output base
+    double *out_prop;      // mixed, optional: the same forces also written here (the propagating
+                           // force of Trotter / classical systems, saving the assembly copy)
     const double *dir;     // tangent direction base (mode 1 jobs), same offsets as pos
     const double *charge;
     const int *point, *list;
