@@ -566,6 +566,17 @@ void enqueue_forces(qtg_ctx *c, int sys, bool force_sc) {
     if (!all_trotter) launch_sc_finish(sa, c->stream, &c->launches);
 }
 
+// Whether the Verlet-list rebuild of a step can run beside its force evaluation:
+// nothing in a mixed second-order evaluation reads the lists (the dense
+// Lennard-Jones takes every pair inside r_cut); FP64 evaluations and the
+// Suzuki-Chin finite-difference terms do.
+bool rebuild_beside_forces(const qtg_ctx *c, int sys) {
+    if (!c->mixed) return false;
+    for (int k = (sys < 0 ? 0 : sys); k < (sys < 0 ? c->n_sys : sys + 1); ++k)
+        if (c->sys_h[k].propagator == QTG_SUZUKI_CHIN) return false;
+    return true;
+}
+
 void enqueue_step(qtg_ctx *c, int sys, int nvt, int ext_noise, bool pile_g) {
     RingArgs r = ring_args(c, sys, RF_KICK | RF_FWD | RF_CAYLEY | RF_BACK | RF_DISP | (nvt ? RF_THERMO : 0));
     r.noise = ext_noise ? c->noise : nullptr;
@@ -577,8 +588,17 @@ void enqueue_step(qtg_ctx *c, int sys, int nvt, int ext_noise, bool pile_g) {
     launch_ring(r, c->stream, &c->launches);
     const int jb = sys < 0 ? 0 : c->sys_h[sys].job_base;
     const int nj = sys < 0 ? (int)c->base.h.size() : c->sys_h[sys].n_beads;
-    launch_skin_rebuild(list_args(c, jb, nj, 0), c->stream, &c->launches);
+    const bool beside = rebuild_beside_forces(c, sys);
+    if (beside) {  // on the side stream, joined before the closing kick
+        cudaEventRecord(c->ev_fork[0], c->stream);
+        cudaStreamWaitEvent(c->side_stream, c->ev_fork[0], 0);
+        launch_skin_rebuild(list_args(c, jb, nj, 0), c->side_stream, &c->launches);
+        cudaEventRecord(c->ev_join, c->side_stream);
+    } else {
+        launch_skin_rebuild(list_args(c, jb, nj, 0), c->stream, &c->launches);
+    }
     enqueue_forces(c, sys, false);
+    if (beside) cudaStreamWaitEvent(c->stream, c->ev_join, 0);
     RingArgs e = ring_args(c, sys, 0);
     e.kick = 1;
     launch_end_step(e, c->stream, &c->launches);
@@ -1785,27 +1805,45 @@ qtg_status qtg_update_pimd(qtg_ctx *ctx, int sys, double *q, double *p, const do
         r.n_draw = noise ? 0 : 1;
         r.draw_sys0 = sys;
         launch_ring(r, ctx->stream, &ctx->launches);
-        launch_skin_rebuild(list_args(ctx, S.job_base, S.n_beads, 0), ctx->stream, &ctx->launches);
-        // staged: q and disp are final here, f and fphys after the forces; each goes
-        // back on the side stream beside the kernels that follow
-        auto side = [&](int k, unsigned mask) {
+        if (err == cudaSuccess) err = cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream);
+        // the rebuild runs on the side stream beside the forces where they do not
+        // read the lists; staged, q and disp go back after it on that stream (both
+        // final there), f and fphys after the forces, each beside the kernels that follow
+        const bool beside = rebuild_beside_forces(ctx, sys);
+        auto fork = [&](int k) {
             if (err == cudaSuccess) err = cudaEventRecord(ctx->ev_fork[k], ctx->stream);
             if (err == cudaSuccess) err = cudaStreamWaitEvent(ctx->side_stream, ctx->ev_fork[k], 0);
+        };
+        auto stage_out_side = [&](unsigned mask) {
             StageArgs so = sg;
             so.mask = mask;
             so.blocks = std::min(sg.blocks, 2 * ctx->n_sm);
             launch_stage_out(so, ctx->side_stream, &ctx->launches);
         };
-        if (staged) side(0, STAGE_Q | STAGE_DISP);
-        if (err == cudaSuccess) err = cudaMemsetAsync(ctx->acc + sys, 0, sizeof(SysAcc), ctx->stream);
+        if (beside) {
+            fork(0);
+            launch_skin_rebuild(list_args(ctx, S.job_base, S.n_beads, 0), ctx->side_stream, &ctx->launches);
+            if (staged) stage_out_side(STAGE_Q | STAGE_DISP);
+        } else {
+            launch_skin_rebuild(list_args(ctx, S.job_base, S.n_beads, 0), ctx->stream, &ctx->launches);
+            if (staged) {
+                fork(0);
+                stage_out_side(STAGE_Q | STAGE_DISP);
+            }
+        }
         enqueue_forces(ctx, sys, false);
-        if (staged) side(1, STAGE_F | STAGE_FPHYS);
+        if (staged) {
+            fork(1);
+            stage_out_side(STAGE_F | STAGE_FPHYS);
+        }
         RingArgs e = ring_args(ctx, sys, 0);
         e.kick = 1;
         launch_end_step(e, ctx->stream, &ctx->launches);
-        if (staged) {
+        if (staged || beside) {
             if (err == cudaSuccess) err = cudaEventRecord(ctx->ev_join, ctx->side_stream);
             if (err == cudaSuccess) err = cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0);
+        }
+        if (staged) {
             StageArgs so = sg;
             so.mask = STAGE_P | STAGE_SMALL;
             launch_stage_out(so, ctx->stream, &ctx->launches);
