@@ -94,8 +94,8 @@ def load(build_if_missing: bool = True):
         "qtg_pile_g": ([V, C.c_int, D, D, D, D], C.c_int),
         "qtg_get_kcv": ([V, C.c_int, D, D, D], C.c_int),
         "qtg_get_conserved": ([V, C.c_int, D, D, D, C.c_double, D], C.c_int),
-        "qtg_update_class": ([V, C.c_int, D, D, D, D, D, I, I, D, D], C.c_int),
-        "qtg_update_pimd": ([V, C.c_int, D, D, D, D, D, D, I, I, D, C.c_int, D, D, D, D], C.c_int),
+        "qtg_update_class": ([V, C.c_int, V, V, V, V, V, V, V, V, D], C.c_int),
+        "qtg_update_pimd": ([V, C.c_int, V, V, V, V, V, V, V, V, V, C.c_int, V, D, D, D], C.c_int),
         "qtg_set_state": ([V, C.c_int, D, D], C.c_int),
         "qtg_get_state": ([V, C.c_int, D, D, D, D, D], C.c_int),
         "qtg_init_forces": ([V], C.c_int),
@@ -142,6 +142,25 @@ def _i(a):
     if a.dtype != np.int32 or not a.flags.c_contiguous:
         raise TypeError("index arrays must be C-contiguous int32")
     return a.ctypes.data_as(I)
+
+
+_F64, _I32 = np.dtype(np.float64), np.dtype(np.int32)
+
+
+def _vd(a):
+    """Address of a C-contiguous float64 array as a plain integer (the per-step
+    entries take void pointers: cheaper to pass than typed ctypes pointers)."""
+    if a is None:
+        return None
+    if a.dtype != _F64 or not a.flags.c_contiguous:
+        raise TypeError("arrays must be C-contiguous float64")
+    return a.ctypes.data
+
+
+def _vi(a):
+    if a.dtype != _I32 or not a.flags.c_contiguous:
+        raise TypeError("index arrays must be C-contiguous int32")
+    return a.ctypes.data
 
 
 class Context:
@@ -384,16 +403,16 @@ class System:
 
     def update_trajectory_class_nospline(self, q, p, mass, f, charge, point, lst, disp):
         e = C.c_double(0.0)
-        self._c(self.ctx.L.qtg_update_class(self.ctx.h, self.idx, _d(q), _d(p), _d(mass), _d(f), _d(charge),
-                                            _i(point), _i(lst), _d(disp), C.byref(e)))
+        self._c(self.ctx.L.qtg_update_class(self.ctx.h, self.idx, _vd(q), _vd(p), _vd(mass), _vd(f), _vd(charge),
+                                            _vi(point), _vi(lst), _vd(disp), C.byref(e)))
         return e.value
 
     def update_sc_nospline(self, q, p, mass, f, fphys, charge, point, lst, disp, is_nvt, heat, noise=None):
         """One ring-polymer step (update.cpp:271-401). Returns (energy, heat, potential estimator)."""
         h, pot, e = C.c_double(heat), C.c_double(0.0), C.c_double(0.0)
-        self._c(self.ctx.L.qtg_update_pimd(self.ctx.h, self.idx, _d(q), _d(p), _d(mass), _d(f), _d(fphys),
-                                           _d(charge), _i(point), _i(lst), _d(disp), 1 if is_nvt else 0,
-                                           _d(noise), C.byref(h), C.byref(pot), C.byref(e)))
+        self._c(self.ctx.L.qtg_update_pimd(self.ctx.h, self.idx, _vd(q), _vd(p), _vd(mass), _vd(f), _vd(fphys),
+                                           _vd(charge), _vi(point), _vi(lst), _vd(disp), 1 if is_nvt else 0,
+                                           _vd(noise), C.byref(h), C.byref(pot), C.byref(e)))
         return e.value, h.value, pot.value
 
     # ---- tier 2: device-resident state -------------------------------------------------
