@@ -270,6 +270,7 @@ struct qtg_ctx {
     ColWork *colwork = nullptr;
     int n_colwork = 0;
     double *cw_part = nullptr;    // [n_colwork][4] block partials of the ordered system sums
+    unsigned *fin_ticket = nullptr;  // systems closed by a fused end step
     unsigned *cw_ticket = nullptr;  // [n_sys] arrival tickets of those sums
     // run state
     SysAcc *acc = nullptr;
@@ -599,14 +600,18 @@ void enqueue_step(qtg_ctx *c, int sys, int nvt, int ext_noise, bool pile_g) {
     }
     enqueue_forces(c, sys, false);
     if (beside) cudaStreamWaitEvent(c->stream, c->ev_join, 0);
-    RingArgs e = ring_args(c, sys, 0);
-    e.kick = 1;
-    launch_end_step(e, c->stream, &c->launches);
     FinalizeArgs fa = fin_args(c, sys, 1, nvt);
     fa.noise = nullptr;
     fa.pile_g = pile_g ? 1 : 0;
     fa.pre_drawn = ahead ? 1 : 0;
-    launch_finalize(fa, c->stream, &c->launches);
+    RingArgs e = ring_args(c, sys, 0);
+    e.kick = 1;
+    // the step's close (estimator record, next centroid factor, counters) runs in
+    // the end step's block that finishes each system
+    e.fuse_fin = 1;
+    e.fin = fa;
+    e.fin.ticket = c->fin_ticket;
+    launch_end_step(e, c->stream, &c->launches);
 }
 
 qtg_status check_sys(qtg_ctx *ctx, int sys) {
@@ -1129,6 +1134,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->colwork, cw.size());
     AL(ctx->cw_part, 4 * cw.size());
     AL(ctx->cw_ticket, n_systems);
+    AL(ctx->fin_ticket, 1);
     AL(ctx->acc, n_systems);
     AL(ctx->run, n_systems);
     AL(ctx->est, (size_t)ctx->max_records * n_systems * 8);
@@ -1203,7 +1209,7 @@ void qtg_destroy(qtg_ctx *ctx) {
                     ctx->phase, ctx->opos, ctx->part, ctx->skp, ctx->dskp, ctx->wsk, ctx->wdsk, ctx->energy, ctx->energy_aux,
                     ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
-                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf};
+                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf, ctx->fin_ticket};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->box) cudaFreeHost(ctx->box);

@@ -281,6 +281,8 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
 }
 
 // Closing kick and the per-step estimator partial sums (bead space).
+__device__ void finalize_system(const FinalizeArgs &a, int s, unsigned long long st, unsigned long long rec);
+
 __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
     const ColWork W = a.work[blockIdx.x];
     const SysDev &S = a.sys[W.sys];
@@ -363,7 +365,25 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
     // the blocks' sums go to the system's accumulators in slot order
     SysAcc *ac = &a.acc[W.sys];
     double *const dst[4] = {&ac->kin, &ac->spring, &ac->kcv_tq, &ac->k0};
-    ordered_system_sum<4>(bsum, W.slot, S.cw_begin, S.cw_count, a.cw_part, a.cw_ticket + W.sys, dst);
+    // the step counters as they stand while this step runs (only the block that
+    // finishes the last system advances them, after every system's close below)
+    const unsigned long long st0 = a.fuse_fin ? *a.fin.step : 0ull, rec0 = a.fuse_fin ? *a.fin.records : 0ull;
+    const bool last = ordered_system_sum<4>(bsum, W.slot, S.cw_begin, S.cw_count, a.cw_part, a.cw_ticket + W.sys, dst);
+    // fused close of the step: the block that completed a system's sums records it
+    // and sets its next centroid factor; the last system to finish advances the
+    // step and record counters, as k_finalize would after every system
+    if (last && a.fuse_fin && threadIdx.x < 32) {
+        __syncwarp();
+        finalize_system(a.fin, W.sys, st0, rec0);
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(a.fin.ticket, 1u) == (unsigned)(a.fin.sys_end - a.fin.sys_begin - 1)) {
+                if (a.fin.record) *a.fin.records = rec0 + 1;
+                *a.fin.step = st0 + 1;
+                *a.fin.ticket = 0u;
+            }
+        }
+    }
 }
 
 // Centroid normal-mode kinetic energy of normal-mode momenta (row 0 of p).
@@ -476,63 +496,69 @@ __global__ void __launch_bounds__(256) k_centroid_alpha(RingArgs a, int sys) {
     }
 }
 
-// One warp per system: the step's estimator record and the next centroid
-// draw for PILE-G. One block, so the step counters advance after every system.
+// One system's step close (called by a whole warp): the estimator record
+// (lane 0) and the next PILE-G centroid factor, then the step accumulators
+// cleared. st, rec: the step and record counters at the start of the step.
+__device__ void finalize_system(const FinalizeArgs &a, int s, unsigned long long st, unsigned long long rec) {
+    const int lane = threadIdx.x & 31;
+    const SysDev &S = a.sys[s];
+    SysAcc *ac = &a.acc[s];
+    SysRun *run = &a.run[s];
+    const int P = S.n_beads;
+    if (a.record && lane == 0) {
+        double vsum = 0.0, veven = 0.0;
+        for (int b = 0; b < P; ++b) {
+            const double e = a.energy[S.job_base + b];
+            vsum += e;
+            if (b % 2 == 0) veven += e;
+        }
+        double vtot, pot, kcv;
+        const double half_nd_beta = 0.5 * S.n_dof / S.beta;
+        if (S.propagator == 0) {  // Suzuki-Chin (forces.cpp:724-781, path_integrals.cpp:29-48)
+            vtot = (2.0 * veven + 4.0 * (vsum - veven) + ac->sc_extra) / 3.0;
+            pot = 2.0 * veven / P;
+            kcv = half_nd_beta + ac->kcv_tq / P;
+        } else {
+            vtot = vsum;
+            pot = vsum / P;
+            kcv = half_nd_beta + ac->kcv_tq / (2.0 * P);
+        }
+        const double cons = vtot + ac->kin + ac->spring + run->heat;
+        double *o = a.est + ((size_t)(rec % (unsigned long long)a.max_records) * a.n_sys + s) * 8;
+        o[0] = pot;
+        o[1] = kcv;
+        o[2] = cons;
+        o[3] = run->heat;
+        o[4] = ac->kin;
+        o[5] = vtot;
+        o[6] = ac->rebuilds;
+        o[7] = (double)st;
+        if (!isfinite(cons) || !isfinite(vtot)) atomicOr(a.status, (unsigned)ST_NONFINITE);
+    }
+    if (a.draw_alpha && (S.thermostat == 1 || a.pile_g)) {
+        double R, g2;
+        if (a.noise && s == 0) {
+            R = a.noise[0];
+            g2 = a.noise[1];
+        } else if (a.pre_drawn) {
+            R = run->R_draw;
+            g2 = run->g2_draw;
+        } else {
+            centroid_draw(S, s, st, &R, &g2, a.status);
+        }
+        if (lane == 0) run->alpha = sqrt((R * R + g2) / (2.0 * S.beta_n * ac->k0));
+    }
+    __syncwarp();
+    if (lane == 0) ac->kin = ac->spring = ac->kcv_tq = ac->k0 = ac->sc_extra = ac->rebuilds = 0.0;
+}
+
+// One warp per system: finalize_system for every system. One block, so the step
+// counters advance after every system.
 __global__ void k_finalize(FinalizeArgs a) {
     const unsigned long long st = *a.step;
     const unsigned long long rec = *a.records;
-    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int s = a.sys_begin + (int)(threadIdx.x >> 5); s < a.sys_end; s += nw) {
-        const SysDev &S = a.sys[s];
-        SysAcc *ac = &a.acc[s];
-        SysRun *run = &a.run[s];
-        const int P = S.n_beads;
-        if (a.record && lane == 0) {
-            double vsum = 0.0, veven = 0.0;
-            for (int b = 0; b < P; ++b) {
-                const double e = a.energy[S.job_base + b];
-                vsum += e;
-                if (b % 2 == 0) veven += e;
-            }
-            double vtot, pot, kcv;
-            const double half_nd_beta = 0.5 * S.n_dof / S.beta;
-            if (S.propagator == 0) {  // Suzuki-Chin (forces.cpp:724-781, path_integrals.cpp:29-48)
-                vtot = (2.0 * veven + 4.0 * (vsum - veven) + ac->sc_extra) / 3.0;
-                pot = 2.0 * veven / P;
-                kcv = half_nd_beta + ac->kcv_tq / P;
-            } else {
-                vtot = vsum;
-                pot = vsum / P;
-                kcv = half_nd_beta + ac->kcv_tq / (2.0 * P);
-            }
-            const double cons = vtot + ac->kin + ac->spring + run->heat;
-            double *o = a.est + ((size_t)(rec % (unsigned long long)a.max_records) * a.n_sys + s) * 8;
-            o[0] = pot;
-            o[1] = kcv;
-            o[2] = cons;
-            o[3] = run->heat;
-            o[4] = ac->kin;
-            o[5] = vtot;
-            o[6] = ac->rebuilds;
-            o[7] = (double)st;
-            if (!isfinite(cons) || !isfinite(vtot)) atomicOr(a.status, (unsigned)ST_NONFINITE);
-        }
-        if (a.draw_alpha && (S.thermostat == 1 || a.pile_g)) {
-            double R, g2;
-            if (a.noise && s == 0) {
-                R = a.noise[0];
-                g2 = a.noise[1];
-            } else if (a.pre_drawn) {
-                R = run->R_draw;
-                g2 = run->g2_draw;
-            } else {
-                centroid_draw(S, s, st, &R, &g2, a.status);
-            }
-            if (lane == 0) run->alpha = sqrt((R * R + g2) / (2.0 * S.beta_n * ac->k0));
-        }
-        __syncwarp();
-        if (lane == 0) ac->kin = ac->spring = ac->kcv_tq = ac->k0 = ac->sc_extra = ac->rebuilds = 0.0;
-    }
+    const int nw = blockDim.x >> 5;
+    for (int s = a.sys_begin + (int)(threadIdx.x >> 5); s < a.sys_end; s += nw) finalize_system(a, s, st, rec);
     __syncthreads();
     if (threadIdx.x == 0) {
         if (a.record) *a.records = rec + 1;

@@ -160,8 +160,9 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 // order (thread t the slots t, t + blockDim.x, ..., all NV values at once, then a
 // fixed shuffle-and-shared-memory tree), adds the NV totals to dst[k] and re-arms
 // the ticket. The totals therefore do not depend on the order the blocks ran in.
+// Returns true in that last block (the totals are visible to its warp 0).
 template <int NV>
-__device__ void ordered_system_sum(const double *v, int slot, int cw_begin, int cw_count, double *part,
+__device__ bool ordered_system_sum(const double *v, int slot, int cw_begin, int cw_count, double *part,
                                    unsigned *ticket, double *const *dst) {
     __shared__ int last;
     __shared__ double red[NV][32];
@@ -171,7 +172,7 @@ __device__ void ordered_system_sum(const double *v, int slot, int cw_begin, int 
         last = atomicAdd(ticket, 1u) == (unsigned)(cw_count - 1);
     }
     __syncthreads();
-    if (!last) return;
+    if (!last) return false;
     __threadfence();
     double t[NV];
 #pragma unroll
@@ -196,6 +197,7 @@ __device__ void ordered_system_sum(const double *v, int slot, int cw_begin, int 
         }
         if (lane == 0) *ticket = 0u;
     }
+    return true;
 }
 
 // Philox4x32-10 counter-based generator (Salmon, Moraes, Dror & Shaw,
@@ -269,6 +271,26 @@ enum RingFlags : int {
     RF_VV = 64,     // classical velocity-Verlet drift q += dt p / m (P = 1)
 };
 
+struct FinalizeArgs {
+    const SysDev *sys;
+    int n_sys;
+    const double *energy;    // base-job energies (job_base + bead)
+    SysAcc *acc;
+    SysRun *run;
+    double *est;             // ring buffer [max_records][n_sys][8]
+    int max_records;
+    unsigned long long *step;
+    unsigned long long *records;
+    unsigned *status;
+    const double *noise;     // optional caller noise for the centroid draw (system 0 only)
+    int record;              // 1: write an estimator record and count a step
+    int draw_alpha;          // 1: draw the next PILE-G centroid factor
+    int sys_begin, sys_end;  // systems handled
+    int pile_g;              // 1: draw alpha whatever the system's thermostat
+    int pre_drawn;           // 1: this step's k_ring already made the centroid draws (SysRun)
+    unsigned *ticket;        // fused into k_end_step: systems finished (the last advances the counters)
+};
+
 struct RingArgs {
     const SysDev *sys;
     const ColWork *work;
@@ -296,6 +318,8 @@ struct RingArgs {
     unsigned *status;        // ring draw blocks: ST_GAMMA_LIMIT
     double *cw_part;         // per column-work slot: block partials of the system sums (4 doubles)
     unsigned *cw_ticket;     // per system: blocks arrived at the system sums of the running kernel
+    int fuse_fin;            // end step: the last block of each system also runs its finalize (fin)
+    FinalizeArgs fin;
     const struct CallBox *box;  // centroid alpha: staged per-call step -- p and f come from the
                                 // caller's arrays named in this mailbox (device address)
     int n_draw;              // ring: extra blocks that make the PILE-G centroid draws at the
@@ -304,24 +328,6 @@ struct RingArgs {
     int draw_sys0;
 };
 
-struct FinalizeArgs {
-    const SysDev *sys;
-    int n_sys;
-    const double *energy;    // base-job energies (job_base + bead)
-    SysAcc *acc;
-    SysRun *run;
-    double *est;             // ring buffer [max_records][n_sys][8]
-    int max_records;
-    unsigned long long *step;
-    unsigned long long *records;
-    unsigned *status;
-    const double *noise;     // optional caller noise for the centroid draw (system 0 only)
-    int record;              // 1: write an estimator record and count a step
-    int draw_alpha;          // 1: draw the next PILE-G centroid factor
-    int sys_begin, sys_end;  // systems handled
-    int pile_g;              // 1: draw alpha whatever the system's thermostat
-    int pre_drawn;           // 1: this step's k_ring already made the centroid draws (SysRun)
-};
 
 struct ScArgs {
     const SysDev *sys;
