@@ -456,6 +456,26 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
         w = qq * fmaf(pref, ex, A) * (iv * iv);
         return qq * A;
     };
+    // the same pair without a branch (the test-free loop between distant tiles):
+    // a pair beyond r_c is evaluated at r_c and weighted by zero
+    auto pair_nb = [&](const float4 &pm, float &dx, float &dy, float &dz, float &w) -> float {
+        dx = ps.x - pm.x;
+        dy = ps.y - pm.y;
+        dz = ps.z - pm.z;
+        dx = fmaf(-L0, rintf(dx * I0), dx);
+        dy = fmaf(-L1, rintf(dy * I1), dy);
+        dz = fmaf(-L2, rintf(dz * I2), dz);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const bool in = r2 < rc2;
+        const float rr = in ? r2 : rc2;
+        const float iv = rsqrt_approx(rr);
+        const float ex = ex2_approx(cex * rr);
+        const float t = rcp_approx(fmaf(ka, rr * iv, 1.0f));
+        const float A = (t * as_poly(t)) * ex * iv;
+        const float qq = in ? ps.w * pm.w : 0.f;
+        w = qq * fmaf(pref, ex, A) * (iv * iv);
+        return qq * A;
+    };
     float Sx = 0.f, Sy = 0.f, Sz = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f, e = 0.f;
     const size_t ts = (size_t)a.total_sites;
     for (int d = d0; d < d1; ++d) {
@@ -490,7 +510,7 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
 #pragma unroll 4
                 for (int r = 0; r < 32; ++r) {
                     float dx, dy, dz, w;
-                    e += pair(pm, dx, dy, dz, w);
+                    e += pair_nb(pm, dx, dy, dz, w);
                     fx = fmaf(w, dx, fx);
                     fy = fmaf(w, dy, fy);
                     fz = fmaf(w, dz, fz);
