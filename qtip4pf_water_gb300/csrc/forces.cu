@@ -435,6 +435,7 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
     const float cex = (float)(-S.kappa * S.kappa * 1.4426950408889634), pref = (float)S.ewald_pref;
     const int s = tJ * 32 + lane, ms = s / 3;
     const bool vs = s < ns;
+    __shared__ float4 vis[HW][32];
     float4 ps = make_float4(0.f, 0.f, 0.f, 0.f);
     if (vs) ps = sites[s];
     // w = q_s q_m (A + B) / r^2 along d = r_s - r_m; returns q_s q_m A (the pair energy)
@@ -507,10 +508,15 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
             // at most two consecutive tiles): between two full tiles every pair counts
             const bool plain = d >= 2 && (tJ + 1) * 32 <= ns && m0 + 32 <= ns;
             if (active && plain) {
+                // the visited sites are read from the warp's shared-memory copy (one
+                // 16-byte load a step); only their force accumulators rotate
+                vis[warp][lane] = pm;
+                __syncwarp();
 #pragma unroll 4
                 for (int r = 0; r < 32; ++r) {
+                    const float4 pv = vis[warp][(lane + r) & 31];
                     float dx, dy, dz, w;
-                    e += pair_nb(pm, dx, dy, dz, w);
+                    e += pair_nb(pv, dx, dy, dz, w);
                     fx = fmaf(w, dx, fx);
                     fy = fmaf(w, dy, fy);
                     fz = fmaf(w, dz, fz);
@@ -518,14 +524,11 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
                     my = fmaf(-w, dy, my);
                     mz = fmaf(-w, dz, mz);
                     const int nx = (lane + 1) & 31;
-                    pm.x = __shfl_sync(0xffffffffu, pm.x, nx);
-                    pm.y = __shfl_sync(0xffffffffu, pm.y, nx);
-                    pm.z = __shfl_sync(0xffffffffu, pm.z, nx);
-                    pm.w = __shfl_sync(0xffffffffu, pm.w, nx);
                     mx = __shfl_sync(0xffffffffu, mx, nx);
                     my = __shfl_sync(0xffffffffu, my, nx);
                     mz = __shfl_sync(0xffffffffu, mz, nx);
                 }
+                __syncwarp();
             } else if (active) {
                 for (int r = 0; r < 32; ++r) {
                     const int m = m0 + ((lane + r) & 31);
