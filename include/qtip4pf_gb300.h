@@ -128,6 +128,14 @@ qtg_status qtg_ftransform(qtg_ctx *ctx, int sys, double *a, int length, int forw
  * draw from the system's counter-based generator. *heat receives the return value. */
 qtg_status qtg_pile_g(qtg_ctx *ctx, int sys, double *p, const double *mass,
                       const double *noise, double *heat);
+/* thermostat.cpp:12-60  double bussi(p, mass, rng): global rescale of the first
+ * n_dof momenta (bead 0; the reference's classical system) to the canonical
+ * kinetic-energy distribution at the system's temperature. noise = [R, g2] (R the
+ * normal draw, g2 the combined chi-square draw of n_dof - 1 degrees of freedom)
+ * from the caller, or NULL to draw from the system's counter-based generator.
+ * *heat receives the return value (kinetic energy before minus after). */
+qtg_status qtg_bussi(qtg_ctx *ctx, int sys, double *p, const double *mass, const double *noise,
+                     double *heat);
 /* path_integrals.cpp:29-48  double get_kcv(q, f) */
 qtg_status qtg_get_kcv(qtg_ctx *ctx, int sys, const double *q, const double *f, double *out);
 /* path_integrals.cpp:55-81  double get_conserved(q, p, mass, energy); like the

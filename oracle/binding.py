@@ -66,6 +66,8 @@ def lib():
         L.qo_ftransform.argtypes = [S, D, C.c_int, C.c_int]
         L.qo_pile_g.argtypes = [S, D, D, D]
         L.qo_pile_g.restype = C.c_double
+        L.qo_bussi.argtypes = [S, D, D, D]
+        L.qo_bussi.restype = C.c_double
         L.qo_get_kcv.argtypes = [S, D, D]
         L.qo_get_kcv.restype = C.c_double
         L.qo_get_conserved.argtypes = [S, D, D, D, C.c_double]
@@ -147,6 +149,9 @@ class Oracle:
 
     def pile_g(self, p, noise):
         return self.L.qo_pile_g(C.byref(self.s), _d(p), _d(self.mass), _d(noise))
+
+    def bussi(self, p, noise):
+        return self.L.qo_bussi(C.byref(self.s), _d(p), _d(self.mass), _d(noise))
 
     def get_kcv(self, q, f):
         return self.L.qo_get_kcv(C.byref(self.s), _d(q), _d(f))

@@ -581,6 +581,22 @@ double qo_pile_g(const qo_sys *s, double *p, const double *mass, const double *n
     return heat;
 }
 
+/* ---- Bussi global rescale: thermostat.cpp:12-60 ----------------------------
+ * The first n_dof momenta (the reference's classical system) are rescaled by
+ * alpha = sqrt((R^2 + g2) / (beta sum p^2 / m)), m the atom's mass; returns the
+ * heat (kinetic energy before minus after). noise = [R, g2]. */
+double qo_bussi(const qo_sys *s, double *p, const double *mass, const double *noise) {
+    const int nd = s->n_dof;
+    double heat = 0.0, p2 = 0.0;
+    for (int i = 0; i < nd; ++i) heat += 0.5 * p[i] * p[i] / mass[3 * (i / 3)];
+    for (int i = 0; i < nd; ++i) p2 += p[i] * p[i] / mass[3 * (i / 3)];
+    const double R = noise[0], g2 = noise[1];
+    const double alpha = sqrt((R * R + g2) / (s->beta * p2));
+    for (int i = 0; i < nd; ++i) p[i] *= alpha;
+    for (int i = 0; i < nd; ++i) heat -= 0.5 * p[i] * p[i] / mass[3 * (i / 3)];
+    return heat;
+}
+
 /* ---- estimators: path_integrals.cpp:10-81 ---------------------------------- */
 double qo_get_kcv(const qo_sys *s, const double *q, const double *f) {
     const int P = s->n_beads, nd = s->n_dof;

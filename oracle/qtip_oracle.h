@@ -62,6 +62,8 @@ void qo_ftransform(const qo_sys *s, double *a, int length, int forwards);
 /* thermostat.cpp:64-133 with the random numbers supplied:
  * noise = [R, g2, xi(bead 1..P-1, dof 0..n_dof-1)]. Returns the heat. */
 double qo_pile_g(const qo_sys *s, double *p, const double *mass, const double *noise);
+/* thermostat.cpp:12-60; noise = [R, g2] (the combined chi-square draw) */
+double qo_bussi(const qo_sys *s, double *p, const double *mass, const double *noise);
 /* path_integrals.cpp:29-48 and :55-81 */
 double qo_get_kcv(const qo_sys *s, const double *q, const double *f);
 double qo_get_conserved(const qo_sys *s, double *q, double *p, const double *mass, double energy);

@@ -195,4 +195,27 @@ double ref_pile_g(double *p, unsigned seed, double *noise) {
     return heat;
 }
 
+// bussi (thermostat.cpp:12-60) with a generator seeded by `seed`; its two
+// draws are replayed as for ref_pile_g and returned in noise = [R, g2].
+double ref_bussi(double *p, unsigned seed, double *noise) {
+    std::mt19937 rng(seed);
+    std::mt19937 replay(seed);
+    double heat = bussi(p, g_mass.data(), rng);
+    std::normal_distribution<double> gauss(0.0, 1.0);
+    int dof = 3 * n_atoms;
+    double R = gauss(replay);
+    double g2;
+    if (dof % 2 == 0) {
+        std::gamma_distribution<double> gam((dof - 2) / 2, 1.0);
+        double R_add = gauss(replay);
+        g2 = 2.0 * gam(replay) + R_add * R_add;
+    } else {
+        std::gamma_distribution<double> gam((dof - 1) / 2, 1.0);
+        g2 = 2.0 * gam(replay);
+    }
+    noise[0] = R;
+    noise[1] = g2;
+    return heat;
+}
+
 }  // extern "C"

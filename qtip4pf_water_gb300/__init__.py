@@ -92,6 +92,7 @@ def load(build_if_missing: bool = True):
         "qtg_force_eval_trotter": ([V, C.c_int, D, D, D, I, I, D, D], C.c_int),
         "qtg_ftransform": ([V, C.c_int, D, C.c_int, C.c_int], C.c_int),
         "qtg_pile_g": ([V, C.c_int, D, D, D, D], C.c_int),
+        "qtg_bussi": ([V, C.c_int, D, D, D, D], C.c_int),
         "qtg_get_kcv": ([V, C.c_int, D, D, D], C.c_int),
         "qtg_get_conserved": ([V, C.c_int, D, D, D, C.c_double, D], C.c_int),
         "qtg_update_class": ([V, C.c_int, V, V, V, V, V, V, V, V, D], C.c_int),
@@ -388,6 +389,12 @@ class System:
     def pile_g(self, p, mass, noise=None):
         h = C.c_double(0.0)
         self._c(self.ctx.L.qtg_pile_g(self.ctx.h, self.idx, _d(p), _d(mass), _d(noise), C.byref(h)))
+        return h.value
+
+    def bussi(self, p, mass, noise=None):
+        """thermostat.cpp:12-60 on the first n_dof momenta; returns the heat."""
+        h = C.c_double(0.0)
+        self._c(self.ctx.L.qtg_bussi(self.ctx.h, self.idx, _d(p), _d(mass), _d(noise), C.byref(h)))
         return h.value
 
     def get_kcv(self, q, f):

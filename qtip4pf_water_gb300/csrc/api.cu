@@ -1528,6 +1528,24 @@ qtg_status qtg_pile_g(qtg_ctx *ctx, int sys, double *p, const double *mass, cons
     return QTG_OK;
 }
 
+qtg_status qtg_bussi(qtg_ctx *ctx, int sys, double *p, const double *mass, const double *noise, double *heat) {
+    CKS(check_sys(ctx, sys));
+    const SysDev &S = ctx->sys_h[sys];
+    if (!p) return fail(ctx, QTG_ERR_ARG, "bad argument");
+    if (mass) CKS(upload_masses(ctx, sys, mass));
+    CK(up(ctx, ctx->p + S.q_off, p, sizeof(double) * S.n_dof));
+    if (noise) CK(up(ctx, ctx->noise, noise, sizeof(double) * 2));
+    RingArgs r = ring_args(ctx, sys, 0);
+    r.noise = noise ? ctx->noise : nullptr;
+    launch_bussi(r, sys, ctx->stream, &ctx->launches);
+    CK(down(ctx, p, ctx->p + S.q_off, sizeof(double) * S.n_dof));
+    double h = 0.0;
+    CK(down(ctx, &h, &ctx->run[sys].heat, sizeof(double)));
+    CKS(sync_status(ctx));
+    if (heat) *heat = h;
+    return QTG_OK;
+}
+
 qtg_status qtg_get_kcv(qtg_ctx *ctx, int sys, const double *q, const double *f, double *out) {
     CKS(check_sys(ctx, sys));
     const SysDev &S = ctx->sys_h[sys];

@@ -161,6 +161,28 @@ double pile_g(double momentum_array[], const double mass_array[], std::mt19937 &
     return heat;
 }
 
+// thermostat.h:4 (the reference's classical runs have it commented out,
+// simulation.cpp:181; the drop-in serves it all the same)
+double bussi(double momentum_array[], const double mass_array[], std::mt19937 &gen) {
+    double heat = 0.0;
+    if (!ctx()) return heat;
+    // the two draws of thermostat.cpp:33-44, from the caller's generator in order
+    std::normal_distribution<double> gauss_dev(0.0, 1.0);
+    const int dof = 3 * n_atoms;
+    double noise[2];
+    noise[0] = gauss_dev(gen);
+    if (dof % 2 == 0) {
+        std::gamma_distribution<double> gamma_dev((dof - 2) / 2, 1.0);
+        const double R_add = gauss_dev(gen);
+        noise[1] = 2.0 * gamma_dev(gen) + R_add * R_add;
+    } else {
+        std::gamma_distribution<double> gamma_dev((dof - 1) / 2, 1.0);
+        noise[1] = 2.0 * gamma_dev(gen);
+    }
+    report(qtg_bussi(g_ctx, 0, momentum_array, mass_array, noise, &heat), "bussi");
+    return heat;
+}
+
 // path_integrals.h:5-6
 double get_kcv(const double position_array[], const double force_array[]) {
     double v = 0.0;

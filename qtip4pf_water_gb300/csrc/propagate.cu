@@ -496,6 +496,40 @@ __global__ void __launch_bounds__(256) k_centroid_alpha(RingArgs a, int sys) {
     }
 }
 
+// Bussi global rescale of a system's first n_dof momenta (thermostat.cpp:12-60):
+// p *= alpha, alpha = sqrt((R^2 + g2) / (beta sum p^2 / m)), R ~ N(0,1) and
+// g2 ~ chi^2(n_dof - 1) (caller noise [R, g2], else the counter-based draw at the
+// system's step). The heat, kinetic energy before minus after = (1 - alpha^2)
+// sum p^2 / 2m, goes to the system's run state. One block.
+__global__ void __launch_bounds__(1024) k_bussi(RingArgs a, int sys) {
+    const SysDev &S = a.sys[sys];
+    const int nd = S.n_dof;
+    double *p = a.p + S.q_off;
+    const double *im = a.inv_mass + S.mass_off;
+    __shared__ double red[32];
+    __shared__ double alpha_sh;
+    double p2 = 0.0;
+    for (int i = threadIdx.x; i < nd; i += blockDim.x) p2 += p[i] * p[i] * im[i];
+    p2 = block_sum(p2, red);  // every lane of warp 0 holds the total
+    if (threadIdx.x < 32) {
+        double R, g2;
+        if (a.noise) {
+            R = a.noise[0];
+            g2 = a.noise[1];
+        } else {
+            centroid_draw(S, sys, *a.step, &R, &g2, a.status);
+        }
+        if (threadIdx.x == 0) {
+            const double al = sqrt((R * R + g2) / (S.beta * p2));
+            alpha_sh = al;
+            a.run[sys].heat = 0.5 * p2 * (1.0 - al * al);
+        }
+    }
+    __syncthreads();
+    const double al = alpha_sh;
+    for (int i = threadIdx.x; i < nd; i += blockDim.x) p[i] *= al;
+}
+
 // One system's step close (called by a whole warp): the estimator record
 // (lane 0) and the next PILE-G centroid factor, then the step accumulators
 // cleared. st, rec: the step and record counters at the start of the step.
@@ -705,6 +739,11 @@ void launch_end_step(const RingArgs &a, cudaStream_t s, unsigned long long *n) {
 void launch_centroid_ke(const RingArgs &a, cudaStream_t s, unsigned long long *n) {
     if (a.n_work <= 0) return;
     k_centroid_ke<<<a.n_work, 256, 0, s>>>(a);
+    if (n) ++*n;
+}
+
+void launch_bussi(const RingArgs &a, int sys, cudaStream_t s, unsigned long long *n) {
+    k_bussi<<<1, 1024, 0, s>>>(a, sys);
     if (n) ++*n;
 }
 

@@ -363,6 +363,8 @@ void launch_sc_finish(const ScArgs &a, cudaStream_t s, unsigned long long *n);
 void launch_transform(const SysDev *sys, int sysi, int P, const double *nm_sys, double *a, int length,
                       int forwards, cudaStream_t s, unsigned long long *n);
 void launch_centroid_ke(const RingArgs &a, cudaStream_t s, unsigned long long *n);
+// Bussi global rescale of system sys (one block)
+void launch_bussi(const RingArgs &a, int sys, cudaStream_t s, unsigned long long *n);
 // per-call PIMD steps: k0 after the opening kick, the centroid draws and alpha of system sys
 void launch_centroid_alpha(const RingArgs &a, int sys, cudaStream_t s, unsigned long long *n);
 // sum_k sum_j (p_kj^2 / 2 m_j + m_j w_k^2 q_kj^2 / 2) of normal-mode arrays -> out[0], out[1]

@@ -74,6 +74,8 @@ def load_ref():
     lib.ref_update_sc.restype = C.c_double
     lib.ref_pile_g.argtypes = [D, C.c_uint, D]
     lib.ref_pile_g.restype = C.c_double
+    lib.ref_bussi.argtypes = [D, C.c_uint, D]
+    lib.ref_bussi.restype = C.c_double
     return lib
 
 
@@ -118,6 +120,11 @@ def run_case(name: str) -> None:
     fk = np.zeros(9 * N)
     ek = lib.ref_kwald(_p(sites), _p(fk), 0)
     out.update(kw_sites=sites, kw_forces=fk, kw_energy=ek)
+    # Bussi rescale (thermostat.cpp:12-60) of the first n_dof momenta with a recorded draw
+    pb = p.copy()
+    noise_b = np.zeros(2)
+    heat_b = lib.ref_bussi(_p(pb), seed + 7, _p(noise_b))
+    out.update(bussi_p_in=p.copy(), bussi_p_out=pb, bussi_noise=noise_b, bussi_heat=heat_b)
 
     if P == 1:
         q1, p1, f1 = q.copy(), p.copy(), f.copy()

@@ -20,7 +20,7 @@ def declared_symbols(path):
 def test_header_declares_entry_points():
     syms = declared_symbols(HEADER)
     for name in ("qtg_create", "qtg_neighbour_list", "qtg_get_forces", "qtg_kwald", "qtg_force_eval_sc",
-                 "qtg_ftransform", "qtg_pile_g", "qtg_get_kcv", "qtg_get_conserved", "qtg_update_class",
+                 "qtg_ftransform", "qtg_pile_g", "qtg_bussi", "qtg_get_kcv", "qtg_get_conserved", "qtg_update_class",
                  "qtg_update_pimd", "qtg_run_steps"):
         assert name in syms
 

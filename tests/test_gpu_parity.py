@@ -140,6 +140,18 @@ def test_normal_mode_transform(gpu_lib, case):
     np.testing.assert_allclose(d, g["nm3_fwd"], rtol=0, atol=1e-12 * np.abs(d).max())
 
 
+@pytest.mark.parametrize("case", CASES)
+def test_bussi_with_recorded_noise(gpu_lib, case):
+    g = load_golden(case)
+    s = make(g, gpu_lib.FP64)
+    p = g["bussi_p_in"].copy()
+    heat = s.bussi(p, s.masses(), np.ascontiguousarray(g["bussi_noise"]))
+    np.testing.assert_allclose(p, g["bussi_p_out"], rtol=1e-12, atol=1e-12 * np.abs(p).max())
+    m = s.masses()
+    ke = 0.5 * float(np.sum(g["bussi_p_in"][: m.size] ** 2 / m))
+    assert abs(heat - float(g["bussi_heat"])) <= 1e-12 * ke
+
+
 @pytest.mark.parametrize("case", PIMD)
 def test_pile_g_with_recorded_noise(gpu_lib, case):
     g = load_golden(case)

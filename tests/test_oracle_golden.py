@@ -116,6 +116,18 @@ def test_normal_mode_transform(case):
     np.testing.assert_allclose(d, g["nm3_fwd"], rtol=0, atol=1e-13 * np.abs(d).max())
 
 
+@pytest.mark.parametrize("case", CASES)
+def test_bussi_with_recorded_noise(case):
+    """thermostat.cpp:12-60 (global rescale of the first n_dof momenta)."""
+    g = load_golden(case)
+    o = make(g)
+    p = g["bussi_p_in"].copy()
+    heat = o.bussi(p, g["bussi_noise"])
+    np.testing.assert_allclose(p, g["bussi_p_out"], rtol=1e-13, atol=1e-13 * np.abs(p).max())
+    ke = 0.5 * float(np.sum(g["bussi_p_in"][: 9 * o.N] ** 2 / np.repeat(o.mass[0::3], 3)))
+    assert abs(heat - float(g["bussi_heat"])) <= 1e-12 * ke
+
+
 @pytest.mark.parametrize("case", PIMD)
 def test_pile_g_with_recorded_noise(case):
     g = load_golden(case)
