@@ -211,6 +211,7 @@ struct qtg_ctx {
     cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join = nullptr;
     Forks forks{};            // branches of a mixed force evaluation (real | k-space | LJ)
     float4 *ljf = nullptr;    // dense LJ oxygen forces per molecule and slot
+    int4 *sites_fix = nullptr;  // fixed-point site fractions per slot (half-interaction real space)
     std::string err;
     Consts K;
     std::vector<qtg_system_desc> desc;
@@ -347,6 +348,7 @@ EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, d
     a.max_grp = c->max_grp;
     a.max_batch = c->max_batch;
     a.sites = c->sites;
+    a.sites_fix = c->sites_fix;
     a.opos = c->opos;
     a.ljf = c->ljf;
     a.phase = c->phase;
@@ -1096,6 +1098,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         ctx->opos = tmp;
     }
     AL(ctx->ljf, ctx->total_sites / 3);
+    AL(ctx->sites_fix, ctx->total_sites);
     AL(ctx->part, (size_t)MAX_PART * 3 * ctx->total_sites);
     AL(ctx->skp, (size_t)MAX_SC * ctx->total_k);
     AL(ctx->dskp, (size_t)MAX_SC * ctx->total_k);
@@ -1209,7 +1212,7 @@ void qtg_destroy(qtg_ctx *ctx) {
                     ctx->phase, ctx->opos, ctx->part, ctx->skp, ctx->dskp, ctx->wsk, ctx->wdsk, ctx->energy, ctx->energy_aux,
                     ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
-                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf, ctx->fin_ticket};
+                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf, ctx->fin_ticket, ctx->sites_fix};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->box) cudaFreeHost(ctx->box);

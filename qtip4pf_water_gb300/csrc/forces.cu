@@ -159,6 +159,10 @@ __global__ void __launch_bounds__(128) k_prep(EvalArgs a) {
     sv.z = (R)(frac[2] * S.box[2]);
     sv.w = (R)chg;
     reinterpret_cast<V4<R> *>(a.sites)[J.site_off + s] = sv;
+    if (sizeof(R) == 4 && a.sites_fix)
+        a.sites_fix[J.site_off + s] = make_int4((int)__double2uint_rz(frac[0] * 4294967296.0),
+                                                (int)__double2uint_rz(frac[1] * 4294967296.0),
+                                                (int)__double2uint_rz(frac[2] * 4294967296.0), __float_as_int((float)chg));
     if (J.mode == 1) {
         V4<R> tv;
         tv.x = (R)u[0];
@@ -414,6 +418,8 @@ __global__ void __launch_bounds__(RT) k_real_f32(EvalArgs a) {
 // the first half of the tiles); the visited tile's sites and their force
 // accumulators rotate through the lanes by shuffles, 32 steps bringing them
 // back home. The stationary tile's own pairs (d = 0) are taken from both sides.
+// Sites are read as 32-bit fixed-point box fractions (k_prep), whose wrapped
+// integer differences are minimum-image separations to 2^-32 of the box.
 // Forces are written as partial planes, deterministic: plane `ch` holds the
 // stationary-side sums of chunk ch of the distances, plane n_ch + d - 1 the
 // visited-side sums of distance d (zero where that visit is not made).
@@ -428,24 +434,28 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
     if (tJ >= T) return;
     const int maxd = T / 2;
     const int d0 = chunk_lo(maxd + 1, ch, n_ch), d1 = chunk_lo(maxd + 1, ch + 1, n_ch);
-    const float4 *sites = reinterpret_cast<const float4 *>(a.sites) + J.site_off;
-    const float L0 = S.boxf[0], L1 = S.boxf[1], L2 = S.boxf[2];
-    const float I0 = S.inv_boxf[0], I1 = S.inv_boxf[1], I2 = S.inv_boxf[2];
+    // sites as 32-bit fixed-point box fractions: the wrapped difference of two
+    // fractions is the minimum image, one integer subtraction and one conversion
+    // a component (scaled by L / 2^32)
+    const int4 *sites = a.sites_fix + J.site_off;
+    const float X0 = (float)(S.box[0] * 2.3283064365386963e-10), X1 = (float)(S.box[1] * 2.3283064365386963e-10),
+                X2 = (float)(S.box[2] * 2.3283064365386963e-10);
     const float rc2 = (float)S.rc_sq, ka = (float)(0.3275911 * S.kappa);
     const float cex = (float)(-S.kappa * S.kappa * 1.4426950408889634), pref = (float)S.ewald_pref;
     const int s = tJ * 32 + lane, ms = s / 3;
     const bool vs = s < ns;
-    __shared__ float4 vis[HW][32];
-    float4 ps = make_float4(0.f, 0.f, 0.f, 0.f);
+    __shared__ int4 vis[HW][32];
+    int4 ps = make_int4(0, 0, 0, 0);
     if (vs) ps = sites[s];
+    const float qs = __int_as_float(ps.w);
+    auto disp = [&](const int4 &pm, float &dx, float &dy, float &dz) {
+        dx = (float)(int)((unsigned)ps.x - (unsigned)pm.x) * X0;
+        dy = (float)(int)((unsigned)ps.y - (unsigned)pm.y) * X1;
+        dz = (float)(int)((unsigned)ps.z - (unsigned)pm.z) * X2;
+    };
     // w = q_s q_m (A + B) / r^2 along d = r_s - r_m; returns q_s q_m A (the pair energy)
-    auto pair = [&](const float4 &pm, float &dx, float &dy, float &dz, float &w) -> float {
-        dx = ps.x - pm.x;
-        dy = ps.y - pm.y;
-        dz = ps.z - pm.z;
-        dx = fmaf(-L0, rintf(dx * I0), dx);
-        dy = fmaf(-L1, rintf(dy * I1), dy);
-        dz = fmaf(-L2, rintf(dz * I2), dz);
+    auto pair = [&](const int4 &pm, float &dx, float &dy, float &dz, float &w) -> float {
+        disp(pm, dx, dy, dz);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         w = 0.f;
         if (!(r2 < rc2)) return 0.f;
@@ -453,19 +463,14 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
         const float ex = ex2_approx(cex * r2);
         const float t = rcp_approx(fmaf(ka, r2 * iv, 1.0f));
         const float A = (t * as_poly(t)) * ex * iv;
-        const float qq = ps.w * pm.w;
+        const float qq = qs * __int_as_float(pm.w);
         w = qq * fmaf(pref, ex, A) * (iv * iv);
         return qq * A;
     };
     // the same pair without a branch (the test-free loop between distant tiles):
     // a pair beyond r_c is evaluated at r_c and weighted by zero
-    auto pair_nb = [&](const float4 &pm, float &dx, float &dy, float &dz, float &w) -> float {
-        dx = ps.x - pm.x;
-        dy = ps.y - pm.y;
-        dz = ps.z - pm.z;
-        dx = fmaf(-L0, rintf(dx * I0), dx);
-        dy = fmaf(-L1, rintf(dy * I1), dy);
-        dz = fmaf(-L2, rintf(dz * I2), dz);
+    auto pair_nb = [&](const int4 &pm, float &dx, float &dy, float &dz, float &w) -> float {
+        disp(pm, dx, dy, dz);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         const bool in = r2 < rc2;
         const float rr = in ? r2 : rc2;
@@ -473,7 +478,7 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
         const float ex = ex2_approx(cex * rr);
         const float t = rcp_approx(fmaf(ka, rr * iv, 1.0f));
         const float A = (t * as_poly(t)) * ex * iv;
-        const float qq = in ? ps.w * pm.w : 0.f;
+        const float qq = in ? qs * __int_as_float(pm.w) : 0.f;
         w = qq * fmaf(pref, ex, A) * (iv * iv);
         return qq * A;
     };
@@ -484,7 +489,7 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
         if (d == 0) {  // the tile's own pairs, from both sides
             for (int r = 1; r < 32; ++r) {
                 const int src = (lane + r) & 31;
-                float4 pm;
+                int4 pm;
                 pm.x = __shfl_sync(0xffffffffu, ps.x, src);
                 pm.y = __shfl_sync(0xffffffffu, ps.y, src);
                 pm.z = __shfl_sync(0xffffffffu, ps.z, src);
@@ -501,7 +506,7 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
             const int tI = (tJ + d) % T;
             const bool active = !((T % 2 == 0) && d == maxd && tJ >= maxd);
             const int m0 = tI * 32;
-            float4 pm = make_float4(0.f, 0.f, 0.f, 0.f);
+            int4 pm = make_int4(0, 0, 0, 0);
             if (active && m0 + lane < ns) pm = sites[m0 + lane];
             float mx = 0.f, my = 0.f, mz = 0.f;
             // tiles two or more apart share no molecule (a molecule's three sites lie in
@@ -514,7 +519,7 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
                 __syncwarp();
 #pragma unroll 4
                 for (int r = 0; r < 32; ++r) {
-                    const float4 pv = vis[warp][(lane + r) & 31];
+                    const int4 pv = vis[warp][(lane + r) & 31];
                     float dx, dy, dz, w;
                     e += pair_nb(pv, dx, dy, dz, w);
                     fx = fmaf(w, dx, fx);

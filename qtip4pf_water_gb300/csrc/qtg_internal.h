@@ -404,6 +404,8 @@ struct EvalArgs {
     const int *kpk;        // per k (as kvec): kz >= 0: (packed slot in its force batch) << 8 | kz; kz < 0: -1
     int max_grp, max_batch;
     void *sites;           // 4 reals per site (x, y, z, q), per slot
+    int4 *sites_fix;       // mixed: per site the box fractions of x, y, z as 32-bit fixed point
+                           // (so a wrapped integer difference is the minimum image) and q's bits
     void *opos;            // wrapped oxygen positions, 4 reals per molecule, per slot
     float4 *ljf;           // dense Lennard-Jones oxygen forces, per molecule, per slot (lj_plane)
     int lj_plane;          // 1: k_lj_dense writes ljf and k_combine_f32 adds it to the O force
