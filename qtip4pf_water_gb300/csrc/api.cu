@@ -73,7 +73,7 @@ void enumerate_k(const SysDev &S, double kc_sq, std::vector<KVec> &out) {
         v.kx = a;
         v.ky = b;
         v.kz = c;
-        v.pad = 0;
+        v.twin = (a == 0 && b > 0) ? 1 : 0;
         v.coef = S.k_pref * exp(-ksq * quart) / ksq * (a ? 2.0 : 1.0);
         v.gx = 2.0 * v.coef * bk[0] * a;
         v.gy = 2.0 * v.coef * bk[1] * b;
@@ -131,10 +131,25 @@ void nm_matrix(int P, std::vector<double> &C) {
 // build the structure-factor groups (<= 8 kz of one column) and the force
 // batches (whole columns, <= 128 vectors).
 void build_columns(const std::vector<KVec> &kv, std::vector<KVec> &kord, std::vector<KCol> &cols,
-                   std::vector<KGroup> &grps, std::vector<KBatch> &bats, std::vector<int> &kpk) {
+                   std::vector<KGroup> &grps, std::vector<KBatch> &bats, std::vector<int> &kpk, int *n_grp_half,
+                   int *n_batch_half, int *n_kvec_half) {
     std::map<std::pair<int, int>, std::map<int, KVec>> by;
     for (const KVec &v : kv) by[{v.kx, v.ky}][v.kz] = v;
-    for (auto &col : by) {
+    // the kx = 0, ky < 0 columns last (the mixed half set leaves them out)
+    std::vector<const std::pair<const std::pair<int, int>, std::map<int, KVec>> *> order;
+    for (auto &col : by)
+        if (!(col.first.first == 0 && col.first.second < 0)) order.push_back(&col);
+    const int n_col_half = (int)order.size();
+    for (auto &col : by)
+        if (col.first.first == 0 && col.first.second < 0) order.push_back(&col);
+    *n_grp_half = 0;
+    *n_kvec_half = 0;
+    for (const auto *colp : order) {
+        const auto &col = *colp;
+        if ((int)cols.size() == n_col_half) {
+            *n_grp_half = (int)grps.size();
+            *n_kvec_half = (int)kord.size();
+        }
         int m = 0;
         for (auto &e : col.second) m = std::max(m, std::abs(e.first));
         KCol c;
@@ -151,7 +166,7 @@ void build_columns(const std::vector<KVec> &kv, std::vector<KVec> &kord, std::ve
                 f.kx = c.kx;
                 f.ky = c.ky;
                 f.kz = kz;
-                f.pad = 0;
+                f.twin = 0;
                 f.coef = f.gx = f.gy = f.gz = 0.0;
                 kord.push_back(f);
             }
@@ -167,10 +182,18 @@ void build_columns(const std::vector<KVec> &kv, std::vector<KVec> &kord, std::ve
             grps.push_back(g);
         }
     }
+    if ((int)cols.size() == n_col_half) {
+        *n_grp_half = (int)grps.size();
+        *n_kvec_half = (int)kord.size();
+    }
+    // force batches of whole columns (<= 128 vectors), none straddling the half-set end
     int c0 = 0;
+    *n_batch_half = 0;
     while (c0 < (int)cols.size()) {
+        if (c0 == n_col_half) *n_batch_half = (int)bats.size();
+        const int c_end = c0 < n_col_half ? n_col_half : (int)cols.size();
         int c1 = c0, n = 0;
-        while (c1 < (int)cols.size() && n + 2 * cols[c1].m + 1 <= 128) {
+        while (c1 < c_end && n + 2 * cols[c1].m + 1 <= 128) {
             n += 2 * cols[c1].m + 1;
             ++c1;
         }
@@ -182,6 +205,7 @@ void build_columns(const std::vector<KVec> &kv, std::vector<KVec> &kord, std::ve
         bats.push_back(b);
         c0 = c1;
     }
+    if (c0 == n_col_half) *n_batch_half = (int)bats.size();
     // the FP32 k-force kernel's packing: per batch, the columns' |kz| = 0 .. m in
     // consecutive slots; the kz >= 0 entry of each pair names its slot and |kz|
     kpk.assign(kord.size(), -1);
@@ -868,7 +892,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         std::vector<KBatch> bats;
         enumerate_k(S, kc * kc, kv);
         std::vector<int> kp;
-        build_columns(kv, kord, cols, grps, bats, kp);
+        build_columns(kv, kord, cols, grps, bats, kp, &S.n_grp_half, &S.n_batch_half, &S.n_kvec_half);
         kpk_all.insert(kpk_all.end(), kp.begin(), kp.end());
         S.n_kvec_ref = (int)kv.size();
         S.n_kvec = (int)kord.size();

@@ -591,7 +591,9 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
     const int sc = blockIdx.y, jb = blockIdx.z;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
-    const int ng = S.n_grp, ns = S.n_sites, km1 = S.k_max + 1;
+    // the FP32 energy/force form runs over the half set (kx = 0, ky < 0 columns left out)
+    const bool half = sizeof(R) == 4 && MODE == 0;
+    const int ng = half ? S.n_grp_half : S.n_grp, ns = S.n_sites, km1 = S.k_max + 1;
     if (blockIdx.x * KT >= ng) return;
     const int t = blockIdx.x * KT + threadIdx.x;
     const bool act = t < ng;
@@ -739,12 +741,17 @@ __global__ void __launch_bounds__(128) k_sk_reduce(EvalArgs a) {
     const int jb = blockIdx.y;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
-    if (blockIdx.x * 128 >= S.n_kvec) return;
+    // FP32 energy/force form: the half set, each kx = 0, ky > 0 vector standing for
+    // itself and its conjugate partner (|S|^2 and the force are the same for both)
+    const bool half = sizeof(R) == 4 && MODE == 0;
+    const int nk = half ? S.n_kvec_half : S.n_kvec;
+    if (blockIdx.x * 128 >= nk) return;
     const int k = blockIdx.x * 128 + threadIdx.x;
     __shared__ double red[4];
     double e = 0.0;
-    if (k < S.n_kvec) {
-        const double w = 2.0 * a.kvec[S.kvec_off + k].coef;
+    if (k < nk) {
+        const KVec kv = a.kvec[S.kvec_off + k];
+        const double w = 2.0 * kv.coef * ((half && kv.twin) ? 2.0 : 1.0);
         double sr = 0.0, si = 0.0, dr = 0.0, di = 0.0;
         if (sizeof(R) == 4 && MODE == 0) {
             // FP32 form: the site chunks' compensated pairs (S, C), summed in chunk
@@ -820,7 +827,8 @@ __global__ void __launch_bounds__(FT) k_kforce(EvalArgs a) {
     const int kc = blockIdx.y, jb = blockIdx.z;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
-    const int nb = S.n_batch, ns = S.n_sites, km1 = S.k_max + 1;
+    // FP32 energy/force form: the half set, whose weights k_sk_reduce<float, 0> writes
+    const int nb = (sizeof(R) == 4 && MODE == 0) ? S.n_batch_half : S.n_batch, ns = S.n_sites, km1 = S.k_max + 1;
     if (blockIdx.x * FT >= ns) return;
     const int i = blockIdx.x * FT + threadIdx.x;
     const bool act = i < ns;
@@ -922,7 +930,8 @@ __global__ void __launch_bounds__(FT) k_kforce_f32(EvalArgs a) {
     const int kc = blockIdx.y, jb = blockIdx.z;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
-    const int nb = S.n_batch, ns = S.n_sites, km1 = S.k_max + 1;
+    // the half set, whose weights k_sk_reduce<float, 0> writes
+    const int nb = S.n_batch_half, ns = S.n_sites, km1 = S.k_max + 1;
     if (blockIdx.x * FT >= ns) return;
     const int i = blockIdx.x * FT + threadIdx.x;
     const bool act = i < ns;

@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(512) k_noalloc_setup(NAParams p, unsigned char
             v.kx = kx;
             v.ky = ky;
             v.kz = kz;
-            v.pad = 0;
+            v.twin = 0;
             double ksq = 0.0;
             if (k_included(p, kx, ky, kz, &ksq)) {
                 v.coef = p.S.k_pref * exp(-ksq * p.quart) / ksq * (kx ? 2.0 : 1.0);
@@ -199,6 +199,8 @@ __global__ void __launch_bounds__(512) k_noalloc_setup(NAParams p, unsigned char
         S.n_col = ncol;
         S.n_grp = ngrp;
         S.n_batch = nb;
+        S.n_grp_half = ngrp;  // FP64 only here: the full set
+        S.n_batch_half = nb;
         *reinterpret_cast<SysDev *>(base + OFF_SYS) = S;
         Job J;
         J.sys = 0;

@@ -28,6 +28,10 @@ struct SysDev {
     int cw_begin, cw_count;  // the system's column-work blocks: slots cw_begin .. cw_begin + cw_count - 1
     int n_kvec_ref;              // the reference's k-vector count (n_kvec includes c_k = 0 fillers)
     int col_off, n_col, grp_off, n_grp, batch_off, n_batch;
+    // the mixed MODE-0 k-space kernels skip the kx = 0, ky < 0 columns (S(-k) =
+    // conj S(k) for real charges; their kx = 0, ky > 0 partners count twice):
+    // those columns come last, so the kept groups, batches and k entries are prefixes
+    int n_grp_half, n_batch_half, n_kvec_half;
     int centroid_fixed;          // 1: the centroid is held fixed (centroid-constrained PIMD)
     int lj_tie_mask;             // bit d: half of box side d lies within r_cut (a half-box tie can matter)
     long long nm_off;   // doubles: P x P bead->normal-mode matrix C (y = C x)
@@ -62,7 +66,8 @@ struct ModeCoef {
 // forces.cpp:251-445 visits, with c_k = (2 pi / V) exp(-k^2/4 kappa^2) / k^2
 // (doubled for kx > 0) and g = 2 c_k k.
 struct KVec {
-    int kx, ky, kz, pad;
+    int kx, ky, kz;
+    int twin;  // 1: kx = 0, ky > 0 (stands for its conjugate partner too in the mixed half set)
     double coef, gx, gy, gz;
 };
 
