@@ -131,8 +131,8 @@ void nm_matrix(int P, std::vector<double> &C) {
 // build the structure-factor groups (<= 8 kz of one column) and the force
 // batches (whole columns, <= 128 vectors).
 void build_columns(const std::vector<KVec> &kv, std::vector<KVec> &kord, std::vector<KCol> &cols,
-                   std::vector<KGroup> &grps, std::vector<KBatch> &bats, std::vector<int> &kpk, int *n_grp_half,
-                   int *n_batch_half, int *n_kvec_half) {
+                   std::vector<KBatch> &bats, std::vector<int> &kpk, int *n_col_half_out, int *n_batch_half,
+                   int *n_kvec_half) {
     std::map<std::pair<int, int>, std::map<int, KVec>> by;
     for (const KVec &v : kv) by[{v.kx, v.ky}][v.kz] = v;
     // the kx = 0, ky < 0 columns last (the mixed half set leaves them out)
@@ -142,14 +142,11 @@ void build_columns(const std::vector<KVec> &kv, std::vector<KVec> &kord, std::ve
     const int n_col_half = (int)order.size();
     for (auto &col : by)
         if (col.first.first == 0 && col.first.second < 0) order.push_back(&col);
-    *n_grp_half = 0;
+    *n_col_half_out = n_col_half;
     *n_kvec_half = 0;
     for (const auto *colp : order) {
         const auto &col = *colp;
-        if ((int)cols.size() == n_col_half) {
-            *n_grp_half = (int)grps.size();
-            *n_kvec_half = (int)kord.size();
-        }
+        if ((int)cols.size() == n_col_half) *n_kvec_half = (int)kord.size();
         int m = 0;
         for (auto &e : col.second) m = std::max(m, std::abs(e.first));
         KCol c;
@@ -171,21 +168,9 @@ void build_columns(const std::vector<KVec> &kv, std::vector<KVec> &kord, std::ve
                 kord.push_back(f);
             }
         }
-        const int ci = (int)cols.size();
         cols.push_back(c);
-        for (int az0 = 0; az0 <= m; az0 += 4) {  // |kz| groups, each |kz| covering +kz and -kz
-            KGroup g;
-            g.col = ci;
-            g.kz0 = az0;
-            g.n = std::min(4, m - az0 + 1);
-            g.pad = 0;
-            grps.push_back(g);
-        }
     }
-    if ((int)cols.size() == n_col_half) {
-        *n_grp_half = (int)grps.size();
-        *n_kvec_half = (int)kord.size();
-    }
+    if ((int)cols.size() == n_col_half) *n_kvec_half = (int)kord.size();
     // force batches of whole columns (<= 128 vectors), none straddling the half-set end
     int c0 = 0;
     *n_batch_half = 0;
@@ -273,6 +258,7 @@ struct qtg_ctx {
     KGroup *kgrp = nullptr;
     KBatch *kbatch = nullptr;
     int max_grp = 0, max_batch = 0;
+    int kz = 4;  // |kz| values per structure-factor group (3 or 4, chosen at creation)
     double *nm = nullptr;
     ModeCoef *modes = nullptr;
     // per-slot scratch
@@ -370,6 +356,7 @@ EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, d
     a.kbatch = c->kbatch;
     a.kpk = c->kpk;
     a.max_grp = c->max_grp;
+    a.kz = c->kz;
     a.max_batch = c->max_batch;
     a.sites = c->sites;
     a.sites_fix = c->sites_fix;
@@ -888,26 +875,21 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         S.c1_centroid = d.thermostat == QTG_THERMO_PILE_L ? exp(-S.dt / (d.tau0_fs * K.fs2au)) : 0.0;
         std::vector<KVec> kv, kord;
         std::vector<KCol> cols;
-        std::vector<KGroup> grps;
         std::vector<KBatch> bats;
         enumerate_k(S, kc * kc, kv);
         std::vector<int> kp;
-        build_columns(kv, kord, cols, grps, bats, kp, &S.n_grp_half, &S.n_batch_half, &S.n_kvec_half);
+        build_columns(kv, kord, cols, bats, kp, &S.n_col_half, &S.n_batch_half, &S.n_kvec_half);
         kpk_all.insert(kpk_all.end(), kp.begin(), kp.end());
         S.n_kvec_ref = (int)kv.size();
         S.n_kvec = (int)kord.size();
         S.kvec_off = (int)kall.size();
         S.col_off = (int)call.size();
         S.n_col = (int)cols.size();
-        S.grp_off = (int)gall.size();
-        S.n_grp = (int)grps.size();
         S.batch_off = (int)ball.size();
         S.n_batch = (int)bats.size();
         kall.insert(kall.end(), kord.begin(), kord.end());
         call.insert(call.end(), cols.begin(), cols.end());
-        gall.insert(gall.end(), grps.begin(), grps.end());
         ball.insert(ball.end(), bats.begin(), bats.end());
-        ctx->max_grp = std::max(ctx->max_grp, S.n_grp);
         ctx->max_batch = std::max(ctx->max_batch, S.n_batch);
         ctx->kc_sq.push_back(kc * kc);
         S.q_off = q_off;
@@ -963,6 +945,41 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         ctx->max_p = std::max(ctx->max_p, P);
         ctx->max_dof = std::max(ctx->max_dof, 9 * N);
         if (d.propagator == QTG_SUZUKI_CHIN && P > 1) ctx->any_sc = true;
+    }
+    // Structure-factor groups: runs of <= kz |kz| values of one column (each |kz|
+    // standing for +kz and -kz), one thread each, 128 threads a block. The width
+    // (3 or 4) is the one whose launch does less work by a simple model: whole
+    // blocks of threads, each paying the column factor (~7 instructions a site) and
+    // ~9 a |kz|, over every system's half set, sites and beads.
+    {
+        double cost[2] = {0.0, 0.0};
+        for (int w = 0; w < 2; ++w) {
+            const int kz = 3 + w;
+            for (const SysDev &S : ctx->sys_h) {
+                long long g = 0;
+                for (int c = 0; c < S.n_col_half; ++c) g += (call[S.col_off + c].m + kz) / kz;
+                cost[w] += (double)((g + 127) / 128 * 128) * (7.0 + 9.0 * kz) * S.n_sites * S.n_beads;
+            }
+        }
+        ctx->kz = cost[0] < cost[1] ? 3 : 4;
+        for (SysDev &S : ctx->sys_h) {
+            S.grp_off = (int)gall.size();
+            for (int c = 0; c < S.n_col; ++c) {
+                if (c == S.n_col_half) S.n_grp_half = (int)gall.size() - S.grp_off;
+                const int m = call[S.col_off + c].m;
+                for (int az0 = 0; az0 <= m; az0 += ctx->kz) {
+                    KGroup g;
+                    g.col = c;
+                    g.kz0 = az0;
+                    g.n = std::min(ctx->kz, m - az0 + 1);
+                    g.pad = 0;
+                    gall.push_back(g);
+                }
+            }
+            S.n_grp = (int)gall.size() - S.grp_off;
+            if (S.n_col_half == S.n_col) S.n_grp_half = S.n_grp;
+            ctx->max_grp = std::max(ctx->max_grp, S.n_grp);
+        }
     }
     ctx->total_dof = (size_t)q_off;
     ctx->total_disp = (size_t)d_off;

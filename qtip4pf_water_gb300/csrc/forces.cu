@@ -583,10 +583,10 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
 // sums kept in shared memory.
 constexpr int KT = 128;  // threads (k groups) per block
 constexpr int CH = 32;   // sites per shared-memory chunk
-constexpr int KZ = 4;    // |kz| values per group (each covering +kz and -kz)
 
 
-template <typename R, int MODE>
+// KZ: |kz| values per group (each covering +kz and -kz), the context's group width
+template <typename R, int MODE, int KZ>
 __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
     const int sc = blockIdx.y, jb = blockIdx.z;
     const Job J = a.jobs[jb];
@@ -1013,6 +1013,15 @@ __global__ void __launch_bounds__(FT) k_kforce_f32(EvalArgs a) {
 
 template <typename R>
 size_t kforce_smem(int kmax);
+template <typename R>
+size_t ksk_smem(int kmax);
+
+// k_ksk for the context's structure-factor group width
+template <typename R, int MODE>
+void launch_ksk(const EvalArgs &a, dim3 grid, cudaStream_t s) {
+    if (a.kz == 3) k_ksk<R, MODE, 3><<<grid, KT, ksk_smem<R>(a.max_kmax), s>>>(a);
+    else k_ksk<R, MODE, 4><<<grid, KT, ksk_smem<R>(a.max_kmax), s>>>(a);
+}
 
 // the FP32 k-force kernel for the largest |kz| of the batch (the general form beyond 32)
 void launch_kforce_f32(const EvalArgs &a, dim3 grid, cudaStream_t s) {
@@ -1657,8 +1666,10 @@ void set_attrs() {
     cudaFuncSetAttribute(k_kforce_f32<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_kforce_f32<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_kforce_f32<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_ksk<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_ksk<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_ksk<R, 0, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_ksk<R, 1, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_ksk<R, 0, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_ksk<R, 1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_kforce<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_kforce<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
 }
@@ -1711,7 +1722,7 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
         cudaEventRecord(forks->fork, s);
         cudaStreamWaitEvent(forks->side[0], forks->fork, 0);
         cudaStreamWaitEvent(forks->side[1], forks->fork, 0);
-        k_ksk<R, 0><<<dim3(ktiles, a.n_sc, a.n_jobs), KT, ksk_smem<R>(a.max_kmax), forks->side[0]>>>(a);
+        launch_ksk<R, 0>(a, dim3(ktiles, a.n_sc, a.n_jobs), forks->side[0]);
         k_sk_reduce<R, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, forks->side[0]>>>(a);
         launch_kforce_f32(a, dim3(tiles, a.n_kc, a.n_jobs), forks->side[0]);
         cudaEventRecord(forks->join[0], forks->side[0]);
@@ -1730,13 +1741,13 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
         if (sizeof(R) == 4 && half_ok(a)) launch_real_half(a, s);
         else if (sizeof(R) == 4) k_real_f32<<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         else k_real<R, 0><<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
-        k_ksk<R, 0><<<dim3(ktiles, a.n_sc, a.n_jobs), KT, ksk_smem<R>(a.max_kmax), s>>>(a);
+        launch_ksk<R, 0>(a, dim3(ktiles, a.n_sc, a.n_jobs), s);
         k_sk_reduce<R, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
         if (sizeof(R) == 4) launch_kforce_f32(a, dim3(tiles, a.n_kc, a.n_jobs), s);
         else k_kforce<R, 0><<<dim3(tiles, a.n_kc, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
     } else {
         k_real<R, 1><<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
-        k_ksk<R, 1><<<dim3(ktiles, a.n_sc, a.n_jobs), KT, ksk_smem<R>(a.max_kmax), s>>>(a);
+        launch_ksk<R, 1>(a, dim3(ktiles, a.n_sc, a.n_jobs), s);
         k_sk_reduce<R, 1><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
         k_kforce<R, 1><<<dim3(tiles, a.n_kc, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
     }
@@ -1785,8 +1796,8 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
         else if (mixed) k_real_f32<<<gr, RT, 0, s>>>(a);
         else k_real<double, 0><<<gr, RT, 0, s>>>(a);
     } else if (n == "ksk") {
-        if (mixed) k_ksk<float, 0><<<gk, KT, ksk_smem<float>(a.max_kmax), s>>>(a);
-        else k_ksk<double, 0><<<gk, KT, ksk_smem<double>(a.max_kmax), s>>>(a);
+        if (mixed) launch_ksk<float, 0>(a, gk, s);
+        else launch_ksk<double, 0>(a, gk, s);
     } else if (n == "sk_reduce") {
         if (mixed) k_sk_reduce<float, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
         else k_sk_reduce<double, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
@@ -1849,12 +1860,12 @@ void launch_kwald_only(const EvalArgs &a0, bool mixed, cudaStream_t s, unsigned 
     const dim3 gr((a.max_kvec + 127) / 128, a.n_jobs);
     if (mixed) {
         k_prep<float><<<gs, 128, 0, s>>>(a);
-        k_ksk<float, 0><<<gk, KT, ksk_smem<float>(a.max_kmax), s>>>(a);
+        launch_ksk<float, 0>(a, gk, s);
         k_sk_reduce<float, 0><<<gr, 128, 0, s>>>(a);
         launch_kforce_f32(a, gf, s);
     } else {
         k_prep<double><<<gs, 128, 0, s>>>(a);
-        k_ksk<double, 0><<<gk, KT, ksk_smem<double>(a.max_kmax), s>>>(a);
+        launch_ksk<double, 0>(a, gk, s);
         k_sk_reduce<double, 0><<<gr, 128, 0, s>>>(a);
         k_kforce<double, 0><<<gf, FT, kforce_smem<double>(a.max_kmax), s>>>(a);
     }

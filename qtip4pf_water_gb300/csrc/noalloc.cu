@@ -288,6 +288,7 @@ extern "C" qtg_status qtg_kwald_noalloc(const double *sites, const double *charg
     a.max_kvec = NA_MAX_K;
     a.max_kmax = kmax;
     a.max_grp = NA_MAX_GRP;
+    a.kz = 4;  // the groups built above hold <= 4 |kz|
     a.max_batch = NA_MAX_BATCH;
     a.pos = sites;
     a.out = f_sites;

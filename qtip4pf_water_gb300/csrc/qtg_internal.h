@@ -31,7 +31,7 @@ struct SysDev {
     // the mixed MODE-0 k-space kernels skip the kx = 0, ky < 0 columns (S(-k) =
     // conj S(k) for real charges; their kx = 0, ky > 0 partners count twice):
     // those columns come last, so the kept groups, batches and k entries are prefixes
-    int n_grp_half, n_batch_half, n_kvec_half;
+    int n_grp_half, n_batch_half, n_kvec_half, n_col_half;
     int centroid_fixed;          // 1: the centroid is held fixed (centroid-constrained PIMD)
     int lj_tie_mask;             // bit d: half of box side d lies within r_cut (a half-box tie can matter)
     long long nm_off;   // doubles: P x P bead->normal-mode matrix C (y = C x)
@@ -393,6 +393,7 @@ struct EvalArgs {
     int max_mols;          // largest N over the jobs' systems (grid sizing)
     int max_kvec;          // largest k-vector count
     int max_kmax;
+    int kz;                  // |kz| values per structure-factor group (3 or 4)
     const double *pos;     // position base (jobs' pos_off are relative to it)
     double *out;           // force output base
     double *out_prop;      // mixed, optional: the same forces also written here (the propagating
