@@ -108,7 +108,7 @@ __device__ __forceinline__ void pair_terms(double r2, double kap, double kap2, d
     *ec = erfc(kap * r);
 }
 
-// ---- k_prep -------------------------------------------------------------------
+// ---- k_prep (FP64 form; the FP32 form is k_prep_f32) ---------------------------
 template <typename R>
 __global__ void __launch_bounds__(128) k_prep(EvalArgs a) {
     const Job J = a.jobs[blockIdx.y];
@@ -159,10 +159,6 @@ __global__ void __launch_bounds__(128) k_prep(EvalArgs a) {
     sv.z = (R)(frac[2] * S.box[2]);
     sv.w = (R)chg;
     reinterpret_cast<V4<R> *>(a.sites)[J.site_off + s] = sv;
-    if (sizeof(R) == 4 && a.sites_fix)
-        a.sites_fix[J.site_off + s] = make_int4((int)__double2uint_rz(frac[0] * 4294967296.0),
-                                                (int)__double2uint_rz(frac[1] * 4294967296.0),
-                                                (int)__double2uint_rz(frac[2] * 4294967296.0), __float_as_int((float)chg));
     if (J.mode == 1) {
         V4<R> tv;
         tv.x = (R)u[0];
@@ -174,33 +170,10 @@ __global__ void __launch_bounds__(128) k_prep(EvalArgs a) {
     // phase table exp(i 2 pi m frac_d), layout [(d * (kmax+1) + m) * ns + s], by
     // complex recursion from exp(i 2 pi frac_d) (as forces.cpp:233-240 does),
     // reseeded every 4 powers from a directly evaluated phase whose argument
-    // 2 m frac_d is reduced exactly (FP64 tables: in FP64; FP32 tables: in fixed
-    // point), so rounding does not accumulate with m
+    // 2 m frac_d is reduced in FP64, so rounding does not accumulate with m (the
+    // FP32 tables of k_prep_f32 reduce it exactly in fixed point)
     const int km1 = S.k_max + 1;
     V2<R> *ph = reinterpret_cast<V2<R> *>(a.phase) + J.phase_off;
-    if (sizeof(R) == 4) {
-        // FP32 tables: frac_d as a 32-bit fixed-point fraction F, so the reseeding
-        // argument 2 m frac_d mod 2 is the wrapped integer product m F, exact,
-        // taken to [-1, 1) as a signed value times 2^-31 (no FP64 per power)
-        for (int d = 0; d < 3; ++d) {
-            const unsigned F = __double2uint_rz(frac[d] * 4294967296.0);
-            float s1, c1;
-            sincospif((float)(int)F * 4.656612873077393e-10f, &s1, &c1);
-            const float qd = (d == 0) ? (float)chg : 1.f;
-            float cr = 1.f, ci = 0.f;
-            for (int m = 0; m < km1; ++m) {
-                if (m > 0 && (m & 3) == 0) sincospif((float)(int)((unsigned)m * F) * 4.656612873077393e-10f, &ci, &cr);
-                V2<R> e;
-                e.x = (R)(cr * qd);
-                e.y = (R)(ci * qd);
-                ph[(size_t)(d * km1 + m) * ns + s] = e;
-                const float nr = cr * c1 - ci * s1;
-                ci = cr * s1 + ci * c1;
-                cr = nr;
-            }
-        }
-        return;
-    }
     for (int d = 0; d < 3; ++d) {
         R s1, c1;
         {
@@ -225,6 +198,78 @@ __global__ void __launch_bounds__(128) k_prep(EvalArgs a) {
             cr = nr;
         }
     }
+}
+
+// FP32 form of k_prep with one thread per (site, dimension): each dimension of
+// the M site, the box fraction, the fixed-point fraction and the phase-table
+// rows depend on that dimension alone. Blocks are dimension-major (a block's
+// threads share d), so the phase rows are written by consecutive sites.
+__global__ void __launch_bounds__(128) k_prep_f32(EvalArgs a) {
+    const Job J = a.jobs[blockIdx.y];
+    const SysDev &S = a.sys[J.sys];
+    const int ns = S.n_sites;
+    const int tiles = (3 * a.max_mols + 127) / 128;
+    const int d = blockIdx.x / tiles;
+    const int s = (blockIdx.x - d * tiles) * 128 + threadIdx.x;
+    if (s == 0 && d == 0) a.energy[J.slot] = 0.0;
+    if (s >= ns) return;
+    const int mol = s / 3, kind = s - 3 * mol;
+    const double *q = a.pos + J.pos_off;
+    const double g = a.c.gamma_vs;
+    double x, u = 0.0;
+    if (a.sites_are_input || kind != 0) {
+        x = q[3 * s + d];
+        if (J.mode == 1) u = a.dir[J.pos_off + 3 * s + d];
+    } else {
+        // M site (forces.cpp:558-564)
+        x = g * q[9 * mol + d] + 0.5 * (1.0 - g) * (q[9 * mol + 3 + d] + q[9 * mol + 6 + d]);
+        if (J.mode == 1) {
+            const double *v = a.dir + J.pos_off;
+            u = g * v[9 * mol + d] + 0.5 * (1.0 - g) * (v[9 * mol + 3 + d] + v[9 * mol + 6 + d]);
+        }
+        // wrapped oxygen position for the Lennard-Jones kernel
+        const double t = q[9 * mol + d] * S.inv_box[d];
+        float *o = reinterpret_cast<float *>(a.opos) + 4 * ((size_t)J.site_off / 3 + mol);
+        o[d] = (float)((t - floor(t)) * S.box[d]);
+        if (d == 0) o[3] = 0.f;
+    }
+    const double chg = a.charge[S.chg_off + s];
+    const double t = x * S.inv_box[d];
+    const double frac = t - floor(t);
+    const unsigned F = __double2uint_rz(frac * 4294967296.0);
+    float *sv = reinterpret_cast<float *>(a.sites) + 4 * ((size_t)J.site_off + s);
+    sv[d] = (float)(frac * S.box[d]);
+    int *fx = reinterpret_cast<int *>(a.sites_fix + J.site_off + s);
+    fx[d] = (int)F;
+    if (d == 0) {
+        sv[3] = (float)chg;
+        fx[3] = __float_as_int((float)chg);
+    }
+    if (J.mode == 1) {
+        float *tv = reinterpret_cast<float *>(a.tan_sites) + 4 * ((size_t)J.site_off + s);
+        tv[d] = (float)u;
+        if (d == 0) tv[3] = 0.f;
+    }
+    // phase row d: exp(i 2 pi m frac) by complex recursion, reseeded every 4 powers
+    // from the exact fixed-point argument m F (see k_prep)
+    const int km1 = S.k_max + 1;
+    float2 *ph = reinterpret_cast<float2 *>(a.phase) + J.phase_off;
+    float s1, c1;
+    sincospif((float)(int)F * 4.656612873077393e-10f, &s1, &c1);
+    const float qd = (d == 0) ? (float)chg : 1.f;
+    float cr = 1.f, ci = 0.f;
+    for (int m = 0; m < km1; ++m) {
+        if (m > 0 && (m & 3) == 0) sincospif((float)(int)((unsigned)m * F) * 4.656612873077393e-10f, &ci, &cr);
+        ph[(size_t)(d * km1 + m) * ns + s] = make_float2(cr * qd, ci * qd);
+        const float nr = cr * c1 - ci * s1;
+        ci = cr * s1 + ci * c1;
+        cr = nr;
+    }
+}
+
+void launch_prep_f32(const EvalArgs &a, cudaStream_t s) {
+    const int tiles = (3 * a.max_mols + 127) / 128;
+    k_prep_f32<<<dim3(3 * tiles, a.n_jobs), 128, 0, s>>>(a);
 }
 
 // Running sum s (+ compensation c) += v, Kahan's compensated summation.
@@ -1718,7 +1763,7 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
         // forked: prep; then real space | reciprocal chain | dense LJ; then combine
         if (half_ok(a)) a.n_rj = half_chunks(a) + (3 * a.max_mols + 31) / 32 / 2;
         a.lj_plane = 1;
-        k_prep<R><<<dim3((ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
+        launch_prep_f32(a, s);
         cudaEventRecord(forks->fork, s);
         cudaStreamWaitEvent(forks->side[0], forks->fork, 0);
         cudaStreamWaitEvent(forks->side[1], forks->fork, 0);
@@ -1736,7 +1781,8 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
         if (n) *n += 7;
         return;
     }
-    k_prep<R><<<dim3((ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
+    if constexpr (sizeof(R) == 4) launch_prep_f32(a, s);
+    else k_prep<R><<<dim3((ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
     if (a.mode == 0) {
         if (sizeof(R) == 4 && half_ok(a)) launch_real_half(a, s);
         else if (sizeof(R) == 4) k_real_f32<<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
@@ -1789,7 +1835,7 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
     const dim3 gm((a.max_mols + 127) / 128, a.n_jobs), gl((a.max_mols + 3) / 4, a.n_jobs);
     const std::string n(name);
     if (n == "prep") {
-        if (mixed) k_prep<float><<<gs, 128, 0, s>>>(a);
+        if (mixed) launch_prep_f32(a, s);
         else k_prep<double><<<gs, 128, 0, s>>>(a);
     } else if (n == "real") {
         if (mixed && half_ok(a)) launch_real_half(a, s);
@@ -1859,7 +1905,7 @@ void launch_kwald_only(const EvalArgs &a0, bool mixed, cudaStream_t s, unsigned 
     const dim3 gs((ns + 127) / 128, a.n_jobs), gk(ktiles, a.n_sc, a.n_jobs), gf(tiles, a.n_kc, a.n_jobs);
     const dim3 gr((a.max_kvec + 127) / 128, a.n_jobs);
     if (mixed) {
-        k_prep<float><<<gs, 128, 0, s>>>(a);
+        launch_prep_f32(a, s);
         launch_ksk<float, 0>(a, gk, s);
         k_sk_reduce<float, 0><<<gr, 128, 0, s>>>(a);
         launch_kforce_f32(a, gf, s);
