@@ -180,6 +180,20 @@ def time_device_steps(s, steps, warmup, flush):
     return sum(ms) / 1e3, s.ctx.kernel_launches() - launches0
 
 
+def replica_timing(t_local, steps, world, dist=None, device="cpu"):
+    """Replicas only: every rank times its own system; the job's time is the
+    maximum over ranks, and its throughput is the world replicas' aggregate
+    ns/day at that time. Returns (time, value)."""
+    t = t_local
+    if dist is not None and world > 1:
+        import torch
+
+        x = torch.tensor([t_local], dtype=torch.float64, device=device)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        t = float(x.item())
+    return t, ns_per_day(t / steps) * world
+
+
 def run_gpu(args):
     import torch
 
@@ -208,13 +222,8 @@ def run_gpu(args):
     t_mix, launches = time_device_steps(mix, args.steps, args.warmup, flush)
     torch.cuda.synchronize()
     sampler.stop()
-    t_tot = t_mix
-    if dist:
-        t = torch.tensor([t_mix], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_tot = float(t.item())
+    t_tot, value = replica_timing(t_mix, args.steps, world, dist, "cuda")
     ms_step = t_tot / args.steps * 1e3
-    value = ns_per_day(t_tot / args.steps) * world  # replicas: world independent systems
     est = mix.estimators()
     fin = bool(np.all(np.isfinite(est["conserved"])))
 
