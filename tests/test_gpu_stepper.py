@@ -124,9 +124,9 @@ def test_run_before_init_is_a_state_error(gpu_lib):
 
 
 def test_counter_based_noise_is_reproducible(gpu_lib):
-    """Two contexts with identical descriptors draw the same thermostat noise, so
-    their NVT trajectories agree to the round-off of the force summation (the LJ
-    term accumulates with FP64 atomics, whose order is not fixed)."""
+    """Two contexts with identical descriptors draw the same thermostat noise and
+    sum their forces and system sums in a fixed order, so their NVT trajectories
+    agree bit for bit."""
     q = gpu_lib
     st = q.seeded_start(27, 4, 298.0, seed=81)
     outs = []
@@ -137,4 +137,4 @@ def test_counter_based_noise_is_reproducible(gpu_lib):
         s.ctx.run_steps(20, is_nvt=True)
         s.ctx.sync()
         outs.append(s.get_state()["q"])
-    assert np.abs(outs[0] - outs[1]).max() < 1e-9
+    assert np.array_equal(outs[0], outs[1])
