@@ -220,6 +220,7 @@ struct qtg_ctx {
     cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join = nullptr;
     Forks forks{};            // branches of a mixed force evaluation (real | k-space | LJ)
     float4 *ljf = nullptr;    // dense LJ oxygen forces per molecule and slot
+    float *intra = nullptr;   // intramolecular forces, 18 floats per molecule and slot
     int4 *sites_fix = nullptr;  // fixed-point site fractions per slot (half-interaction real space)
     std::string err;
     Consts K;
@@ -362,6 +363,7 @@ EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, d
     a.sites_fix = c->sites_fix;
     a.opos = c->opos;
     a.ljf = c->ljf;
+    a.intra = c->intra;
     a.phase = c->phase;
     a.tan_sites = c->tan_sites;
     a.part = c->part;
@@ -1139,6 +1141,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         ctx->opos = tmp;
     }
     AL(ctx->ljf, ctx->total_sites / 3);
+    AL(ctx->intra, 6 * ctx->total_sites);
     AL(ctx->sites_fix, ctx->total_sites);
     AL(ctx->part, (size_t)MAX_PART * 3 * ctx->total_sites);
     AL(ctx->skp, (size_t)MAX_SC * ctx->total_k);
@@ -1253,7 +1256,7 @@ void qtg_destroy(qtg_ctx *ctx) {
                     ctx->phase, ctx->opos, ctx->part, ctx->skp, ctx->dskp, ctx->wsk, ctx->wdsk, ctx->energy, ctx->energy_aux,
                     ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
-                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf, ctx->fin_ticket, ctx->sites_fix};
+                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf, ctx->fin_ticket, ctx->sites_fix, ctx->intra};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->box) cudaFreeHost(ctx->box);

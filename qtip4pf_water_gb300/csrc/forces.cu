@@ -1231,10 +1231,117 @@ __device__ __forceinline__ float ewald_same_mol_f32(const float *rd, float qiqj,
     return e;
 }
 
+// Intramolecular terms of molecule m of job J (mixed): the same-molecule Ewald
+// pairs (erfc - 1) as site-force increments fs[9] (M, H1, H2), the quartic Morse
+// bonds and the HOH angle as atom forces fa[9] (O, H1, H2); returns their energy.
+__device__ double intra_f32(const EvalArgs &a, const Job &J, const SysDev &S, int m, float *fs, float *fa) {
+    const double *q = a.pos + J.pos_off + 9 * m;
+    const Consts &C = a.c;
+    const double g = C.gamma_vs, h = 0.5 * (1.0 - g);
+    const double *cq = a.charge + S.chg_off + 3 * m;
+    double e = 0.0;
+    // charge sites M, H1, H2 (forces.cpp:558-564) and their differences
+    double site[9];
+    for (int d = 0; d < 3; ++d) {
+        site[d] = g * q[d] + h * (q[3 + d] + q[6 + d]);
+        site[3 + d] = q[3 + d];
+        site[6 + d] = q[6 + d];
+    }
+    float dm1[3], dm2[3], d12[3];
+    for (int d = 0; d < 3; ++d) {
+        dm1[d] = (float)(site[d] - site[3 + d]);
+        dm2[d] = (float)(site[d] - site[6 + d]);
+        d12[d] = (float)(site[3 + d] - site[6 + d]);
+    }
+    min_image3f(dm1, S);
+    min_image3f(dm2, S);
+    min_image3f(d12, S);
+    float ef = ewald_same_mol_f32(dm1, (float)(cq[0] * cq[1]), S, fs, fs + 3);
+    ef += ewald_same_mol_f32(dm2, (float)(cq[0] * cq[2]), S, fs, fs + 6);
+    ef += ewald_same_mol_f32(d12, (float)(cq[1] * cq[2]), S, fs + 3, fs + 6);
+    e += (double)ef;
+    // quartic Morse bonds (forces.cpp:65-93, :519-551)
+    double rad[3], rbd[3];
+    for (int d = 0; d < 3; ++d) {
+        rad[d] = q[d] - q[3 + d];
+        rbd[d] = q[d] - q[6 + d];
+    }
+    min_image3(rad, S);
+    min_image3(rbd, S);
+    float ra[3], rb[3], xs[2], ls[2];
+    for (int d = 0; d < 3; ++d) {
+        ra[d] = (float)rad[d];
+        rb[d] = (float)rbd[d];
+    }
+    for (int bnd = 0; bnd < 2; ++bnd) {
+        const double *r = bnd ? rbd : rad;
+        const double s2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        const float l0 = sqrtf((float)s2);
+        const float corr = (float)(s2 - (double)l0 * (double)l0) * (0.5f / l0);
+        xs[bnd] = (float)((double)l0 - C.roheq) + corr;
+        ls[bnd] = l0 + corr;
+    }
+    const float ar2 = (float)C.ar2, ar3 = (float)C.ar3, ar4 = (float)C.ar4fac, Dr = (float)C.Dr;
+    float eb = 0.f;
+    for (int bnd = 0; bnd < 2; ++bnd) {
+        const float *r = bnd ? rb : ra;
+        const float x = xs[bnd], x2 = x * x, x3 = x2 * x, x4 = x2 * x2;
+        eb += Dr * (ar2 * x2 - ar3 * x3 + ar4 * x4);
+        const float gg = (2.f * ar2 * x - 3.f * ar3 * x2 + 4.f * ar4 * x3) * Dr / ls[bnd];
+        for (int d = 0; d < 3; ++d) {
+            fa[d] -= gg * r[d];
+            fa[3 + 3 * bnd + d] += gg * r[d];
+        }
+    }
+    e += (double)eb;
+    // harmonic HOH angle (forces.cpp:96-138)
+    const float la = ls[0], lb = ls[1];
+    const float dot = ra[0] * rb[0] + ra[1] * rb[1] + ra[2] * rb[2];
+    const float ia = 1.f / la, ib = 1.f / lb, iab = ia * ib;
+    const float c = dot * iab;
+    const float dacos = 1.f / sqrtf(1.f - c * c);
+    const float ca = dot * ia * ia * iab, cb = dot * ib * ib * iab;
+    const float dth = acosf(c) - (float)C.theta_eq;
+    e += 0.5 * C.ktheta * (double)dth * (double)dth;
+    const float gp = (float)C.ktheta * dth * dacos;
+    for (int d = 0; d < 3; ++d) {
+        fa[d] += gp * (iab * (ra[d] + rb[d]) - ca * ra[d] - cb * rb[d]);
+        fa[3 + d] -= gp * (iab * rb[d] - ca * ra[d]);
+        fa[6 + d] -= gp * (iab * ra[d] - cb * rb[d]);
+    }
+    return e;
+}
+
+// The intramolecular terms of a forked mixed evaluation, on a branch beside the
+// pair kernels (they need positions only): per molecule 18 floats (fs, fa) for
+// k_combine_f32, the energy (with the Ewald self term) into the job's slot.
+__global__ void __launch_bounds__(128) k_intra_f32(EvalArgs a) {
+    const Job J = a.jobs[blockIdx.y];
+    const SysDev &S = a.sys[J.sys];
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (blockIdx.x * blockDim.x >= S.n_mols) return;
+    __shared__ double red[4];
+    double e = 0.0;
+    if (m < S.n_mols) {
+        float fs[9], fa[9];
+        for (int k = 0; k < 9; ++k) fs[k] = fa[k] = 0.f;
+        e = intra_f32(a, J, S, m, fs, fa);
+        if (m == 0) e -= S.self_energy;
+        float *o = a.intra + 18 * ((size_t)J.site_off / 3 + m);
+        for (int k = 0; k < 9; ++k) {
+            o[k] = fs[k];
+            o[9 + k] = fa[k];
+        }
+    }
+    const double t = block_sum(e, red);
+    if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
+}
+
 // CMB molecules per 128-thread block: first every thread sums site-force
 // components over the partial planes (one component a thread, plane order,
 // Kahan-compensated: the same sums as one thread per molecule would form, spread
-// over the block), then one thread per molecule adds the short-range terms.
+// over the block), then one thread per molecule adds the intramolecular and
+// Lennard-Jones terms and applies the M-site chain rule.
 constexpr int CMB = 32;
 __global__ void __launch_bounds__(128) k_combine_f32(EvalArgs a) {
     const int jb = blockIdx.y;
@@ -1274,81 +1381,18 @@ __global__ void __launch_bounds__(128) k_combine_f32(EvalArgs a) {
         for (int k = 0; k < 9; ++k) fs[k] = fsum[9 * threadIdx.x + k];
         float fa[9];
         for (int k = 0; k < 9; ++k) fa[k] = 0.f;
-        if (J.mode == 0) {
-            const Consts &C = a.c;
-            const double g = C.gamma_vs, h = 0.5 * (1.0 - g);
-            const double *cq = a.charge + S.chg_off + 3 * m;
-            // charge sites M, H1, H2 (forces.cpp:558-564) and their differences
-            double site[9];
-            for (int d = 0; d < 3; ++d) {
-                site[d] = g * q[d] + h * (q[3 + d] + q[6 + d]);
-                site[3 + d] = q[3 + d];
-                site[6 + d] = q[6 + d];
+        if (J.mode == 0 && a.intra_plane) {  // computed beside the pair kernels (k_intra_f32)
+            const float *o = a.intra + 18 * ((size_t)J.site_off / 3 + m);
+            for (int k = 0; k < 9; ++k) {
+                fs[k] += o[k];
+                fa[k] = o[9 + k];
             }
-            float dm1[3], dm2[3], d12[3];
-            for (int d = 0; d < 3; ++d) {
-                dm1[d] = (float)(site[d] - site[3 + d]);
-                dm2[d] = (float)(site[d] - site[6 + d]);
-                d12[d] = (float)(site[3 + d] - site[6 + d]);
-            }
-            min_image3f(dm1, S);
-            min_image3f(dm2, S);
-            min_image3f(d12, S);
-            float ef = ewald_same_mol_f32(dm1, (float)(cq[0] * cq[1]), S, fs, fs + 3);
-            ef += ewald_same_mol_f32(dm2, (float)(cq[0] * cq[2]), S, fs, fs + 6);
-            ef += ewald_same_mol_f32(d12, (float)(cq[1] * cq[2]), S, fs + 3, fs + 6);
-            e += (double)ef;
-            // quartic Morse bonds (forces.cpp:65-93, :519-551)
-            double rad[3], rbd[3];
-            for (int d = 0; d < 3; ++d) {
-                rad[d] = q[d] - q[3 + d];
-                rbd[d] = q[d] - q[6 + d];
-            }
-            min_image3(rad, S);
-            min_image3(rbd, S);
-            float ra[3], rb[3], xs[2], ls[2];
-            for (int d = 0; d < 3; ++d) {
-                ra[d] = (float)rad[d];
-                rb[d] = (float)rbd[d];
-            }
-            for (int bnd = 0; bnd < 2; ++bnd) {
-                const double *r = bnd ? rbd : rad;
-                const double s2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
-                const float l0 = sqrtf((float)s2);
-                const float corr = (float)(s2 - (double)l0 * (double)l0) * (0.5f / l0);
-                xs[bnd] = (float)((double)l0 - C.roheq) + corr;
-                ls[bnd] = l0 + corr;
-            }
-            const float ar2 = (float)C.ar2, ar3 = (float)C.ar3, ar4 = (float)C.ar4fac, Dr = (float)C.Dr;
-            float eb = 0.f;
-            for (int bnd = 0; bnd < 2; ++bnd) {
-                const float *r = bnd ? rb : ra;
-                const float x = xs[bnd], x2 = x * x, x3 = x2 * x, x4 = x2 * x2;
-                eb += Dr * (ar2 * x2 - ar3 * x3 + ar4 * x4);
-                const float gg = (2.f * ar2 * x - 3.f * ar3 * x2 + 4.f * ar4 * x3) * Dr / ls[bnd];
-                for (int d = 0; d < 3; ++d) {
-                    fa[d] -= gg * r[d];
-                    fa[3 + 3 * bnd + d] += gg * r[d];
-                }
-            }
-            e += (double)eb;
-            // harmonic HOH angle (forces.cpp:96-138)
-            {
-                const float la = ls[0], lb = ls[1];
-                const float dot = ra[0] * rb[0] + ra[1] * rb[1] + ra[2] * rb[2];
-                const float ia = 1.f / la, ib = 1.f / lb, iab = ia * ib;
-                const float c = dot * iab;
-                const float dacos = 1.f / sqrtf(1.f - c * c);
-                const float ca = dot * ia * ia * iab, cb = dot * ib * ib * iab;
-                const float dth = acosf(c) - (float)C.theta_eq;
-                e += 0.5 * C.ktheta * (double)dth * (double)dth;
-                const float gp = (float)C.ktheta * dth * dacos;
-                for (int d = 0; d < 3; ++d) {
-                    fa[d] += gp * (iab * (ra[d] + rb[d]) - ca * ra[d] - cb * rb[d]);
-                    fa[3 + d] -= gp * (iab * rb[d] - ca * ra[d]);
-                    fa[6 + d] -= gp * (iab * ra[d] - cb * rb[d]);
-                }
-            }
+        } else if (J.mode == 0) {  // the same sums in the same order as k_intra_f32's
+            float fi[9];
+            for (int k = 0; k < 9; ++k) fi[k] = 0.f;
+            e += intra_f32(a, J, S, m, fi, fa);
+            if (m == 0) e -= S.self_energy;
+            for (int k = 0; k < 9; ++k) fs[k] += fi[k];
         }
         // M-site chain rule (forces.cpp:613-619); the dense Lennard-Jones force of a
         // forked evaluation joins the oxygen here
@@ -1375,8 +1419,7 @@ __global__ void __launch_bounds__(128) k_combine_f32(EvalArgs a) {
             }
         }
     }
-    if (J.mode == 0) {
-        if (m == 0) e -= S.self_energy;
+    if (J.mode == 0 && !a.intra_plane) {
         const double t = block_sum(e, red);
         if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
     }
@@ -1772,13 +1815,17 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
         launch_kforce_f32(a, dim3(tiles, a.n_kc, a.n_jobs), forks->side[0]);
         cudaEventRecord(forks->join[0], forks->side[0]);
         launch_lj_dense(a, forks->side[1]);
+        if (a.intra) {
+            a.intra_plane = 1;
+            k_intra_f32<<<dim3((a.max_mols + 127) / 128, a.n_jobs), 128, 0, forks->side[1]>>>(a);
+        }
         cudaEventRecord(forks->join[1], forks->side[1]);
         if (half_ok(a)) launch_real_half(a, s);
         else k_real_f32<<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         cudaStreamWaitEvent(s, forks->join[0], 0);
         cudaStreamWaitEvent(s, forks->join[1], 0);
         k_combine_f32<<<dim3((a.max_mols + CMB - 1) / CMB, a.n_jobs), 128, 0, s>>>(a);
-        if (n) *n += 7;
+        if (n) *n += a.intra_plane ? 8 : 7;
         return;
     }
     if constexpr (sizeof(R) == 4) launch_prep_f32(a, s);

@@ -415,6 +415,8 @@ struct EvalArgs {
     void *opos;            // wrapped oxygen positions, 4 reals per molecule, per slot
     float4 *ljf;           // dense Lennard-Jones oxygen forces, per molecule, per slot (lj_plane)
     int lj_plane;          // 1: k_lj_dense writes ljf and k_combine_f32 adds it to the O force
+    float *intra;          // mixed: intramolecular site and atom forces, 18 floats per molecule and slot
+    int intra_plane;       // 1: k_intra_f32 wrote intra (and the energy) and k_combine_f32 adds it
     void *phase;           // complex phase tables, per slot
     void *tan_sites;       // tangent of the site positions (mode 1), per slot
     double *part;          // partial site forces [MAX_PART][total_sites][3]
