@@ -952,15 +952,17 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     // standing for +kz and -kz), one thread each, 128 threads a block. The width
     // (3 or 4) is the one whose launch does less work by a simple model: whole
     // blocks of threads, each paying the column factor (~7 instructions a site) and
-    // ~9 a |kz|, over every system's half set, sites and beads.
+    // ~9 a |kz| (mixed, the three-multiplication form: ~8 and ~5), over every
+    // system's half set, sites and beads.
     {
+        const double per_col = ctx->mixed ? 8.0 : 7.0, per_kz = ctx->mixed ? 5.0 : 9.0;
         double cost[2] = {0.0, 0.0};
         for (int w = 0; w < 2; ++w) {
             const int kz = 3 + w;
             for (const SysDev &S : ctx->sys_h) {
                 long long g = 0;
                 for (int c = 0; c < S.n_col_half; ++c) g += (call[S.col_off + c].m + kz) / kz;
-                cost[w] += (double)((g + 127) / 128 * 128) * (7.0 + 9.0 * kz) * S.n_sites * S.n_beads;
+                cost[w] += (double)((g + 127) / 128 * 128) * (per_col + per_kz * kz) * S.n_sites * S.n_beads;
             }
         }
         ctx->kz = cost[0] < cost[1] ? 3 : 4;

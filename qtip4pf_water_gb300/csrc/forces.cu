@@ -626,11 +626,32 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
 // site is formed once and multiplied by Z and conj(Z) with shared products. Sites are staged through shared memory in chunks of CH; each
 // chunk's partial sums (registers, working precision) are added to FP64 running
 // sums kept in shared memory.
+// Asynchronous global -> shared copies (cp.async) of B = 8 or 16 bytes; an invalid
+// source copies nothing and zero-fills the destination.
+template <int B>
+__device__ __forceinline__ void cp_async(void *dst, const void *src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    const int n = valid ? B : 0;
+    if constexpr (B == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(n) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(d), "l"(src), "n"(B), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 constexpr int KT = 128;  // threads (k groups) per block
 constexpr int CH = 32;   // sites per shared-memory chunk
 
 
-// KZ: |kz| values per group (each covering +kz and -kz), the context's group width
+// KZ: |kz| values per group (each covering +kz and -kz), the context's group width.
+// The FP32 energy/force form (G3) accumulates, per |kz| and with A = X Y = Ar + i Ai
+// the site's column factor, the four sums T1 = sum Ar Zr, T2 = sum Ai Zi,
+// U = sum (Ar + Ai) Zr and V = sum (Ar + Ai) Zi (Gauss's three-multiplication
+// complex product, whose third products (Ar + Ai)(Zr +- Zi) are U +- V, with T1 and
+// T2 shared by +kz and -kz): four FMAs for the pair instead of eight. Then
+// S(+kz) = T1 - T2 + i (U + V - T1 - T2) and S(-kz) = T1 + T2 + i (U - V - T1 + T2).
 template <typename R, int MODE, int KZ>
 __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
     const int sc = blockIdx.y, jb = blockIdx.z;
@@ -644,8 +665,10 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
     const bool act = t < ng;
     const int s0 = chunk_lo(ns, sc, a.n_sc), s1 = chunk_lo(ns, sc + 1, a.n_sc);
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    V4<R> *ush = reinterpret_cast<V4<R> *>(smem_raw);  // [CH] (mode 1)
-    V2<R> *tab = reinterpret_cast<V2<R> *>(ush + CH);  // [3*km1][CH+1]
+    // two buffers (chunk i computed while chunk i + 1 is copied in)
+    V4<R> *ush = reinterpret_cast<V4<R> *>(smem_raw);      // [2][CH] (mode 1)
+    V2<R> *tab = reinterpret_cast<V2<R> *>(ush + 2 * CH);  // [2][3*km1][CH+1]
+    constexpr bool G3 = sizeof(R) == 4 && MODE == 0;
     KGroup G;
     G.col = G.kz0 = G.n = 0;
     KCol C;
@@ -674,22 +697,39 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
         for (int h = 0; h < 2; ++h) Sr[g][h] = Si[g][h] = Cr[g][h] = Ci[g][h] = dSr[g][h] = dSi[g][h] = dCr[g][h] = dCi[g][h] = (R)0;
     const V2<R> *ph = reinterpret_cast<const V2<R> *>(a.phase) + J.phase_off;
     const V4<R> *tans = reinterpret_cast<const V4<R> *>(a.tan_sites) + J.site_off;
-    const int rows = 3 * km1;
-    for (int c0 = s0; c0 < s1; c0 += CH) {
-        __syncthreads();
+    const int rows = 3 * km1, nchunk = s1 > s0 ? (s1 - s0 + CH - 1) / CH : 0;
+    // copies of chunk ci's phase rows (and tangents) into buffer ci & 1, zero past s1
+    auto stage = [&](int ci) {
+        const int c0 = s0 + ci * CH;
+        V2<R> *tb = tab + (ci & 1) * rows * (CH + 1);
         for (int idx = threadIdx.x; idx < rows * CH; idx += KT) {
             const int row = idx / CH, c = idx - row * CH, s = c0 + c;
-            V2<R> v;
-            v.x = v.y = (R)0;
-            if (s < s1) v = ph[(size_t)row * ns + s];
-            tab[row * (CH + 1) + c] = v;
+            cp_async<sizeof(V2<R>)>(tb + row * (CH + 1) + c, ph + (size_t)row * ns + min(s, s1 - 1), s < s1);
         }
         if (MODE == 1 && threadIdx.x < CH) {
-            V4<R> z;
-            z.x = z.y = z.z = z.w = (R)0;
-            ush[threadIdx.x] = (c0 + threadIdx.x < s1) ? tans[c0 + threadIdx.x] : z;
+            const int s = c0 + threadIdx.x;
+            const V4<R> *src = tans + min(s, s1 - 1);
+            V4<R> *dst = ush + (ci & 1) * CH + threadIdx.x;
+            if constexpr (sizeof(V4<R>) == 16) {
+                cp_async<16>(dst, src, s < s1);
+            } else {
+                cp_async<16>(dst, src, s < s1);
+                cp_async<16>(reinterpret_cast<unsigned char *>(dst) + 16, reinterpret_cast<const unsigned char *>(src) + 16,
+                             s < s1);
+            }
         }
-        __syncthreads();
+        cp_async_commit();
+    };
+    if (nchunk > 0) stage(0);
+    for (int ci = 0; ci < nchunk; ++ci) {
+        const int c0 = s0 + ci * CH;
+        __syncthreads();  // every thread is done with buffer (ci + 1) & 1
+        if (ci + 1 < nchunk) stage(ci + 1);
+        else cp_async_commit();
+        cp_async_wait<1>();  // this thread's copies of chunk ci have landed
+        __syncthreads();     // and every other thread's
+        const V2<R> *tab_c = tab + (ci & 1) * rows * (CH + 1);
+        const V4<R> *ush_c = ush + (ci & 1) * CH;
         const int nc = min(CH, s1 - c0);
         R sr[KZ][2], si[KZ][2], dsr[KZ][2], dsi[KZ][2];
 #pragma unroll
@@ -697,18 +737,30 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
 #pragma unroll
             for (int h = 0; h < 2; ++h) sr[g][h] = si[g][h] = dsr[g][h] = dsi[g][h] = (R)0;
         auto site = [&](int c) {
-            const V2<R> x = tab[ax * (CH + 1) + c], y = tab[(km1 + ay) * (CH + 1) + c];
+            const V2<R> x = tab_c[ax * (CH + 1) + c], y = tab_c[(km1 + ay) * (CH + 1) + c];
             const R yi = sy * y.y;
             const R pr = x.x * y.x - x.y * yi, pi = x.x * yi + x.y * y.x;
+            if constexpr (G3) {
+                const float ps = (float)(pr + pi);
+#pragma unroll
+                for (int g = 0; g < KZ; ++g) {
+                    const V2<R> z = tab_c[zrow[g] + c];
+                    sr[g][0] = fmaf((float)pr, (float)z.x, sr[g][0]);  // T1
+                    sr[g][1] = fmaf((float)pi, (float)z.y, sr[g][1]);  // T2
+                    si[g][0] = fmaf(ps, (float)z.x, si[g][0]);         // U
+                    si[g][1] = fmaf(ps, (float)z.y, si[g][1]);         // V
+                }
+                return;
+            }
             R kxyu = (R)0, uz = (R)0;
             if (MODE == 1) {
-                const V4<R> u = ush[c];
+                const V4<R> u = ush_c[c];
                 kxyu = kx * u.x + ky * u.y;
                 uz = u.z;
             }
 #pragma unroll
             for (int g = 0; g < KZ; ++g) {
-                const V2<R> z = tab[zrow[g] + c];
+                const V2<R> z = tab_c[zrow[g] + c];
                 if (MODE == 0) {
                     // A Z (kz = +az) and A conj(Z) (kz = -az) accumulated by FMAs alone
                     sr[g][0] = fma(pr, z.x, sr[g][0]);
@@ -764,10 +816,19 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
                     if (h == 1 && az == 0) continue;  // kz = 0 has one entry
                     const int kz = h ? -az : az;
                     const size_t at = (size_t)sc * a.total_k + J.sk_off + C.k_begin + (kz + C.m);
-                    if (sizeof(R) == 4 && MODE == 0)  // FP32 form: the compensated pair (S, C) itself
-                        reinterpret_cast<float4 *>(a.skp)[at] =
-                            make_float4((float)Sr[g][h], (float)Si[g][h], (float)Cr[g][h], (float)Ci[g][h]);
-                    else
+                    if constexpr (G3) {
+                        // FP32 form: the compensated pair (S, C) of S(kz) itself, from the
+                        // (sum, compensation) pairs of T1, T2, U and V
+                        const float t1 = (float)Sr[g][0], t2 = (float)Sr[g][1], u1 = (float)Cr[g][0], u2 = (float)Cr[g][1];
+                        const float us = (float)Si[g][0], vs = (float)Si[g][1], uc = (float)Ci[g][0], vc = (float)Ci[g][1];
+                        float4 o;
+                        if (h == 0) {
+                            o = make_float4(t1 - t2, ((us + vs) - t1) - t2, u1 - u2, ((uc + vc) - u1) - u2);
+                        } else {
+                            o = make_float4(t1 + t2, ((us - vs) - t1) + t2, u1 + u2, ((uc - vc) - u1) + u2);
+                        }
+                        reinterpret_cast<float4 *>(a.skp)[at] = o;
+                    } else
                         a.skp[at] = make_double2((double)Sr[g][h] - (double)Cr[g][h], (double)Si[g][h] - (double)Ci[g][h]);
                     if (MODE == 1)
                         a.dskp[at] = make_double2((double)dSr[g][h] - (double)dCr[g][h],
@@ -1739,7 +1800,7 @@ __global__ void __launch_bounds__(256) k_fp32_probe(float *out, int iters) {
 
 template <typename R>
 size_t ksk_smem(int kmax) {
-    return CH * sizeof(V4<R>) + (size_t)3 * (kmax + 1) * (CH + 1) * sizeof(V2<R>);
+    return 2 * (CH * sizeof(V4<R>) + (size_t)3 * (kmax + 1) * (CH + 1) * sizeof(V2<R>));
 }
 template <typename R>
 size_t kforce_smem(int kmax) {
