@@ -871,6 +871,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         S.kappa_sqf = (float)(kappa * kappa);
         S.rc_sqf = (float)S.rc_sq;
         S.ewald_preff = (float)S.ewald_pref;
+        set_float_consts(S);
         S.r_cut_sq = K.r_cut_sq;
         S.r_skin_sq = K.r_skin_sq;
         S.skin_margin = K.r_skin - K.r_cut;

@@ -483,13 +483,12 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
     // fractions is the minimum image, one integer subtraction and one conversion
     // a component (scaled by L / 2^32)
     const int4 *sites = a.sites_fix + J.site_off;
-    const float X0 = (float)(S.box[0] * 2.3283064365386963e-10), X1 = (float)(S.box[1] * 2.3283064365386963e-10),
-                X2 = (float)(S.box[2] * 2.3283064365386963e-10);
-    const float rc2 = (float)S.rc_sq, ka = (float)(0.3275911 * S.kappa);
-    const float cex = (float)(-S.kappa * S.kappa * 1.4426950408889634), pref = (float)S.ewald_pref;
+    const float X0 = S.fixf[0], X1 = S.fixf[1], X2 = S.fixf[2];
+    const float rc2 = S.rc_sqf, ka = S.kaf, cex = S.cexf, pref = S.ewald_preff;
     const int s = tJ * 32 + lane, ms = s / 3;
     const bool vs = s < ns;
-    __shared__ int4 vis[HW][32];
+    // the visited tile twice over, so that step r of lane l reads entry l + r
+    __shared__ int4 vis[HW][64];
     int4 ps = make_int4(0, 0, 0, 0);
     if (vs) ps = sites[s];
     const float qs = __int_as_float(ps.w);
@@ -561,22 +560,66 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
                 // the visited sites are read from the warp's shared-memory copy (one
                 // 16-byte load a step); only their force accumulators rotate
                 vis[warp][lane] = pm;
+                vis[warp][lane + 32] = pm;
                 __syncwarp();
+                const int4 *vr = &vis[warp][lane];
+                const int nx = (lane + 1) & 31;
+                if (S.fix_cubic) {
+                    // cubic box: distances in fixed-point units u = L / 2^32 (the integer
+                    // differences themselves), constants scaled to match; forces come out
+                    // in units of 1 / u^2 and energies of 1 / u, rescaled once at the end
+                    const float rc2u = S.rc2u, cexu = S.cexu, kau = S.kau, prefu = S.prefu;
+                    float eu = 0.f;
 #pragma unroll 4
-                for (int r = 0; r < 32; ++r) {
-                    const int4 pv = vis[warp][(lane + r) & 31];
-                    float dx, dy, dz, w;
-                    e += pair_nb(pv, dx, dy, dz, w);
-                    fx = fmaf(w, dx, fx);
-                    fy = fmaf(w, dy, fy);
-                    fz = fmaf(w, dz, fz);
-                    mx = fmaf(-w, dx, mx);
-                    my = fmaf(-w, dy, my);
-                    mz = fmaf(-w, dz, mz);
-                    const int nx = (lane + 1) & 31;
-                    mx = __shfl_sync(0xffffffffu, mx, nx);
-                    my = __shfl_sync(0xffffffffu, my, nx);
-                    mz = __shfl_sync(0xffffffffu, mz, nx);
+                    for (int r = 0; r < 32; ++r) {
+                        const int4 pv = vr[r];
+                        const float dx = (float)(int)((unsigned)ps.x - (unsigned)pv.x);
+                        const float dy = (float)(int)((unsigned)ps.y - (unsigned)pv.y);
+                        const float dz = (float)(int)((unsigned)ps.z - (unsigned)pv.z);
+                        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                        const bool in = r2 < rc2u;
+                        const float rr = in ? r2 : rc2u;
+                        const float iv = rsqrt_approx(rr);
+                        const float ex = ex2_approx(cexu * rr);
+                        const float t = rcp_approx(fmaf(kau, rr * iv, 1.0f));
+                        const float A = (t * as_poly(t)) * ex * iv;
+                        const float qq = in ? qs * __int_as_float(pv.w) : 0.f;
+                        const float w = qq * fmaf(prefu, ex, A) * (iv * iv);
+                        eu = fmaf(qq, A, eu);
+                        fx = fmaf(w, dx, fx);
+                        fy = fmaf(w, dy, fy);
+                        fz = fmaf(w, dz, fz);
+                        mx = fmaf(-w, dx, mx);
+                        my = fmaf(-w, dy, my);
+                        mz = fmaf(-w, dz, mz);
+                        mx = __shfl_sync(0xffffffffu, mx, nx);
+                        my = __shfl_sync(0xffffffffu, my, nx);
+                        mz = __shfl_sync(0xffffffffu, mz, nx);
+                    }
+                    const float s2 = S.s2u;
+                    fx *= s2;
+                    fy *= s2;
+                    fz *= s2;
+                    mx *= s2;
+                    my *= s2;
+                    mz *= s2;
+                    e = fmaf(eu, S.invu, e);
+                } else {
+#pragma unroll 4
+                    for (int r = 0; r < 32; ++r) {
+                        const int4 pv = vr[r];
+                        float dx, dy, dz, w;
+                        e += pair_nb(pv, dx, dy, dz, w);
+                        fx = fmaf(w, dx, fx);
+                        fy = fmaf(w, dy, fy);
+                        fz = fmaf(w, dz, fz);
+                        mx = fmaf(-w, dx, mx);
+                        my = fmaf(-w, dy, my);
+                        mz = fmaf(-w, dz, mz);
+                        mx = __shfl_sync(0xffffffffu, mx, nx);
+                        my = __shfl_sync(0xffffffffu, my, nx);
+                        mz = __shfl_sync(0xffffffffu, mz, nx);
+                    }
                 }
                 __syncwarp();
             } else if (active) {

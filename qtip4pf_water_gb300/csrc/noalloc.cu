@@ -271,6 +271,7 @@ extern "C" qtg_status qtg_kwald_noalloc(const double *sites, const double *charg
         S.inv_boxf[d] = (float)S.inv_box[d];
         p.bk[d] = 2.0 * PI_REF / box_bohr[d];
     }
+    set_float_consts(S);
     p.kc_sq = kc * kc;
     p.quart = 0.25 / (kappa * kappa);
     p.kmax = kmax;

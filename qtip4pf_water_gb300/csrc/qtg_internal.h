@@ -50,8 +50,36 @@ struct SysDev {
     double beta, beta_n, omega_psq, dt, halfdt, eps_sc, c1_centroid, inv_sqrt_beta_n;
     float boxf[3], inv_boxf[3];
     float kappaf, rc_sqf, ewald_preff, kappa_sqf;
+    float kbf[3];   // 2 pi / L_d, the reciprocal-lattice steps
+    // real space (FP32): fixf[d] = L_d / 2^32, one unit of a 32-bit fixed-point box
+    // fraction; ka = 0.3275911 kappa (Abramowitz & Stegun 7.1.26), cex = -kappa^2
+    // log2(e). A cubic box (fix_cubic) also has the constants in fixed-point units
+    // (u = L / 2^32): r_c^2 / u^2, cex u^2, ka u, the Ewald prefactor times u, 1 / u^2
+    // and 1 / u, so the pair loop needs no scaling of its integer differences.
+    float fixf[3], kaf, cexf;
+    int fix_cubic;
+    float rc2u, cexu, kau, prefu, s2u, invu;
     unsigned long long seed;
 };
+
+// The FP32 constants above, from the FP64 ones (host).
+inline void set_float_consts(SysDev &S) {
+    const double two32 = 2.3283064365386963e-10, pi = PI_REF;
+    for (int d = 0; d < 3; ++d) {
+        S.kbf[d] = (float)(2.0 * pi * S.inv_box[d]);
+        S.fixf[d] = (float)(S.box[d] * two32);
+    }
+    S.kaf = (float)(0.3275911 * S.kappa);
+    S.cexf = (float)(-S.kappa * S.kappa * 1.4426950408889634);
+    S.fix_cubic = S.box[0] == S.box[1] && S.box[1] == S.box[2];
+    const double u = S.box[0] * two32;
+    S.rc2u = (float)(S.rc_sq / (u * u));
+    S.cexu = (float)(-S.kappa * S.kappa * 1.4426950408889634 * u * u);
+    S.kau = (float)(0.3275911 * S.kappa * u);
+    S.prefu = (float)(S.ewald_pref * u);
+    S.s2u = (float)(1.0 / (u * u));
+    S.invu = (float)(1.0 / u);
+}
 
 // Per normal mode k of a system: free ring-polymer frequency and the
 // sqrt-Cayley / PILE coefficients (update.cpp:301-320, thermostat.cpp:117-123).
