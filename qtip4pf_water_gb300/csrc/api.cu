@@ -255,6 +255,9 @@ struct qtg_ctx {
     size_t noise_len = 0;
     KVec *kvec = nullptr;
     int *kpk = nullptr;  // FP32 k-force packing code per k (see build_columns)
+    int4 *kfc = nullptr;     // per column: kx, ky, m, packed slot of kz = 0
+    float2 *kfb = nullptr;   // per column: FP32 reciprocal-lattice components of kx, ky
+    float4 *wpk = nullptr;   // packed +-kz force weights, 2 per k slot
     KCol *kcol = nullptr;
     KGroup *kgrp = nullptr;
     KBatch *kbatch = nullptr;
@@ -356,6 +359,9 @@ EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, d
     a.kgrp = c->kgrp;
     a.kbatch = c->kbatch;
     a.kpk = c->kpk;
+    a.kfc = c->kfc;
+    a.kfb = c->kfb;
+    a.wpk = c->wpk;
     a.max_grp = c->max_grp;
     a.kz = c->kz;
     a.max_batch = c->max_batch;
@@ -803,6 +809,8 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     const Consts &K = ctx->K;
     std::vector<KVec> kall;
     std::vector<int> kpk_all;
+    std::vector<int4> kfc_all;
+    std::vector<float2> kfb_all;
     std::vector<KCol> call;
     std::vector<KGroup> gall;
     std::vector<KBatch> ball;
@@ -883,6 +891,10 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         std::vector<int> kp;
         build_columns(kv, kord, cols, bats, kp, &S.n_col_half, &S.n_batch_half, &S.n_kvec_half);
         kpk_all.insert(kpk_all.end(), kp.begin(), kp.end());
+        for (const KCol &c : cols) {
+            kfc_all.push_back(make_int4(c.kx, c.ky, c.m, kp[c.k_begin + c.m] >> 8));
+            kfb_all.push_back(make_float2(S.kbf[0] * (float)c.kx, S.kbf[1] * (float)c.ky));
+        }
         S.n_kvec_ref = (int)kv.size();
         S.n_kvec = (int)kord.size();
         S.kvec_off = (int)kall.size();
@@ -1121,6 +1133,8 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->noise, ctx->noise_len);
     AL(ctx->kvec, kall.size());
     AL(ctx->kpk, kpk_all.size());
+    AL(ctx->kfc, kfc_all.size());
+    AL(ctx->kfb, kfb_all.size());
     AL(ctx->kcol, call.size());
     AL(ctx->kgrp, gall.size());
     AL(ctx->kbatch, ball.size());
@@ -1150,6 +1164,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->skp, (size_t)MAX_SC * ctx->total_k);
     AL(ctx->dskp, (size_t)MAX_SC * ctx->total_k);
     AL(ctx->wsk, ctx->total_k);
+    AL(ctx->wpk, 2 * ctx->total_k);
     AL(ctx->wdsk, ctx->total_k);
     AL(ctx->energy, ctx->total_slots);
     AL(ctx->energy_aux, ctx->total_slots);
@@ -1210,6 +1225,8 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     }
     cp(ctx->kvec, kall.data(), sizeof(KVec) * kall.size());
     cp(ctx->kpk, kpk_all.data(), sizeof(int) * kpk_all.size());
+    cp(ctx->kfc, kfc_all.data(), sizeof(int4) * kfc_all.size());
+    cp(ctx->kfb, kfb_all.data(), sizeof(float2) * kfb_all.size());
     cp(ctx->kcol, call.data(), sizeof(KCol) * call.size());
     cp(ctx->kgrp, gall.data(), sizeof(KGroup) * gall.size());
     cp(ctx->kbatch, ball.data(), sizeof(KBatch) * ball.size());
@@ -1259,7 +1276,7 @@ void qtg_destroy(qtg_ctx *ctx) {
                     ctx->phase, ctx->opos, ctx->part, ctx->skp, ctx->dskp, ctx->wsk, ctx->wdsk, ctx->energy, ctx->energy_aux,
                     ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
-                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf, ctx->fin_ticket, ctx->sites_fix, ctx->intra};
+                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf, ctx->fin_ticket, ctx->sites_fix, ctx->intra, ctx->kfc, ctx->kfb, ctx->wpk};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->box) cudaFreeHost(ctx->box);

@@ -891,12 +891,24 @@ __global__ void __launch_bounds__(128) k_sk_reduce(EvalArgs a) {
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
     // FP32 energy/force form: the half set, each kx = 0, ky > 0 vector standing for
-    // itself and its conjugate partner (|S|^2 and the force are the same for both)
+    // itself and its conjugate partner (|S|^2 and the force are the same for both),
+    // one block per force batch (whole columns, <= 128 vectors), so that the block
+    // also packs the batch's +-kz weights for k_kforce_f32
     const bool half = sizeof(R) == 4 && MODE == 0;
-    const int nk = half ? S.n_kvec_half : S.n_kvec;
-    if (blockIdx.x * 128 >= nk) return;
-    const int k = blockIdx.x * 128 + threadIdx.x;
+    int k, nk, kb0 = 0;
+    if (half) {
+        if ((int)blockIdx.x >= S.n_batch_half) return;
+        const KBatch B = a.kbatch[S.batch_off + blockIdx.x];
+        kb0 = B.k0;
+        k = B.k0 + threadIdx.x;
+        nk = B.k1;
+    } else {
+        nk = S.n_kvec;
+        if (blockIdx.x * 128 >= nk) return;
+        k = blockIdx.x * 128 + threadIdx.x;
+    }
     __shared__ double red[4];
+    __shared__ float2 wl[128];
     double e = 0.0;
     if (k < nk) {
         const KVec kv = a.kvec[S.kvec_off + k];
@@ -929,6 +941,7 @@ __global__ void __launch_bounds__(128) k_sk_reduce(EvalArgs a) {
             v.x = (R)(wf * fr);
             v.y = (R)(wf * fi);
             reinterpret_cast<V2<R> *>(a.wsk)[J.sk_off + k] = v;
+            wl[threadIdx.x] = make_float2(wf * fr, wf * fi);
         } else {
         for (int sc = 0; sc < a.n_sc; ++sc) {
             const size_t at = (size_t)sc * a.total_k + J.sk_off + k;
@@ -955,10 +968,39 @@ __global__ void __launch_bounds__(128) k_sk_reduce(EvalArgs a) {
         }
         }
     }
+    if (half && a.wpk && a.kpk) {
+        // the batch's packed weights: slot of |kz| = az of a column holds, with
+        // s = W(+az) + W(-az) and d = W(+az) - W(-az), P1 = (s.x, d.y, d.x, s.y) and
+        // P2 = az (d.x, s.y, s.x, d.y) (az = 0: P1 = (W, 0, 0))
+        __syncthreads();
+        const int code = k < nk ? a.kpk[S.kvec_off + k] : -1;
+        if (code >= 0) {
+            const int slot = code >> 8, az = code & 255;
+            const float2 wp = wl[threadIdx.x];
+            float4 *o = a.wpk + 2 * ((size_t)J.sk_off + kb0 + slot);
+            if (az == 0) {
+                o[0] = make_float4(wp.x, wp.y, 0.f, 0.f);
+            } else {
+                const float2 wm = wl[threadIdx.x - 2 * az];
+                const float sx = wp.x + wm.x, sy = wp.y + wm.y, dx = wp.x - wm.x, dy = wp.y - wm.y;
+                const float fa = (float)az;
+                o[0] = make_float4(sx, dy, dx, sy);
+                o[1] = make_float4(fa * dx, fa * sy, fa * sx, fa * dy);
+            }
+        }
+    }
     if (MODE == 0) {
         const double t = block_sum(e, red);
         if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
     }
+}
+
+// k_sk_reduce's grid: FP32 energy/force form one block per force batch, else per 128 k
+template <typename R, int MODE>
+void launch_sk_reduce(const EvalArgs &a, cudaStream_t s) {
+    const bool half = sizeof(R) == 4 && MODE == 0;
+    const dim3 g(half ? a.max_batch : (a.max_kvec + 127) / 128, a.n_jobs);
+    k_sk_reduce<R, MODE><<<g, 128, 0, s>>>(a);
 }
 
 // ---- k_kforce: reciprocal-space site forces -------------------------------------
@@ -1098,34 +1140,21 @@ __global__ void __launch_bounds__(FT) k_kforce_f32(EvalArgs a) {
         z[az - 1] = make_float2(0.f, 0.f);
         if (act && az < km1) z[az - 1] = ph[(size_t)(2 * km1 + az) * ns + i];
     }
-    const float bx = (float)(2.0 * PI_REF * S.inv_box[0]), by = (float)(2.0 * PI_REF * S.inv_box[1]),
-                bz = (float)(2.0 * PI_REF * S.inv_box[2]);
+    const float bz = S.kbf[2];
     float Fx = 0.f, Fy = 0.f, Fz = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f;
-    const float2 *wsk = reinterpret_cast<const float2 *>(a.wsk) + J.sk_off;
-    const int *kpk = a.kpk + S.kvec_off;
+    // the batch's columns (static) and +-kz weights (packed by k_sk_reduce), copied as they are
+    const float4 *wpk = a.wpk + 2 * (size_t)J.sk_off;
     for (int bt = bt0; bt < bt1; ++bt) {
         const KBatch B = a.kbatch[S.batch_off + bt];
         const int ncol = B.c1 - B.c0;
         __syncthreads();
         for (int idx = threadIdx.x; idx < ncol; idx += FT) {
-            const KCol C = a.kcol[S.col_off + B.c0 + idx];
-            cs[idx] = make_int4(C.kx, C.ky, C.m, kpk[C.k_begin + C.m] >> 8);
-            cb[idx] = make_float2(bx * (float)C.kx, by * (float)C.ky);
+            cs[idx] = a.kfc[S.col_off + B.c0 + idx];
+            cb[idx] = a.kfb[S.col_off + B.c0 + idx];
         }
         for (int idx = threadIdx.x; idx < B.k1 - B.k0; idx += FT) {
-            const int k = B.k0 + idx, code = kpk[k];
-            if (code < 0) continue;
-            const int slot = code >> 8, az = code & 255;
-            const float2 wp = wsk[k];
-            if (az == 0) {
-                P1[slot] = make_float4(wp.x, wp.y, 0.f, 0.f);
-            } else {
-                const float2 wm = wsk[k - 2 * az];
-                const float sx = wp.x + wm.x, sy = wp.y + wm.y, dx = wp.x - wm.x, dy = wp.y - wm.y;
-                const float fa = (float)az;
-                P1[slot] = make_float4(sx, dy, dx, sy);
-                P2[slot] = make_float4(fa * dx, fa * sy, fa * sx, fa * dy);
-            }
+            P1[idx] = wpk[2 * (B.k0 + idx)];
+            P2[idx] = wpk[2 * (B.k0 + idx) + 1];
         }
         __syncthreads();
         float fx = 0.f, fy = 0.f, fz = 0.f;
@@ -1915,7 +1944,7 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
         cudaStreamWaitEvent(forks->side[0], forks->fork, 0);
         cudaStreamWaitEvent(forks->side[1], forks->fork, 0);
         launch_ksk<R, 0>(a, dim3(ktiles, a.n_sc, a.n_jobs), forks->side[0]);
-        k_sk_reduce<R, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, forks->side[0]>>>(a);
+        launch_sk_reduce<R, 0>(a, forks->side[0]);
         launch_kforce_f32(a, dim3(tiles, a.n_kc, a.n_jobs), forks->side[0]);
         cudaEventRecord(forks->join[0], forks->side[0]);
         launch_lj_dense(a, forks->side[1]);
@@ -1939,13 +1968,13 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
         else if (sizeof(R) == 4) k_real_f32<<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         else k_real<R, 0><<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         launch_ksk<R, 0>(a, dim3(ktiles, a.n_sc, a.n_jobs), s);
-        k_sk_reduce<R, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
+        launch_sk_reduce<R, 0>(a, s);
         if (sizeof(R) == 4) launch_kforce_f32(a, dim3(tiles, a.n_kc, a.n_jobs), s);
         else k_kforce<R, 0><<<dim3(tiles, a.n_kc, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
     } else {
         k_real<R, 1><<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         launch_ksk<R, 1>(a, dim3(ktiles, a.n_sc, a.n_jobs), s);
-        k_sk_reduce<R, 1><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
+        launch_sk_reduce<R, 1>(a, s);
         k_kforce<R, 1><<<dim3(tiles, a.n_kc, a.n_jobs), FT, kforce_smem<R>(a.max_kmax), s>>>(a);
     }
     const dim3 gm((a.max_mols + 127) / 128, a.n_jobs);
@@ -1996,8 +2025,8 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
         if (mixed) launch_ksk<float, 0>(a, gk, s);
         else launch_ksk<double, 0>(a, gk, s);
     } else if (n == "sk_reduce") {
-        if (mixed) k_sk_reduce<float, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
-        else k_sk_reduce<double, 0><<<dim3((a.max_kvec + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
+        if (mixed) launch_sk_reduce<float, 0>(a, s);
+        else launch_sk_reduce<double, 0>(a, s);
     } else if (n == "kforce") {
         if (mixed) launch_kforce_f32(a, gf, s);
         else k_kforce<double, 0><<<gf, FT, kforce_smem<double>(a.max_kmax), s>>>(a);
@@ -2054,16 +2083,15 @@ void launch_kwald_only(const EvalArgs &a0, bool mixed, cudaStream_t s, unsigned 
     a.n_sc = chunks_or(a.tune_sc, (long long)ktiles * a.n_jobs, MAX_SC);
     a.n_kc = chunks_or(a.tune_kc, (long long)tiles * a.n_jobs, MAX_KC);
     const dim3 gs((ns + 127) / 128, a.n_jobs), gk(ktiles, a.n_sc, a.n_jobs), gf(tiles, a.n_kc, a.n_jobs);
-    const dim3 gr((a.max_kvec + 127) / 128, a.n_jobs);
     if (mixed) {
         launch_prep_f32(a, s);
         launch_ksk<float, 0>(a, gk, s);
-        k_sk_reduce<float, 0><<<gr, 128, 0, s>>>(a);
+        launch_sk_reduce<float, 0>(a, s);
         launch_kforce_f32(a, gf, s);
     } else {
         k_prep<double><<<gs, 128, 0, s>>>(a);
         launch_ksk<double, 0>(a, gk, s);
-        k_sk_reduce<double, 0><<<gr, 128, 0, s>>>(a);
+        launch_sk_reduce<double, 0>(a, s);
         k_kforce<double, 0><<<gf, FT, kforce_smem<double>(a.max_kmax), s>>>(a);
     }
     if (mixed) k_sum_parts<float><<<dim3((3 * ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);

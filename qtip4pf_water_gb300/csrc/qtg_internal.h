@@ -436,6 +436,9 @@ struct EvalArgs {
     const KGroup *kgrp;
     const KBatch *kbatch;
     const int *kpk;        // per k (as kvec): kz >= 0: (packed slot in its force batch) << 8 | kz; kz < 0: -1
+    const int4 *kfc;       // per column (as kcol): kx, ky, m, packed slot of its kz = 0 (FP32 k-force)
+    const float2 *kfb;     // per column: (2 pi / L_x) kx, (2 pi / L_y) ky in FP32
+    float4 *wpk;           // per k slot: the packed +-kz weights P1, P2 of k_kforce_f32 (k_sk_reduce)
     int max_grp, max_batch;
     void *sites;           // 4 reals per site (x, y, z, q), per slot
     int4 *sites_fix;       // mixed: per site the box fractions of x, y, z as 32-bit fixed point
