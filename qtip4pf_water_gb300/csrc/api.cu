@@ -852,6 +852,10 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         S.inv_sqrt_beta_n = 1.0 / sqrt(S.beta_n);
         const double omega_p = 1.0 / S.beta_n;
         S.omega_psq = omega_p * omega_p;
+        S.inv_p = 1.0 / P;
+        S.sqrt_inv_p = sqrt(1.0 / P);
+        S.half_omega_psq = 0.5 * S.omega_psq;
+        S.half_nd_beta = 0.5 * S.n_dof / S.beta;
         S.dt = d.dt_fs * K.fs2au;
         S.halfdt = 0.5 * S.dt;
         S.eps_sc = d.eps_sc;

@@ -297,6 +297,7 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
     __shared__ double qbar[256];
     const bool cf = a.kick && S.centroid_fixed && a.cf_acc;
     __shared__ double red4[4][256];
+    __shared__ double2 cpart[256];  // [b][c], b < min(8, P): bead-sum partials of (q, p + dt/2 f)
     const long long at = S.q_off + (long long)b * S.n_dof + col;
     double qb = 0.0, pb = 0.0, fb = 0.0, fpb = 0.0;
     const double m = act ? a.mass[S.mass_off + col] : 1.0;
@@ -322,17 +323,27 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
         a.cf_acc[S.mass_off + col] += sf / (double)P;
         if (col == 0) a.run[W.sys].cf_samples += 1.0;
     }
-    // bead 0 of each column: the centroid (path_integrals.cpp:10-26) and the
-    // centroid normal-mode kinetic energy after the next opening kick
+    // the centroid (path_integrals.cpp:10-26) and the centroid normal-mode kinetic
+    // energy after the next opening kick: rows b < 8 sum beads b, b + 8, ... of each
+    // column, then row 0 adds the eight partials
     double k0 = 0.0;
-    if (b == 0 && c < W.ncols) {
+    if (b < 8 && c < W.ncols) {
         double sq = 0.0, sp = 0.0;
-        for (int j = 0; j < P; ++j) {
+        for (int j = b; j < P; j += 8) {
             sq += Xq[j * C + c];
             sp += Xp[j * C + c];
         }
-        qbar[c] = sq / (double)P;
-        const double p0 = sqrt(1.0 / P) * sp;
+        cpart[b * C + c] = make_double2(sq, sp);
+    }
+    __syncthreads();
+    if (b == 0 && c < W.ncols) {
+        double sq = 0.0, sp = 0.0;
+        for (int j = 0; j < 8 && j < P; ++j) {
+            sq += cpart[j * C + c].x;
+            sp += cpart[j * C + c].y;
+        }
+        qbar[c] = sq * S.inv_p;
+        const double p0 = S.sqrt_inv_p * sp;
         k0 = 0.5 * p0 * p0 * im;
     }
     __syncthreads();
@@ -341,7 +352,7 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
         kin = 0.5 * pb * pb * im;
         const double qn = Xq[((b + 1) % P) * C + c];
         const double dq = qb - qn;
-        spring = 0.5 * m * S.omega_psq * dq * dq;
+        spring = m * S.half_omega_psq * dq * dq;
         const int all = a.kcv_all_beads < 0 ? (S.propagator == 1) : a.kcv_all_beads;
         if (all || (b % 2 == 0)) tq = -(qb - qbar[c]) * fpb;
     }
@@ -539,23 +550,27 @@ __device__ void finalize_system(const FinalizeArgs &a, int s, unsigned long long
     SysAcc *ac = &a.acc[s];
     SysRun *run = &a.run[s];
     const int P = S.n_beads;
-    if (a.record && lane == 0) {
-        double vsum = 0.0, veven = 0.0;
-        for (int b = 0; b < P; ++b) {
+    double vsum = 0.0, veven = 0.0;
+    if (a.record) {  // the beads' energies summed across the warp
+        for (int b = lane; b < P; b += 32) {
             const double e = a.energy[S.job_base + b];
             vsum += e;
             if (b % 2 == 0) veven += e;
         }
+        vsum = warp_sum(vsum);
+        veven = warp_sum(veven);
+    }
+    if (a.record && lane == 0) {
         double vtot, pot, kcv;
-        const double half_nd_beta = 0.5 * S.n_dof / S.beta;
+        const double half_nd_beta = S.half_nd_beta;
         if (S.propagator == 0) {  // Suzuki-Chin (forces.cpp:724-781, path_integrals.cpp:29-48)
             vtot = (2.0 * veven + 4.0 * (vsum - veven) + ac->sc_extra) / 3.0;
-            pot = 2.0 * veven / P;
-            kcv = half_nd_beta + ac->kcv_tq / P;
+            pot = 2.0 * veven * S.inv_p;
+            kcv = half_nd_beta + ac->kcv_tq * S.inv_p;
         } else {
             vtot = vsum;
-            pot = vsum / P;
-            kcv = half_nd_beta + ac->kcv_tq / (2.0 * P);
+            pot = vsum * S.inv_p;
+            kcv = half_nd_beta + ac->kcv_tq * (0.5 * S.inv_p);
         }
         const double cons = vtot + ac->kin + ac->spring + run->heat;
         double *o = a.est + ((size_t)(rec % (unsigned long long)a.max_records) * a.n_sys + s) * 8;

@@ -48,6 +48,7 @@ struct SysDev {
     double kappa, rc_sq, ewald_pref, k_pref, self_energy;
     double r_cut_sq, r_skin_sq, skin_margin;
     double beta, beta_n, omega_psq, dt, halfdt, eps_sc, c1_centroid, inv_sqrt_beta_n;
+    double inv_p, sqrt_inv_p, half_omega_psq, half_nd_beta;  // 1/P, sqrt(1/P), omega_P^2 / 2, n_dof / (2 beta)
     float boxf[3], inv_boxf[3];
     float kappaf, rc_sqf, ewald_preff, kappa_sqf;
     float kbf[3];   // 2 pi / L_d, the reciprocal-lattice steps
