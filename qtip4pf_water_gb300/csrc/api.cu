@@ -888,6 +888,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         S.r_skin_sq = K.r_skin_sq;
         S.skin_margin = K.r_skin - K.r_cut;
         S.c1_centroid = d.thermostat == QTG_THERMO_PILE_L ? exp(-S.dt / (d.tau0_fs * K.fs2au)) : 0.0;
+        S.c2n_centroid = sqrt(1.0 - S.c1_centroid * S.c1_centroid) * S.inv_sqrt_beta_n;
         std::vector<KVec> kv, kord;
         std::vector<KCol> cols;
         std::vector<KBatch> bats;
@@ -945,6 +946,9 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
             const double gk = gpref * sin(k * PI_REF / P);
             mc.c1 = exp(-S.dt * gk);
             mc.c2 = sqrt(1.0 - mc.c1 * mc.c1);
+            mc.cq = mc.scale * S.halfdt;
+            mc.cp = mc.scale * S.halfdt * mc.w2;
+            mc.c2n = mc.c2 * S.inv_sqrt_beta_n;
             mode_all.push_back(mc);
         }
         for (int m = 0; m < N; ++m) {

@@ -215,35 +215,37 @@ __global__ void __launch_bounds__(128) k_prep_f32(EvalArgs a) {
     if (s >= ns) return;
     const int mol = s / 3, kind = s - 3 * mol;
     const double *q = a.pos + J.pos_off;
-    const double g = a.c.gamma_vs;
+    const double g = a.c.gamma_vs, h = 0.5 * (1.0 - g);
     double x, u = 0.0;
+    // box fractions in 32-bit fixed point: the low 32 bits of round(x 2^32 / L), an
+    // FP64 product (exact scaling by 2^32 of x / L rounded once) and one conversion;
+    // the wrapped FP32 coordinates follow from the fixed-point value
     if (a.sites_are_input || kind != 0) {
         x = q[3 * s + d];
         if (J.mode == 1) u = a.dir[J.pos_off + 3 * s + d];
     } else {
         // M site (forces.cpp:558-564)
-        x = g * q[9 * mol + d] + 0.5 * (1.0 - g) * (q[9 * mol + 3 + d] + q[9 * mol + 6 + d]);
+        x = fma(g, q[9 * mol + d], h * (q[9 * mol + 3 + d] + q[9 * mol + 6 + d]));
         if (J.mode == 1) {
             const double *v = a.dir + J.pos_off;
-            u = g * v[9 * mol + d] + 0.5 * (1.0 - g) * (v[9 * mol + 3 + d] + v[9 * mol + 6 + d]);
+            u = fma(g, v[9 * mol + d], h * (v[9 * mol + 3 + d] + v[9 * mol + 6 + d]));
         }
-        // wrapped oxygen position for the Lennard-Jones kernel
-        const double t = q[9 * mol + d] * S.inv_box[d];
+        // wrapped oxygen position for the Lennard-Jones kernel and the skin test
+        const unsigned FO = (unsigned)__double2ll_rn(q[9 * mol + d] * S.fix_scale[d]);
         float *o = reinterpret_cast<float *>(a.opos) + 4 * ((size_t)J.site_off / 3 + mol);
-        o[d] = (float)((t - floor(t)) * S.box[d]);
+        o[d] = (float)FO * S.fixf[d];
         if (d == 0) o[3] = 0.f;
     }
-    const double chg = a.charge[S.chg_off + s];
-    const double t = x * S.inv_box[d];
-    const double frac = t - floor(t);
-    const unsigned F = __double2uint_rz(frac * 4294967296.0);
+    const unsigned F = (unsigned)__double2ll_rn(x * S.fix_scale[d]);
     float *sv = reinterpret_cast<float *>(a.sites) + 4 * ((size_t)J.site_off + s);
-    sv[d] = (float)(frac * S.box[d]);
+    sv[d] = (float)F * S.fixf[d];
     int *fx = reinterpret_cast<int *>(a.sites_fix + J.site_off + s);
     fx[d] = (int)F;
+    float cf = 1.f;
     if (d == 0) {
-        sv[3] = (float)chg;
-        fx[3] = __float_as_int((float)chg);
+        cf = (float)a.charge[S.chg_off + s];
+        sv[3] = cf;
+        fx[3] = __float_as_int(cf);
     }
     if (J.mode == 1) {
         float *tv = reinterpret_cast<float *>(a.tan_sites) + 4 * ((size_t)J.site_off + s);
@@ -256,7 +258,7 @@ __global__ void __launch_bounds__(128) k_prep_f32(EvalArgs a) {
     float2 *ph = reinterpret_cast<float2 *>(a.phase) + J.phase_off;
     float s1, c1;
     sincospif((float)(int)F * 4.656612873077393e-10f, &s1, &c1);
-    const float qd = (d == 0) ? (float)chg : 1.f;
+    const float qd = cf;  // the charge in row 0 (x), 1 in the y and z rows
     float cr = 1.f, ci = 0.f;
     for (int m = 0; m < km1; ++m) {
         if (m > 0 && (m & 3) == 0) sincospif((float)(int)((unsigned)m * F) * 4.656612873077393e-10f, &ci, &cr);

@@ -179,23 +179,23 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
             yq += dq;
         }
         const ModeCoef mc = a.modes[S.mode_off + k];
+        // half sqrt-Cayley step (update.cpp:301-320): q' = scale (q + dt/2 p / m),
+        // p' = scale (p - dt/2 omega_k^2 m q), with the mode's products precomputed
+        const double cqi = mc.cq * im, cpm = mc.cp * m;
         if (flags & RF_CAYLEY) {
-            // update.cpp:301-320
-            double t = S.halfdt * yp * im + yq;
-            t *= mc.scale;
-            yp = yp - S.halfdt * mc.w2 * yq * m;
-            yp *= mc.scale;
-            yq = t;
+            const double nq = fma(cqi, yp, mc.scale * yq);
+            yp = fma(-cpm, yq, mc.scale * yp);
+            yq = nq;
         }
         if ((flags & RF_THERMO) && (S.thermostat != 0 || a.pile_g) && !fixed0) {
-            const double before = 0.5 * yp * yp * im;
+            const double before = yp;
             if (k == 0 && (S.thermostat == 1 || a.pile_g)) {
                 yp *= a.run[W.sys].alpha;  // PILE-G centroid (thermostat.cpp:88-104)
             } else {
-                double c1 = mc.c1, c2 = mc.c2;
+                double c1 = mc.c1, c2n = mc.c2n;
                 if (k == 0) {  // PILE-L centroid
                     c1 = S.c1_centroid;
-                    c2 = sqrt(1.0 - c1 * c1);
+                    c2n = S.c2n_centroid;
                 }
                 double xi;
                 if (a.noise && k > 0) {
@@ -208,16 +208,15 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
                                                   (uint32_t)(st >> 32), k0, k1));
                 }
                 // thermostat.cpp:131-136: sqrt(m / beta_P) c2 xi
-                yp = c1 * yp + a.sqrt_mass[S.mass_off + col] * S.inv_sqrt_beta_n * c2 * xi;
+                yp = fma(c1, yp, a.sqrt_mass[S.mass_off + col] * c2n * xi);
             }
-            heat = 0.5 * yp * yp * im - before;
+            // kinetic energy change p'^2 / 2m - p^2 / 2m
+            heat = 0.5 * im * (yp - before) * (yp + before);
         }
         if (flags & RF_CAYLEY) {
-            double t = S.halfdt * yp * im + yq;
-            t *= mc.scale;
-            yp = yp - S.halfdt * mc.w2 * yq * m;
-            yp *= mc.scale;
-            yq = t;
+            const double nq = fma(cqi, yp, mc.scale * yq);
+            yp = fma(-cpm, yq, mc.scale * yp);
+            yq = nq;
         }
     }
     double qn = yq, pn = yp;

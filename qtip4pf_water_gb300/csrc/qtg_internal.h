@@ -49,6 +49,7 @@ struct SysDev {
     double r_cut_sq, r_skin_sq, skin_margin;
     double beta, beta_n, omega_psq, dt, halfdt, eps_sc, c1_centroid, inv_sqrt_beta_n;
     double inv_p, sqrt_inv_p, half_omega_psq, half_nd_beta;  // 1/P, sqrt(1/P), omega_P^2 / 2, n_dof / (2 beta)
+    double c2n_centroid;  // PILE-L centroid: sqrt(1 - c1_centroid^2) / sqrt(beta_P)
     float boxf[3], inv_boxf[3];
     float kappaf, rc_sqf, ewald_preff, kappa_sqf;
     float kbf[3];   // 2 pi / L_d, the reciprocal-lattice steps
@@ -58,6 +59,7 @@ struct SysDev {
     // (u = L / 2^32): r_c^2 / u^2, cex u^2, ka u, the Ewald prefactor times u, 1 / u^2
     // and 1 / u, so the pair loop needs no scaling of its integer differences.
     float fixf[3], kaf, cexf;
+    double fix_scale[3];  // 2^32 / L_d: a coordinate times this, rounded, is its box fraction in fixed point
     int fix_cubic;
     float rc2u, cexu, kau, prefu, s2u, invu;
     unsigned long long seed;
@@ -69,6 +71,7 @@ inline void set_float_consts(SysDev &S) {
     for (int d = 0; d < 3; ++d) {
         S.kbf[d] = (float)(2.0 * pi * S.inv_box[d]);
         S.fixf[d] = (float)(S.box[d] * two32);
+        S.fix_scale[d] = S.inv_box[d] * 4294967296.0;
     }
     S.kaf = (float)(0.3275911 * S.kappa);
     S.cexf = (float)(-S.kappa * S.kappa * 1.4426950408889634);
@@ -89,6 +92,9 @@ struct ModeCoef {
     double scale;  // 1 / sqrt(1 + omega_k^2 dt^2 / 4)
     double c1;     // exp(-dt gamma_k), gamma_k = (4 / beta_P hbar) sin(k pi / P)
     double c2;     // sqrt(1 - c1^2)
+    double cq;     // scale dt / 2: a half Cayley step is q' = scale q + cq p / m
+    double cp;     //   and p' = scale p - cp m q, with cp = scale omega_k^2 dt / 2
+    double c2n;    // c2 / sqrt(beta_P), the PILE noise amplitude per sqrt(m)
 };
 
 // One reciprocal-lattice vector k = 2 pi (kx/Lx, ky/Ly, kz/Lz) of the set
