@@ -1118,32 +1118,38 @@ __global__ void __launch_bounds__(FT) k_kforce(EvalArgs a) {
 // sum v = pi (U1 + W0x) + pr (U2 - W0y), sum kz v = pi U3 + pr U4 (W0: kz = 0).
 // The batch's weights are staged as (sx, dy, dx, sy) and kz (dx, sy, sx, dy);
 // a site's Z(1 .. ZM) stays in registers, its X and Y rows in shared memory.
-template <int ZM>
+template <int ZM, int SPT>  // SPT: sites per thread (the block's weights serve SPT x FT sites)
 __global__ void __launch_bounds__(FT) k_kforce_f32(EvalArgs a) {
+    constexpr int NS = SPT * FT;  // sites per block
     const int kc = blockIdx.y, jb = blockIdx.z;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
     // the half set, whose weights k_sk_reduce<float, 0> writes
     const int nb = S.n_batch_half, ns = S.n_sites, km1 = S.k_max + 1;
-    if (blockIdx.x * FT >= ns) return;
-    const int i = blockIdx.x * FT + threadIdx.x;
-    const bool act = i < ns;
-    const int ii = act ? i : 0;
+    if (blockIdx.x * NS >= ns) return;
     const int bt0 = chunk_lo(nb, kc, a.n_kc), bt1 = chunk_lo(nb, kc + 1, a.n_kc);
     __shared__ float4 P1[KB], P2[KB];
     __shared__ int4 cs[KB];      // kx, ky, m, packed slot of kz = 0
     __shared__ float2 cb[KB];    // b_x kx, b_y ky
-    extern __shared__ float2 xyrow[];  // [2 km1][FT]: this block's sites' X(0 .. k_max), Y(0 .. k_max)
+    extern __shared__ float2 xyrow[];  // [2 km1][NS]: this block's sites' X(0 .. k_max), Y(0 .. k_max)
     const float2 *ph = reinterpret_cast<const float2 *>(a.phase) + J.phase_off;
-    for (int r = 0; r < 2 * km1; ++r) xyrow[r * FT + threadIdx.x] = ph[(size_t)r * ns + ii];
-    float2 z[ZM];
+    int site[SPT];
+    float2 z[SPT][ZM];
 #pragma unroll
-    for (int az = 1; az <= ZM; ++az) {
-        z[az - 1] = make_float2(0.f, 0.f);
-        if (act && az < km1) z[az - 1] = ph[(size_t)(2 * km1 + az) * ns + i];
+    for (int u = 0; u < SPT; ++u) {
+        site[u] = blockIdx.x * NS + u * FT + threadIdx.x;
+        const int ii = site[u] < ns ? site[u] : 0;
+        for (int r = 0; r < 2 * km1; ++r) xyrow[r * NS + u * FT + threadIdx.x] = ph[(size_t)r * ns + ii];
+#pragma unroll
+        for (int az = 1; az <= ZM; ++az) {
+            z[u][az - 1] = make_float2(0.f, 0.f);
+            if (site[u] < ns && az < km1) z[u][az - 1] = ph[(size_t)(2 * km1 + az) * ns + site[u]];
+        }
     }
     const float bz = S.kbf[2];
-    float Fx = 0.f, Fy = 0.f, Fz = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f;
+    float Fx[SPT], Fy[SPT], Fz[SPT], Cx[SPT], Cy[SPT], Cz[SPT];
+#pragma unroll
+    for (int u = 0; u < SPT; ++u) Fx[u] = Fy[u] = Fz[u] = Cx[u] = Cy[u] = Cz[u] = 0.f;
     // the batch's columns (static) and +-kz weights (packed by k_sk_reduce), copied as they are
     const float4 *wpk = a.wpk + 2 * (size_t)J.sk_off;
     for (int bt = bt0; bt < bt1; ++bt) {
@@ -1159,36 +1165,59 @@ __global__ void __launch_bounds__(FT) k_kforce_f32(EvalArgs a) {
             P2[idx] = wpk[2 * (B.k0 + idx) + 1];
         }
         __syncthreads();
-        float fx = 0.f, fy = 0.f, fz = 0.f;
+        float fx[SPT], fy[SPT], fz[SPT];
+#pragma unroll
+        for (int u = 0; u < SPT; ++u) fx[u] = fy[u] = fz[u] = 0.f;
         for (int cc = 0; cc < ncol; ++cc) {
             const int4 C = cs[cc];
-            const float2 x = xyrow[C.x * FT + threadIdx.x];
-            const float2 y = xyrow[(km1 + abs(C.y)) * FT + threadIdx.x];
-            const float yi = C.y < 0 ? -y.y : y.y;
-            const float pr = x.x * y.x - x.y * yi, pi = x.x * yi + x.y * y.x;
             const float4 w0 = P1[C.w];
-            float u1 = w0.x, u2 = -w0.y, u3 = 0.f, u4 = 0.f;
+            float pr[SPT], pi[SPT], u1[SPT], u2[SPT], u3[SPT], u4[SPT];
+#pragma unroll
+            for (int u = 0; u < SPT; ++u) {
+                const float2 x = xyrow[C.x * NS + u * FT + threadIdx.x];
+                const float2 y = xyrow[(km1 + abs(C.y)) * NS + u * FT + threadIdx.x];
+                const float yi = C.y < 0 ? -y.y : y.y;
+                pr[u] = x.x * y.x - x.y * yi;
+                pi[u] = x.x * yi + x.y * y.x;
+                u1[u] = w0.x;
+                u2[u] = -w0.y;
+                u3[u] = 0.f;
+                u4[u] = 0.f;
+            }
 #pragma unroll
             for (int az = 1; az <= ZM; ++az) {
                 if (az > C.z) break;
                 const float4 p1 = P1[C.w + az], p2 = P2[C.w + az];
-                const float zx = z[az - 1].x, zy = z[az - 1].y;
-                u1 = fmaf(zx, p1.x, fmaf(zy, p1.y, u1));
-                u2 = fmaf(zy, p1.z, fmaf(-zx, p1.w, u2));
-                u3 = fmaf(zx, p2.x, fmaf(zy, p2.y, u3));
-                u4 = fmaf(zy, p2.z, fmaf(-zx, p2.w, u4));
+#pragma unroll
+                for (int u = 0; u < SPT; ++u) {
+                    const float zx = z[u][az - 1].x, zy = z[u][az - 1].y;
+                    u1[u] = fmaf(zx, p1.x, fmaf(zy, p1.y, u1[u]));
+                    u2[u] = fmaf(zy, p1.z, fmaf(-zx, p1.w, u2[u]));
+                    u3[u] = fmaf(zx, p2.x, fmaf(zy, p2.y, u3[u]));
+                    u4[u] = fmaf(zy, p2.z, fmaf(-zx, p2.w, u4[u]));
+                }
             }
-            const float v = fmaf(pi, u1, pr * u2), vz = fmaf(pi, u3, pr * u4);
             const float2 b = cb[cc];
-            fx = fmaf(b.x, v, fx);
-            fy = fmaf(b.y, v, fy);
-            fz = fmaf(bz, vz, fz);
+#pragma unroll
+            for (int u = 0; u < SPT; ++u) {
+                const float v = fmaf(pi[u], u1[u], pr[u] * u2[u]), vz = fmaf(pi[u], u3[u], pr[u] * u4[u]);
+                fx[u] = fmaf(b.x, v, fx[u]);
+                fy[u] = fmaf(b.y, v, fy[u]);
+                fz[u] = fmaf(bz, vz, fz[u]);
+            }
         }
-        kahan_add(Fx, Cx, fx);
-        kahan_add(Fy, Cy, fy);
-        kahan_add(Fz, Cz, fz);
+#pragma unroll
+        for (int u = 0; u < SPT; ++u) {
+            kahan_add(Fx[u], Cx[u], fx[u]);
+            kahan_add(Fy[u], Cy[u], fy[u]);
+            kahan_add(Fz[u], Cz[u], fz[u]);
+        }
     }
-    if (act) store_plane<float>(a.part, 3 * ((size_t)(a.n_rj + kc) * a.total_sites + J.site_off + i), Fx - Cx, Fy - Cy, Fz - Cz);
+#pragma unroll
+    for (int u = 0; u < SPT; ++u)
+        if (site[u] < ns)
+            store_plane<float>(a.part, 3 * ((size_t)(a.n_rj + kc) * a.total_sites + J.site_off + site[u]),
+                               Fx[u] - Cx[u], Fy[u] - Cy[u], Fz[u] - Cz[u]);
 }
 
 template <typename R>
@@ -1205,12 +1234,15 @@ void launch_ksk(const EvalArgs &a, dim3 grid, cudaStream_t s) {
 
 // the FP32 k-force kernel for the largest |kz| of the batch (the general form beyond 32)
 void launch_kforce_f32(const EvalArgs &a, dim3 grid, cudaStream_t s) {
-    const size_t sm = (size_t)2 * (a.max_kmax + 1) * FT * sizeof(float2);
-    if (a.kpk && a.max_kmax <= 8) k_kforce_f32<8><<<grid, FT, sm, s>>>(a);
-    else if (a.kpk && a.max_kmax <= 12) k_kforce_f32<12><<<grid, FT, sm, s>>>(a);
-    else if (a.kpk && a.max_kmax <= 16) k_kforce_f32<16><<<grid, FT, sm, s>>>(a);
-    else if (a.kpk && a.max_kmax <= 24) k_kforce_f32<24><<<grid, FT, sm, s>>>(a);
-    else if (a.kpk && a.max_kmax <= 32) k_kforce_f32<32><<<grid, FT, sm, s>>>(a);
+    // two sites a thread (the block covers 2 FT sites: grid.x halves)
+    const size_t sm = (size_t)2 * (a.max_kmax + 1) * 2 * FT * sizeof(float2);
+    dim3 g2 = grid;
+    g2.x = (grid.x + 1) / 2;
+    if (a.kpk && a.max_kmax <= 8) k_kforce_f32<8, 2><<<g2, FT, sm, s>>>(a);
+    else if (a.kpk && a.max_kmax <= 12) k_kforce_f32<12, 2><<<g2, FT, sm, s>>>(a);
+    else if (a.kpk && a.max_kmax <= 16) k_kforce_f32<16, 2><<<g2, FT, sm, s>>>(a);
+    else if (a.kpk && a.max_kmax <= 24) k_kforce_f32<24, 2><<<g2, FT, sm, s>>>(a);
+    else if (a.kpk && a.max_kmax <= 32) k_kforce_f32<32, 2><<<g2, FT, sm, s>>>(a);
     else k_kforce<float, 0><<<grid, FT, kforce_smem<float>(a.max_kmax), s>>>(a);
 }
 
@@ -1884,11 +1916,11 @@ size_t kforce_smem(int kmax) {
 template <typename R>
 void set_attrs() {
     const int big = 200 * 1024;
-    cudaFuncSetAttribute(k_kforce_f32<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_kforce_f32<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_kforce_f32<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_kforce_f32<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_kforce_f32<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_kforce_f32<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_kforce_f32<12, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_kforce_f32<16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_kforce_f32<24, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(k_kforce_f32<32, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_ksk<R, 0, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_ksk<R, 1, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_ksk<R, 0, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
