@@ -2158,36 +2158,37 @@ qtg_status qtg_autotune(qtg_ctx *ctx, int iters, double *ms_heuristic, double *m
         a.lj_full = 1;
         return time_on_stream(ctx, iters, [&] { launch_eval(ctx, a); }, ms);
     };
-    // each count governs one kernel: k_real (n_rj), k_ksk (n_sc), k_kforce (n_kc)
-    static const int cand_rk[] = {1, 2, 3, 4, 6, 8, 12, 16};          // k_real, k_kforce
-    static const int cand_sc[] = {1, 2, 4, 6, 8, 12, 16, 24, 32};     // k_ksk
-    static const char *kname[3] = {"real", "ksk", "kforce"};
+    // each count governs one kernel: k_real (n_rj), k_ksk (n_sc), k_kforce (n_kc), 0
+    // the launcher's heuristic. The force kernels run concurrently (forked branches
+    // of one evaluation), so candidates are judged by the time of the whole force
+    // evaluation: coordinate descent from the heuristic, one count at a time.
+    static const int cand_rk[] = {0, 1, 2, 3, 4, 6, 8, 12, 16};       // k_real, k_kforce
+    static const int cand_sc[] = {0, 1, 2, 4, 6, 8, 12, 16, 24, 32};  // k_ksk
     int best[3] = {0, 0, 0};
-    {
-        const int zero[3] = {0, 0, 0};
-        double ms;
-        CKS(eval_ms(zero, &ms));  // fills the scratch arrays the single kernels read
-    }
-    for (int k = 0; k < 3; ++k) {
-        double best_ms = 1e30;
-        const int *cand = k == 1 ? cand_sc : cand_rk;
-        const int n_cand = k == 1 ? (int)(sizeof(cand_sc) / sizeof(int)) : (int)(sizeof(cand_rk) / sizeof(int));
-        for (int ci = 0; ci < n_cand; ++ci) {
-            const int c = cand[ci];
-            int t[3] = {0, 0, 0};
-            t[k] = c;
-            for (int q = 0; q < 3; ++q) ctx->tune[q] = t[q];
-            EvalArgs a = eval_args(ctx, ctx->base.d, nj, ctx->q, ctx->fphys, 0, 0);
-            a.lj_full = 1;
-            double ms;
-            CKS(time_on_stream(ctx, iters, [&] { launch_ewald_kernel(a, ctx->mixed, kname[k], ctx->stream); }, &ms));
-            if (ms < best_ms) {
-                best_ms = ms;
-                best[k] = c;
+    double best_ms = 0.0;
+    CKS(eval_ms(best, &best_ms));  // fills the scratch arrays, warms the kernels
+    CKS(eval_ms(best, &best_ms));
+    for (int round = 0; round < 2; ++round) {
+        bool moved = false;
+        for (int k = 0; k < 3; ++k) {
+            const int *cand = k == 1 ? cand_sc : cand_rk;
+            const int n_cand = k == 1 ? (int)(sizeof(cand_sc) / sizeof(int)) : (int)(sizeof(cand_rk) / sizeof(int));
+            for (int ci = 0; ci < n_cand; ++ci) {
+                if (cand[ci] == best[k]) continue;
+                int t[3] = {best[0], best[1], best[2]};
+                t[k] = cand[ci];
+                double ms;
+                CKS(eval_ms(t, &ms));
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best[k] = cand[ci];
+                    moved = true;
+                }
             }
         }
+        if (!moved) break;
     }
-    // the whole force evaluation decides between the tuned counts and the heuristic
+    // a fresh measurement of both decides between the descent's counts and the heuristic
     const int zero[3] = {0, 0, 0};
     double t0 = 0.0, t1 = 0.0;
     CKS(eval_ms(zero, &t0));
