@@ -124,6 +124,60 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
     }
     const double q_old = qb;
     double yq = qb, yp = pb;
+    // P divisible by 4 (P >= 8): the rows are also symmetric about b = P/4 -- cos rows k
+    // have C[k][P/2 - b] = (-1)^k C[k][b], sin rows of frequency j = P - k have
+    // C[k][P/2 - b] = (-1)^(j+1) C[k][b] -- so a second fold halves the FMAs again
+    const bool fold2 = (P % 4) == 0 && P >= 8;
+    const int q4 = P / 4;
+    if ((flags & RF_FWD) && fold2) {
+        if (k < P) {
+            Xq[k * C + c] = qb;
+            Xp[k * C + c] = pb;
+        }
+        __syncthreads();
+        // folded inputs, index j (x C + c): ss_b, sd_b, ds_b, dd_b (b = 1 .. q4 - 1) at
+        // j = b - 1 + {0, 1, 2, 3} (q4 - 1), then s_q4, d_q4, x_0 + x_P/2, x_0 - x_P/2
+        if (k < q4 && c < W.ncols) {
+            for (int u = 0; u < 2; ++u) {
+                const double *X = u ? Xp : Xq;
+                double *Z = u ? Zp : Zq;
+                if (k == 0) {
+                    const double a0 = X[c], ah = X[half * C + c], a4 = X[q4 * C + c], a3 = X[(P - q4) * C + c];
+                    Z[(4 * q4 - 4) * C + c] = a4 + a3;
+                    Z[(4 * q4 - 3) * C + c] = a4 - a3;
+                    Z[(4 * q4 - 2) * C + c] = a0 + ah;
+                    Z[(4 * q4 - 1) * C + c] = a0 - ah;
+                } else {
+                    const double x1 = X[k * C + c], x2 = X[(P - k) * C + c];
+                    const double x3 = X[(half - k) * C + c], x4 = X[(half + k) * C + c];
+                    const double s1 = x1 + x2, s2 = x3 + x4, d1 = x1 - x2, d2 = x3 - x4;
+                    Z[(k - 1) * C + c] = s1 + s2;
+                    Z[(q4 - 1 + k - 1) * C + c] = s1 - s2;
+                    Z[(2 * q4 - 2 + k - 1) * C + c] = d1 + d2;
+                    Z[(3 * q4 - 3 + k - 1) * C + c] = d1 - d2;
+                }
+            }
+        }
+        __syncthreads();
+        if (act) {
+            const double *row = Cm + k * P;
+            const bool sym = k <= half;
+            const int par = sym ? (k & 1) : ((P - k) & 1);
+            // cos rows: ss (k even) or sd (k odd); sin rows: ds (j odd) or dd (j even)
+            const int base = sym ? (par ? q4 - 1 : 0) : (par ? 2 * q4 - 2 : 3 * q4 - 3);
+            const int mid = sym ? 4 * q4 - 4 : 4 * q4 - 3;
+            const int end = par ? 4 * q4 - 1 : 4 * q4 - 2;
+            double sq = sym ? row[0] * Zq[end * C + c] : 0.0;
+            double sp = sym ? row[0] * Zp[end * C + c] : 0.0;
+            for (int b = 1; b < q4; ++b) {
+                sq += row[b] * Zq[(base + b - 1) * C + c];
+                sp += row[b] * Zp[(base + b - 1) * C + c];
+            }
+            yq = sq + row[q4] * Zq[mid * C + c];
+            yp = sp + row[q4] * Zp[mid * C + c];
+        }
+        __syncthreads();
+    } else
     if (flags & RF_FWD) {
         if (k < P) {
             Xq[k * C + c] = qb;
@@ -220,6 +274,39 @@ __global__ void __launch_bounds__(256) k_ring(RingArgs a) {
         }
     }
     double qn = yq, pn = yp;
+    if ((flags & RF_BACK) && fold2) {
+        if (k < P) {
+            Xq[k * C + c] = yq;
+            Xp[k * C + c] = yp;
+        }
+        __syncthreads();
+        // thread t = k < 2 (q4 + 1): quantity t / (q4 + 1) (q, p), column entry
+        // b = t % (q4 + 1); cos rows split by the parity of k (E, O), sin rows by the
+        // parity of j (Be, Bo): A_b = E + O, A_P/2-b = E - O, B_b = Bo + Be,
+        // B_P/2-b = Bo - Be, and x_b = A_b + B_b, x_P-b = A_b - B_b (likewise at P/2 - b)
+        if (k < 2 * (q4 + 1) && c < W.ncols) {
+            const int u = k / (q4 + 1), b = k - u * (q4 + 1);
+            const double *X = u ? Xp : Xq;
+            double *Z = u ? Zp : Zq;
+            double E = 0.0, O = 0.0, Be = 0.0, Bo = 0.0;
+            for (int r = 0; r <= half; r += 2) E += Cm[r * P + b] * X[r * C + c];
+            for (int r = 1; r < half; r += 2) O += Cm[r * P + b] * X[r * C + c];
+            for (int j = 2; j < half; j += 2) Be += Cm[(P - j) * P + b] * X[(P - j) * C + c];
+            for (int j = 1; j < half; j += 2) Bo += Cm[(P - j) * P + b] * X[(P - j) * C + c];
+            const double A1 = E + O, A2 = E - O, B1 = Bo + Be, B2 = Bo - Be;
+            Z[b * C + c] = A1 + B1;
+            if (b > 0) Z[(P - b) * C + c] = A1 - B1;
+            if (b < q4) {
+                Z[(half - b) * C + c] = A2 + B2;
+                if (b > 0) Z[(half + b) * C + c] = A2 - B2;
+            }
+        }
+        __syncthreads();
+        if (act) {
+            qn = Zq[k * C + c];
+            pn = Zp[k * C + c];
+        }
+    } else
     if (flags & RF_BACK) {
         if (k < P) {
             Xq[k * C + c] = yq;
