@@ -205,6 +205,7 @@ __global__ void __launch_bounds__(128) k_prep(EvalArgs a) {
 // rows depend on that dimension alone. Blocks are dimension-major (a block's
 // threads share d), so the phase rows are written by consecutive sites.
 __global__ void __launch_bounds__(128) k_prep_f32(EvalArgs a) {
+    pdl_wait();  // the positions of the ring step ahead
     const Job J = a.jobs[blockIdx.y];
     const SysDev &S = a.sys[J.sys];
     const int ns = S.n_sites;
@@ -271,7 +272,7 @@ __global__ void __launch_bounds__(128) k_prep_f32(EvalArgs a) {
 
 void launch_prep_f32(const EvalArgs &a, cudaStream_t s) {
     const int tiles = (3 * a.max_mols + 127) / 128;
-    k_prep_f32<<<dim3(3 * tiles, a.n_jobs), 128, 0, s>>>(a);
+    launch_pdl(k_prep_f32, dim3(3 * tiles, a.n_jobs), dim3(128), 0, s, a);
 }
 
 // Running sum s (+ compensation c) += v, Kahan's compensated summation.
@@ -889,6 +890,8 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
 // (and 2 c_k dS(k)) in the working precision for k_kforce. One thread per k.
 template <typename R, int MODE>
 __global__ void __launch_bounds__(128) k_sk_reduce(EvalArgs a) {
+    pdl_launch_dependents();  // the k-force may start its staging of the phase rows
+    pdl_wait();               // the structure-factor partials of k_ksk
     const int jb = blockIdx.y;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];
@@ -1002,7 +1005,7 @@ template <typename R, int MODE>
 void launch_sk_reduce(const EvalArgs &a, cudaStream_t s) {
     const bool half = sizeof(R) == 4 && MODE == 0;
     const dim3 g(half ? a.max_batch : (a.max_kvec + 127) / 128, a.n_jobs);
-    k_sk_reduce<R, MODE><<<g, 128, 0, s>>>(a);
+    launch_pdl(k_sk_reduce<R, MODE>, g, dim3(128), 0, s, a);
 }
 
 // ---- k_kforce: reciprocal-space site forces -------------------------------------
@@ -1147,6 +1150,9 @@ __global__ void __launch_bounds__(FT) k_kforce_f32(EvalArgs a) {
         }
     }
     const float bz = S.kbf[2];
+    // the phase rows above come from the force evaluation's prep, complete before
+    // the structure factors started; the weights below from k_sk_reduce
+    pdl_wait();
     float Fx[SPT], Fy[SPT], Fz[SPT], Cx[SPT], Cy[SPT], Cz[SPT];
 #pragma unroll
     for (int u = 0; u < SPT; ++u) Fx[u] = Fy[u] = Fz[u] = Cx[u] = Cy[u] = Cz[u] = 0.f;
@@ -1238,11 +1244,11 @@ void launch_kforce_f32(const EvalArgs &a, dim3 grid, cudaStream_t s) {
     const size_t sm = (size_t)2 * (a.max_kmax + 1) * 2 * FT * sizeof(float2);
     dim3 g2 = grid;
     g2.x = (grid.x + 1) / 2;
-    if (a.kpk && a.max_kmax <= 8) k_kforce_f32<8, 2><<<g2, FT, sm, s>>>(a);
-    else if (a.kpk && a.max_kmax <= 12) k_kforce_f32<12, 2><<<g2, FT, sm, s>>>(a);
-    else if (a.kpk && a.max_kmax <= 16) k_kforce_f32<16, 2><<<g2, FT, sm, s>>>(a);
-    else if (a.kpk && a.max_kmax <= 24) k_kforce_f32<24, 2><<<g2, FT, sm, s>>>(a);
-    else if (a.kpk && a.max_kmax <= 32) k_kforce_f32<32, 2><<<g2, FT, sm, s>>>(a);
+    if (a.kpk && a.max_kmax <= 8) launch_pdl(k_kforce_f32<8, 2>, g2, dim3(FT), sm, s, a);
+    else if (a.kpk && a.max_kmax <= 12) launch_pdl(k_kforce_f32<12, 2>, g2, dim3(FT), sm, s, a);
+    else if (a.kpk && a.max_kmax <= 16) launch_pdl(k_kforce_f32<16, 2>, g2, dim3(FT), sm, s, a);
+    else if (a.kpk && a.max_kmax <= 24) launch_pdl(k_kforce_f32<24, 2>, g2, dim3(FT), sm, s, a);
+    else if (a.kpk && a.max_kmax <= 32) launch_pdl(k_kforce_f32<32, 2>, g2, dim3(FT), sm, s, a);
     else k_kforce<float, 0><<<grid, FT, kforce_smem<float>(a.max_kmax), s>>>(a);
 }
 
@@ -1511,6 +1517,7 @@ __global__ void __launch_bounds__(128) k_intra_f32(EvalArgs a) {
 // Lennard-Jones terms and applies the M-site chain rule.
 constexpr int CMB = 32;
 __global__ void __launch_bounds__(128) k_combine_f32(EvalArgs a) {
+    pdl_launch_dependents();  // the end step may load positions and masses meanwhile
     const int jb = blockIdx.y;
     const Job J = a.jobs[jb];
     const SysDev &S = a.sys[J.sys];

@@ -391,6 +391,9 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
     if (act) {
         qb = a.q[at];
         pb = a.p[at];
+    }
+    pdl_wait();  // the forces of the evaluation ahead
+    if (act) {
         fb = a.f[at];
         fpb = a.fphys[at];
         if (a.kick) {
@@ -833,7 +836,7 @@ void launch_ring(const RingArgs &a, cudaStream_t s, unsigned long long *n) {
 
 void launch_end_step(const RingArgs &a, cudaStream_t s, unsigned long long *n) {
     if (a.n_work <= 0) return;
-    k_end_step<<<a.n_work, 256, 3 * 256 * sizeof(double), s>>>(a);
+    launch_pdl(k_end_step, dim3(a.n_work), dim3(256), 3 * 256 * sizeof(double), s, a);
     if (n) ++*n;
 }
 
