@@ -1937,15 +1937,17 @@ qtg_status qtg_update_pimd(qtg_ctx *ctx, int sys, double *q, double *p, const do
         }
         RingArgs e = ring_args(ctx, sys, 0);
         e.kick = 1;
+        if (staged) {  // the end step writes p back and posts the small results itself
+            e.post_box = sg.box;
+            e.post_energy = sg.box_energy;
+            e.post_rebuilt = sg.box_rebuilt;
+            e.sys_energy = sg.energy;
+            e.sys_rebuilt = sg.rebuilt;
+        }
         launch_end_step(e, ctx->stream, &ctx->launches);
         if (staged || beside) {
             if (err == cudaSuccess) err = cudaEventRecord(ctx->ev_join, ctx->side_stream);
             if (err == cudaSuccess) err = cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0);
-        }
-        if (staged) {
-            StageArgs so = sg;
-            so.mask = STAGE_P | STAGE_SMALL;
-            launch_stage_out(so, ctx->stream, &ctx->launches);
         }
         return err;
     };

@@ -388,11 +388,14 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
     double qb = 0.0, pb = 0.0, fb = 0.0, fpb = 0.0;
     const double m = act ? a.mass[S.mass_off + col] : 1.0;
     const double im = act ? a.inv_mass[S.mass_off + col] : 1.0;
+    __shared__ double *p_out;  // staged per-call step: the caller's momentum array
+    if (threadIdx.x == 0) p_out = a.post_box ? a.post_box->p : nullptr;
     if (act) {
         qb = a.q[at];
         pb = a.p[at];
     }
     pdl_wait();  // the forces of the evaluation ahead
+    __syncthreads();
     if (act) {
         fb = a.f[at];
         fpb = a.fphys[at];
@@ -400,6 +403,7 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
             pb += S.halfdt * fb;  // update.cpp:391-397
             a.p[at] = pb;
         }
+        if (p_out) p_out[(long long)b * S.n_dof + col] = pb;
         Xq[b * C + c] = qb;
         Xp[b * C + c] = pb + S.halfdt * fb;
         if (cf) Xf[b * C + c] = fpb;
@@ -469,6 +473,19 @@ __global__ void __launch_bounds__(256) k_end_step(RingArgs a) {
     // finishes the last system advances them, after every system's close below)
     const unsigned long long st0 = a.fuse_fin ? *a.fin.step : 0ull, rec0 = a.fuse_fin ? *a.fin.records : 0ull;
     const bool last = ordered_system_sum<4>(bsum, W.slot, S.cw_begin, S.cw_count, a.cw_part, a.cw_ticket + W.sys, dst);
+    if (last && a.post_box) {
+        for (int k = threadIdx.x; k < P; k += blockDim.x) {
+            a.post_energy[k] = a.sys_energy[k];
+            a.post_rebuilt[k] = a.sys_rebuilt[k];
+        }
+        if (threadIdx.x == 0) {  // the thread that completed the accumulators
+            a.post_box->heat_out = a.run[W.sys].heat;
+            a.post_box->acc = a.acc[W.sys];
+            a.post_box->status = *a.status;
+            a.acc[W.sys] = SysAcc{};
+            *a.status = 0u;
+        }
+    }
     // fused close of the step: the block that completed a system's sums records it
     // and sets its next centroid factor; the last system to finish advances the
     // step and record counters, as k_finalize would after every system

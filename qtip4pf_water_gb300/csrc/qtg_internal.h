@@ -389,6 +389,15 @@ struct RingArgs {
                              // current step of systems draw_sys0 .. draw_sys0 + n_draw - 1
                              // while the ring work runs (0: none)
     int draw_sys0;
+    // end step of a staged per-call step: the kicked momenta also go to the caller's
+    // array named in this mailbox, and the block that completes the system's sums
+    // posts the small results there (heat, energies, rebuild flags, accumulators,
+    // status), then clears the accumulators and the status word
+    struct CallBox *post_box;
+    double *post_energy;       // device address of the mailbox's energy[]
+    int *post_rebuilt;         // device address of its rebuilt[]
+    const double *sys_energy;  // the system's per-bead energies
+    const int *sys_rebuilt;    // the system's per-bead rebuild flags
 };
 
 
