@@ -275,7 +275,7 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def run_e2e(q, st, steps, flush):
+def run_e2e(q, st, steps, flush, autotune=True):
     import torch
 
     s = q.System.create(N_MOLS, N_BEADS, st.box_bohr, precision=q.MIXED, temp_K=TEMP, dt_fs=DT_FS,
@@ -295,7 +295,8 @@ def run_e2e(q, st, steps, flush):
     _, fp = pinned(np.zeros_like(st.q))
     mass, charge = s.masses(), s.charges()
     s.set_state(st.q, st.p)  # the autotuner times force evaluations of the device state
-    s.ctx.autotune(10)  # the library's launch-shape autotuner, once at set-up as a user would
+    if autotune:  # the library's launch-shape autotuner, once at set-up as a user would
+        s.ctx.autotune(10)
     s.force_eval_trotter(qq, f, charge, point, lst)
     fp[:] = f
     heat = 0.0
