@@ -349,7 +349,7 @@ def roofline(q, st, mix):
            "frac": ring_bw / hbm, "peak_source": which + " (MEASURED_PEAKS.json hbm_gbs)",
            "algorithmic_bytes_per_launch": ring_bytes,
            "note": "stated against HBM as the bandwidth convention for the integrator; the kernel is bound by "
-                   "the FP64 pipe (folded P x P normal-mode transforms in FP64, ncu: FP64 pipe ~77 % busy; "
+                   "the FP64 pipe (twice-folded P x P normal-mode transforms in FP64, ncu: FP64 pipe ~69 % busy; "
                    "GB300 FP64 is ~1/64 of FP32), its data L2-resident"}
     return {"main": main, "secondary": sec, "kernel_ms": ms,
             "pairs_within_rc_per_bead": nreal, "lj_pairs_per_bead": nlj}
