@@ -914,7 +914,9 @@ __global__ void __launch_bounds__(128) k_sk_reduce(EvalArgs a) {
     }
     __shared__ double red[4];
     __shared__ float2 wl[128];
+    __shared__ float redf[4];
     double e = 0.0;
+    float ef = 0.f;  // FP32 form: the k's energy term, summed over the block in FP32
     if (k < nk) {
         const KVec kv = a.kvec[S.kvec_off + k];
         const double w = 2.0 * kv.coef * ((half && kv.twin) ? 2.0 : 1.0);
@@ -941,7 +943,7 @@ __global__ void __launch_bounds__(128) k_sk_reduce(EvalArgs a) {
                 kahan_add(ys, yc, p.y - p.w);
             }
             const float fr = xs - xc, fi = ys - yc, wf = (float)w;
-            e = 0.5 * w * ((double)fr * fr + (double)fi * fi);
+            ef = 0.5f * wf * fmaf(fr, fr, fi * fi);
             V2<R> v;
             v.x = (R)(wf * fr);
             v.y = (R)(wf * fi);
@@ -994,7 +996,13 @@ __global__ void __launch_bounds__(128) k_sk_reduce(EvalArgs a) {
             }
         }
     }
-    if (MODE == 0) {
+    if (half) {  // the block's FP32 partial, added to the FP64 energy
+        float t = warp_sum(ef);
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        if (lane == 0) redf[w] = t;
+        __syncthreads();
+        if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], (double)(((redf[0] + redf[1]) + redf[2]) + redf[3]));
+    } else if (MODE == 0) {
         const double t = block_sum(e, red);
         if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
     }
@@ -1535,12 +1543,12 @@ __global__ void __launch_bounds__(128) k_combine_f32(EvalArgs a) {
         for (int o = threadIdx.x; o < 9 * nm; o += blockDim.x) {
             float sum = 0.f, comp = 0.f;
             int p = 0;
-            for (; p + 8 <= np; p += 8) {  // eight planes' loads in flight, then their sums in order
-                float v[8];
+            for (; p + 16 <= np; p += 16) {  // sixteen planes' loads in flight, then their sums in order
+                float v[16];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) v[u] = pl[(p + u) * stride + o];
+                for (int u = 0; u < 16; ++u) v[u] = pl[(p + u) * stride + o];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) kahan_add(sum, comp, v[u]);
+                for (int u = 0; u < 16; ++u) kahan_add(sum, comp, v[u]);
             }
             for (; p < np; ++p) kahan_add(sum, comp, pl[p * stride + o]);
             fsum[o] = sum - comp;
