@@ -1803,7 +1803,6 @@ __global__ void __launch_bounds__(128) k_lj_dense(EvalArgs a) {
     const int N = S.n_mols;
     if (blockIdx.x * LJD_ROWS >= N) return;
     __shared__ float4 sj[LJD_CH];
-    __shared__ double red[4];
     const int sub = threadIdx.x & (LJD_SUB - 1);
     const int i = blockIdx.x * LJD_ROWS + threadIdx.x / LJD_SUB;
     const bool act = i < N;
@@ -1874,7 +1873,7 @@ __global__ void __launch_bounds__(128) k_lj_dense(EvalArgs a) {
         fz += __shfl_xor_sync(0xffffffffu, fz, m);
         el += __shfl_xor_sync(0xffffffffu, el, m);
     }
-    double e = 0.0;
+    float e = 0.f;
     if (act && sub == 0) {
         if (a.lj_plane) {
             a.ljf[J.site_off / 3 + i] = make_float4(fx, fy, fz, 0.f);
@@ -1884,10 +1883,14 @@ __global__ void __launch_bounds__(128) k_lj_dense(EvalArgs a) {
             f[9 * i + 1] += (double)fy;
             f[9 * i + 2] += (double)fz;
         }
-        e = 0.5 * (double)el;
+        e = 0.5f * el;
     }
-    const double t = block_sum(e, red);
-    if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
+    // the block's FP32 partial (as the real-space warp partials), added to the FP64 energy
+    __shared__ float redf[4];
+    e = warp_sum(e);
+    if ((threadIdx.x & 31) == 0) redf[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], (double)(((redf[0] + redf[1]) + redf[2]) + redf[3]));
 }
 
 // site-force output of the reciprocal-space-only path: out += sum of the k-chunk planes
