@@ -1557,7 +1557,6 @@ __global__ void __launch_bounds__(128) k_combine_f32(EvalArgs a) {
     __syncthreads();
     double e = 0.0;
     if ((int)threadIdx.x < nm) {
-        const double *q = a.pos + J.pos_off + 9 * m;
         double *f = a.out + J.out_off + 9 * m;
         float fs[9];
         for (int k = 0; k < 9; ++k) fs[k] = fsum[9 * threadIdx.x + k];
