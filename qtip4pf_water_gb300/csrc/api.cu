@@ -2162,7 +2162,7 @@ qtg_status qtg_autotune(qtg_ctx *ctx, int iters, double *ms_heuristic, double *m
     };
     // each count governs one kernel: k_real (n_rj), k_ksk (n_sc), k_kforce (n_kc), 0
     // the launcher's heuristic. The force kernels run concurrently (forked branches
-    // of one evaluation), so candidates are judged by the time of the whole force
+    // of one evaluation), so candidates are compared by the time of the whole force
     // evaluation: coordinate descent from the heuristic, one count at a time.
     static const int cand_rk[] = {0, 1, 2, 3, 4, 6, 8, 12, 16};       // k_real, k_kforce
     static const int cand_sc[] = {0, 1, 2, 4, 6, 8, 12, 16, 24, 32};  // k_ksk
@@ -2170,7 +2170,7 @@ qtg_status qtg_autotune(qtg_ctx *ctx, int iters, double *ms_heuristic, double *m
     double best_ms = 0.0;
     CKS(eval_ms(best, &best_ms));  // fills the scratch arrays, warms the kernels
     CKS(eval_ms(best, &best_ms));
-    for (int round = 0; round < 2; ++round) {
+    for (int sweep = 0; sweep < 2; ++sweep) {
         bool moved = false;
         for (int k = 0; k < 3; ++k) {
             const int *cand = k == 1 ? cand_sc : cand_rk;
