@@ -153,8 +153,9 @@ qtg_status qtg_get_conserved(qtg_ctx *ctx, int sys, double *q, double *p, const 
  * the Suzuki-Chin finite-difference terms read them as the reference does.
  * When q, p, f, (fphys,) disp lie in page-locked host memory the device can
  * address (cudaHostAlloc / cudaHostRegister without the read-only flag) and do
- * not overlap, qtg_update_pimd moves them inside its captured step graph (stage
- * kernels); otherwise by copy calls. Results are the same bits either way. */
+ * not overlap, qtg_update_pimd moves them inside its captured step graph (the
+ * step's kernels read and write the caller's memory directly); otherwise by copy
+ * calls. Results are the same bits either way. */
 qtg_status qtg_update_class(qtg_ctx *ctx, int sys, double *q, double *p, const double *mass,
                             double *f, const double *charge, int *point, int *list, double *disp,
                             double *energy);
