@@ -245,7 +245,7 @@ def run_gpu(args):
     e2e = run_e2e(q, st, min(args.steps, 200), flush)
 
     # ---- roofline of the dominant kernel -----------------------------------------------------
-    roof = roofline(q, st, mix)
+    roof = roofline(q, st, mix, t64 / k2)
     line = {
         "metric": METRIC,
         "value": value, "unit": "ns/day", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -266,6 +266,7 @@ def run_gpu(args):
         "gpu_launches": launches,
         "e2e": e2e,
         "roofline": roof["main"], "roofline_secondary": roof["secondary"], "kernel_ms": roof["kernel_ms"],
+        "roofline_fp64_form": roof.get("fp64_form"), "fp64_peak_tflops": roof["fp64_peak_tflops"],
         "clocks": sampler.summary(),
     }
     if rank == 0:
@@ -320,16 +321,34 @@ def run_e2e(q, st, steps, flush, autotune=True):
                     "launch shapes autotuned once at set-up (qtg_autotune)"}
 
 
-def roofline(q, st, mix):
+def ring_fp64_flop(P, n_dof):
+    """FP64 flops one k_ring launch executes for one system, counted from its
+    source: per dof column, four transforms (q and p, forward and back), each
+    with the folds (8 (P/4 - 1) + 4 adds for P divisible by 4, else P - 1) and
+    P rows of about 2 (P/4) + 0.5 flops (twice-folded) or P + 1 (once-folded);
+    per bead and dof 26 flops for the kick, two half sqrt-Cayley steps, the O
+    step and its heat."""
+    if P % 4 == 0 and P >= 8:
+        q4 = P // 4
+        tr = 8 * (q4 - 1) + 4 + (2 * q4 + 0.5) * P
+    else:
+        tr = (P - 1) + (P + 1) * P
+    return n_dof * (4 * tr + 26 * P)
+
+
+def roofline(q, st, mix, t64_step=None):
     hbm, which = _peaks()
     fp32 = q.fp32_peak_tflops()
+    fp64 = q.fp64_peak_tflops()
     s = make_system(q, q.MIXED, q.TROTTER, st)
     info = s.info
     nreal, nlj = count_pairs(st.q, st.box_bohr, info.rc ** 2, N_MOLS)
     ms = {k: s.ctx.time_kernel(k, 20)
           for k in ("prep", "real", "ksk", "sk_reduce", "kforce", "combine", "lj", "ring", "end_step", "rebuild")}
     P, ns = N_BEADS, 3 * N_MOLS
-    flop = {"real": 2 * nreal * FLOP_REAL * P,  # every pair is evaluated from both sides
+    # algorithmic work per launch: each site pair within r_c counted once (60 flop),
+    # each (site, k-vector) of the half set 8 flop for S(k) and 12 for the force
+    flop = {"real": nreal * FLOP_REAL * P,
             "ksk": ns * info.n_kvectors * FLOP_SK * P, "kforce": ns * info.n_kvectors * FLOP_KF * P}
     top = max(("real", "ksk", "kforce"), key=lambda k: ms[k])
     ach = flop[top] / (ms[top] * 1e-3) / 1e12
@@ -337,22 +356,33 @@ def roofline(q, st, mix):
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
         with open(tp) as f:
-            traffic = json.load(f).get(top)
+            tj = json.load(f)
+        traffic = tj.get(top)
     main = {"kernel": "k_" + top, "bound": "fp32", "achieved": ach, "peak": fp32, "unit": "TFLOP/s",
             "frac": ach / fp32, "traffic": traffic,
+            "traffic_source": "not measured in this run: dram__bytes_read.sum + dram__bytes_write.sum per launch "
+                              "from the ncu capture recorded in profiles/traffic.json (command there)",
             "peak_source": "FP32 FMA throughput measured live by qtg_fp32_peak (MEASURED_PEAKS.json has no FP32 figure)",
-            "algorithmic_flop_per_launch": flop[top]}
+            "algorithmic_flop_per_launch": flop[top],
+            "work": "site pairs within r_c once each x 60 flop x %d beads (%.0f pairs a bead)" % (P, nreal)}
     nd = 9 * N_MOLS
     ring_bytes = P * nd * 8 * 5  # read q, p, f; write q, p
     ring_bw = ring_bytes / (ms["ring"] * 1e-3) / 1e9
-    sec = {"kernel": "k_ring", "bound": "hbm", "achieved": ring_bw, "peak": hbm, "unit": "GB/s",
-           "frac": ring_bw / hbm, "peak_source": which + " (MEASURED_PEAKS.json hbm_gbs)",
-           "algorithmic_bytes_per_launch": ring_bytes,
-           "note": "stated against HBM as the bandwidth convention for the integrator; the kernel is bound by "
-                   "the FP64 pipe (twice-folded P x P normal-mode transforms in FP64, ncu: FP64 pipe ~69 % busy; "
-                   "GB300 FP64 is ~1/64 of FP32), its data L2-resident"}
-    return {"main": main, "secondary": sec, "kernel_ms": ms,
-            "pairs_within_rc_per_bead": nreal, "lj_pairs_per_bead": nlj}
+    ring_flop = ring_fp64_flop(P, nd)
+    ring_tf = ring_flop / (ms["ring"] * 1e-3) / 1e12
+    sec = {"kernel": "k_ring", "bound": "fp64", "achieved": ring_tf, "peak": fp64, "unit": "TFLOP/s",
+           "frac": ring_tf / fp64, "peak_source": "FP64 FMA throughput measured live by qtg_fp64_peak",
+           "fp64_flop_per_launch": ring_flop,
+           "bytes": {"achieved_gbs": ring_bw, "peak_gbs": hbm, "frac": ring_bw / hbm,
+                     "algorithmic_bytes_per_launch": ring_bytes, "peak_source": which + " (MEASURED_PEAKS.json hbm_gbs)"}}
+    out = {"main": main, "secondary": sec, "kernel_ms": ms, "fp32_peak_tflops": fp32, "fp64_peak_tflops": fp64,
+           "pairs_within_rc_per_bead": nreal, "lj_pairs_per_bead": nlj}
+    if t64_step:
+        per_eval = nreal * FLOP_REAL + nlj * FLOP_LJ + ns * info.n_kvectors * (FLOP_SK + FLOP_KF) + N_MOLS * FLOP_INTRA
+        tf = per_eval * P / t64_step / 1e12
+        out["fp64_form"] = {"achieved": tf, "peak": fp64, "unit": "TFLOP/s", "frac": tf / fp64,
+                            "work": "algorithmic flop of one step (%d force evaluations) / step time" % P}
+    return out
 
 
 def pile_noise(rng, n_dof, n_beads):

@@ -202,9 +202,9 @@ qtg_status qtg_reset_estimators(qtg_ctx *ctx);
 /* No counterpart in the reference: the reciprocal-space Ewald sum of qtg_kwald
  * (FP64) for callers that cannot allocate device memory -- engines and plugins
  * that own the GPU memory budget and pass preallocated buffers to their force
- * routines, and work issued while another library captures the stream into a
- * CUDA graph. It calls no cudaMalloc/cudaFree and needs no qtg_ctx: all scratch
- * lives in one static device array of 2.76 MiB (2,895,616 bytes) that every GPU loading the
+ * routines (an allocation of their own would escape that budget or fail under
+ * its cap). It calls no cudaMalloc/cudaFree and needs no qtg_ctx: all scratch
+ * lives in one static device array of 2.76 MiB (2,895,872 bytes) that every GPU loading the
  * library holds until exit.
  *   sites   device, double[3 n_sites]: charge sites (M, H1, H2 per molecule)
  *   charge  device, double[n_sites]
@@ -216,9 +216,12 @@ qtg_status qtg_reset_estimators(qtg_ctx *ctx);
  * anything larger returns QTG_ERR_ARG. Work is queued on `cuda_stream` and the
  * call returns without waiting. The first call on a device looks up the array's
  * device address (once per device, that device current) and should therefore
- * come before any stream capture. Every call shares the array, so calls that
+ * come before any stream capture; that set-up is locked, so first calls from
+ * several host threads are safe. Every call shares the array, so calls that
  * overlap on the GPU (other streams, other host threads) race; each call
- * rebuilds every table it reads, so nothing carries over between calls. */
+ * rebuilds every table it reads, so nothing carries over between calls. An
+ * error already pending from the caller's own CUDA work is returned as
+ * QTG_ERR_CUDA, uncleared, and nothing is launched. */
 #define QTG_NOALLOC_MAX_SITES 1536
 #define QTG_NOALLOC_MAX_KMAX 12
 qtg_status qtg_kwald_noalloc(const double *sites, const double *charge, int n_sites,
@@ -235,6 +238,9 @@ qtg_status qtg_time_kernel(qtg_ctx *ctx, const char *name, int iters, double *av
 /* FP32 fused-multiply-add throughput of the current device (TFLOP/s, 2 flops
  * per FMA) from a dependent-chain kernel filling every SM. */
 qtg_status qtg_fp32_peak(double *tflops);
+/* The same for FP64 fused multiply-adds (the bound of the FP64 form and of the
+ * FP64 normal-mode / integrator kernels). */
+qtg_status qtg_fp64_peak(double *tflops);
 
 /* ---- centroid-constrained PIMD (no reference counterpart) ------------------- */
 /* With the centroid fixed, the device stepper holds each atom's bead centroid

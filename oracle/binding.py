@@ -35,6 +35,12 @@ class QoSys(C.Structure):
     ]
 
 
+class QoStepper(C.Structure):
+    _fields_ = [("seed", C.c_ulonglong), ("sys", C.c_int), ("thermostat", C.c_int), ("trotter", C.c_int),
+                ("centroid_fixed", C.c_int), ("tau0_fs", C.c_double), ("step", C.c_ulonglong),
+                ("cf_samples", C.c_double)]
+
+
 def build(force: bool = False) -> str:
     src = os.path.join(HERE, "qtip_oracle.c")
     if force or not os.path.exists(SO) or os.path.getmtime(SO) < os.path.getmtime(src):
@@ -76,10 +82,27 @@ def lib():
         L.qo_update_class.restype = C.c_double
         L.qo_update_pimd.argtypes = [S, D, D, D, D, D, D, I, I, D, C.c_int, D, D, D, C.c_int]
         L.qo_update_pimd.restype = C.c_double
+        U = C.POINTER(C.c_uint)
+        L.qo_philox4x32_10.argtypes = [U, C.c_uint, C.c_uint, U]
+        L.qo_stepper_normal_f32.argtypes = [C.c_uint, C.c_uint]
+        L.qo_stepper_normal_f32.restype = C.c_double
+        L.qo_stepper_centroid_draw.argtypes = [C.c_ulonglong, C.c_int, C.c_int, C.c_ulonglong, D, D]
+        L.qo_stepper_centroid_draw.restype = C.c_int
+        L.qo_stepper_step.argtypes = [S, C.POINTER(QoStepper), D, D, D, D, D, D, I, I, D, C.c_int, D, D]
+        L.qo_stepper_step.restype = C.c_double
         L.qo_count_kvectors.argtypes = [S]
         L.qo_count_kvectors.restype = C.c_int
         _lib = L
     return _lib
+
+
+def philox4x32_10(ctr, key):
+    """Philox4x32-10 block of the oracle (four 32-bit words)."""
+    L = lib()
+    c = (C.c_uint * 4)(*[int(x) & 0xFFFFFFFF for x in ctr])
+    o = (C.c_uint * 4)()
+    L.qo_philox4x32_10(c, int(key[0]) & 0xFFFFFFFF, int(key[1]) & 0xFFFFFFFF, o)
+    return [int(x) for x in o]
 
 
 def _d(a):
@@ -172,6 +195,19 @@ class Oracle:
                                   _d(self.charge), _i(point), _i(lst), _d(disp), 1 if is_nvt else 0,
                                   _d(nz), C.byref(h), C.byref(pot), 1 if trotter else 0)
         return e, h.value, pot.value
+
+    def stepper(self, seed, sys=0, thermostat=1, trotter=True, centroid_fixed=False, tau0_fs=100.0):
+        """State of the device stepper's propagation for this system (counter at 1,
+        as the device's stands after its first force evaluation)."""
+        return QoStepper(seed=int(seed), sys=int(sys), thermostat=int(thermostat), trotter=1 if trotter else 0,
+                         centroid_fixed=1 if centroid_fixed else 0, tau0_fs=float(tau0_fs), step=1, cf_samples=0.0)
+
+    def stepper_step(self, st, q, p, f, fphys, point, lst, disp, is_nvt=True, cf_acc=None):
+        pot = C.c_double(0.0)
+        e = self.L.qo_stepper_step(C.byref(self.s), C.byref(st), _d(q), _d(p), _d(self.mass), _d(f), _d(fphys),
+                                   _d(self.charge), _i(point), _i(lst), _d(disp), 1 if is_nvt else 0,
+                                   None if cf_acc is None else _d(cf_acc), C.byref(pot))
+        return e, pot.value
 
     def count_kvectors(self):
         return self.L.qo_count_kvectors(C.byref(self.s))

@@ -9,6 +9,7 @@
 #include "qtip_oracle.h"
 
 #include <math.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -717,5 +718,181 @@ double qo_update_pimd(const qo_sys *s, double *q, double *p, const double *mass,
         e = qo_force_eval_sc(s, q, f, charge, mass, point, list, pot_est, fphys);
     }
     for (size_t i = 0; i < (size_t)P * nd; ++i) p[i] += s->halfdt * f[i];
+    return e;
+}
+
+/* ==== the device stepper's propagation (new paths, no reference counterpart) ====
+ * The library's device-resident stepper follows update.cpp:271-401 (B, NM
+ * forward, sqrt-Cayley A, O, A, NM back, list check, forces, B) but draws its
+ * thermostat noise from a counter-based generator keyed by (seed, system, step,
+ * mode, dof) instead of std::mt19937, and adds two thermostat variants and a
+ * centroid constraint. This section restates that propagation on the CPU so
+ * that a thermostatted device trajectory can be followed step for step.
+ *
+ * Generator: Philox4x32-10 (Salmon, Moraes, Dror & Shaw, "Parallel random
+ * numbers: as easy as 1, 2, 3", SC'11): ten rounds of
+ *   (c0, c1, c2, c3) <- (hi(M1 c2) ^ c1 ^ k0, lo(M1 c2), hi(M0 c0) ^ c3 ^ k1, lo(M0 c0))
+ * with M0 = 0xD2511F53, M1 = 0xCD9E8D57 and the key bumped by the Weyl
+ * constants (0x9E3779B9, 0xBB67AE85) after every round. */
+void qo_philox4x32_10(const uint32_t ctr[4], uint32_t k0, uint32_t k1, uint32_t out[4]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c0 = n0;
+        c1 = (uint32_t)p1;
+        c2 = n2;
+        c3 = (uint32_t)p0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+
+/* stream keys: the low and high seed words mixed with the system index and the
+ * stream tag (1 normal-mode noise, 2 centroid normal, 3 centroid gamma) */
+static void stepper_key(uint64_t seed, int sys, uint32_t tag, uint32_t *k0, uint32_t *k1) {
+    *k0 = (uint32_t)seed ^ ((uint32_t)sys * 0x85EBCA6Bu);
+    *k1 = (uint32_t)(seed >> 32) ^ (tag * 0xC2B2AE35u);
+}
+
+static void stepper_block(uint32_t c0, uint32_t c1, uint64_t st, uint32_t k0, uint32_t k1, uint32_t out[4]) {
+    const uint32_t ctr[4] = {c0, c1, (uint32_t)st, (uint32_t)(st >> 32)};
+    qo_philox4x32_10(ctr, k0, k1, out);
+}
+
+/* uniform in (0, 1) from two words, 53 significant bits */
+static double u01_from(uint32_t a, uint32_t b) {
+    uint64_t x = ((uint64_t)a << 21) ^ (uint64_t)(b >> 11);
+    x &= ((1ull << 53) - 1ull);
+    return ((double)x + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+/* thermostat noise of the normal modes: Box-Muller in single precision from the
+ * block's first two words (24-bit uniforms at cell centres); each operation is
+ * rounded to float here as on the device (libm in double, then rounded: the
+ * device's single-precision functions differ from this by an ulp or two) */
+double qo_stepper_normal_f32(uint32_t v0, uint32_t v1) {
+    const float u1 = ((float)(v0 >> 8) + 0.5f) * (1.0f / 16777216.0f);
+    const float u2 = ((float)(v1 >> 8) + 0.5f) * (1.0f / 16777216.0f);
+    const float c = (float)cos(2.0 * 3.14159265358979323846 * (double)u2);
+    const float l = (float)log((double)u1);
+    const float r = sqrtf(-2.0f * l);
+    return (double)(r * c);
+}
+
+/* Box-Muller in double precision: the first of the pair */
+static double normal2_x(const uint32_t v[4]) {
+    const double u1 = u01_from(v[0], v[1]), u2 = u01_from(v[2], v[3]);
+    return sqrt(-2.0 * log(u1)) * cos(2.0 * 3.14159265358979323846 * u2);
+}
+
+/* Gamma(shape), shape >= 1, by Marsaglia & Tsang ("A simple method for
+ * generating gamma variables", ACM TOMS 26, 2000): candidate `it` takes its
+ * normal from block (2 it, 0) and its uniform from block (2 it + 1, 0); the
+ * first accepted of at most 64 candidates is returned (*ok = 0 if none is). */
+static double stepper_gamma(double shape, uint64_t seed, int sys, uint64_t st, int *ok) {
+    const double d = shape - 1.0 / 3.0, cc = 1.0 / sqrt(9.0 * d);
+    uint32_t k0, k1, v[4];
+    stepper_key(seed, sys, 3u, &k0, &k1);
+    for (uint32_t it = 0; it < 64; ++it) {
+        stepper_block(2 * it, 0u, st, k0, k1, v);
+        const double x = normal2_x(v);
+        double w = 1.0 + cc * x;
+        if (w <= 0.0) continue;
+        w = w * w * w;
+        stepper_block(2 * it + 1, 0u, st, k0, k1, v);
+        const double u = u01_from(v[0], v[1]);
+        if (u < 1.0 - 0.0331 * x * x * x * x || log(u) < 0.5 * x * x + d * (1.0 - w + log(w))) return d * w;
+    }
+    *ok = 0;
+    return shape;
+}
+
+int qo_stepper_centroid_draw(unsigned long long seed, int sys, int n_dof, unsigned long long st, double *R,
+                             double *g2) {
+    uint32_t k0, k1, v[4];
+    stepper_key(seed, sys, 2u, &k0, &k1);
+    stepper_block(0u, 0u, st, k0, k1, v);
+    *R = normal2_x(v);
+    int ok = 1;
+    *g2 = 2.0 * stepper_gamma(0.5 * (n_dof - 1), seed, sys, st, &ok);
+    return ok;
+}
+
+/* One device-stepper step (update.cpp:271-401 with the changes above):
+ *  - PILE-G (thermostat 1): centroid p *= alpha, alpha^2 = (R^2 + g2) /
+ *    (2 beta_n K0), K0 the centroid normal-mode kinetic energy at the O step and
+ *    (R, g2) drawn at counter step - 1; modes k >= 1 as thermostat.cpp:119-133
+ *    with xi from block (dof, k) at counter step;
+ *  - PILE-L (thermostat 2): as PILE-G for k >= 1; the centroid is a Langevin
+ *    mode too, c1 = exp(-dt / tau0), xi from block (dof, 0);
+ *  - centroid_fixed: the centroid normal-mode momentum is zeroed before the
+ *    free ring-polymer step and not thermostatted, so the centroid stays put;
+ *    cf_acc (per dof, may be NULL) accumulates (1/P) sum_b fphys_b after the
+ *    forces, st->cf_samples counts the steps.
+ * The counter advances by one per step (the device's starts at 1 after its
+ * first force evaluation). Returns the force assembly's total energy. */
+double qo_stepper_step(const qo_sys *s, qo_stepper *st, double *q, double *p, const double *mass, double *f,
+                       double *fphys, const double *charge, int *point, int *list, double *disp, int is_nvt,
+                       double *cf_acc, double *pot_est) {
+    const int P = s->n_beads, nd = s->n_dof, N = s->n_mols;
+    for (size_t i = 0; i < (size_t)P * nd; ++i) p[i] += s->halfdt * f[i];
+    qo_ftransform(s, q, nd, 1);
+    qo_ftransform(s, p, nd, 1);
+    qo_ftransform(s, disp, 3 * N, 1);
+    if (st->centroid_fixed)
+        for (int i = 0; i < nd; ++i) p[i] = 0.0;
+    cayley_half(s, q, p, mass, disp);
+    if (is_nvt && st->thermostat != 0) {
+        uint32_t k0, k1, v[4];
+        stepper_key(st->seed, st->sys, 1u, &k0, &k1);
+        const double pref = 4.0 / s->beta_n;
+        for (int k = 0; k < P; ++k) {
+            double *pk = p + (size_t)k * nd;
+            if (k == 0 && st->centroid_fixed) continue;
+            if (k == 0 && st->thermostat == 1) {
+                double ke0 = 0.0, R, g2;
+                for (int i = 0; i < nd; ++i) ke0 += 0.5 * pk[i] * pk[i] / mass[i];
+                qo_stepper_centroid_draw(st->seed, st->sys, nd, st->step - 1, &R, &g2);
+                const double alpha = sqrt((R * R + g2) / (2.0 * s->beta_n * ke0));
+                for (int i = 0; i < nd; ++i) pk[i] *= alpha;
+                continue;
+            }
+            const double c1 = k == 0 ? exp(-s->dt / (st->tau0_fs * K.fs2au)) : exp(-s->dt * pref * sin(k * QO_PI / P));
+            const double c2 = sqrt(1.0 - c1 * c1);
+            for (int i = 0; i < nd; ++i) {
+                stepper_block((uint32_t)i, (uint32_t)k, st->step, k0, k1, v);
+                const double xi = qo_stepper_normal_f32(v[0], v[1]);
+                pk[i] = c1 * pk[i] + sqrt(mass[i] / s->beta_n) * c2 * xi;
+            }
+        }
+    }
+    cayley_half(s, q, p, mass, disp);
+    qo_ftransform(s, q, nd, 0);
+    qo_ftransform(s, p, nd, 0);
+    qo_ftransform(s, disp, 3 * N, 0);
+    for (int b = 0; b < P; ++b)
+        if (needs_rebuild(s, disp, b)) qo_neighbour_list(s, q, point, list, disp, b);
+    double e;
+    if (st->trotter) {
+        e = qo_force_eval_trotter(s, q, f, charge, point, list, pot_est);
+        memcpy(fphys, f, sizeof(double) * (size_t)P * nd);
+    } else {
+        e = qo_force_eval_sc(s, q, f, charge, mass, point, list, pot_est, fphys);
+    }
+    if (cf_acc && st->centroid_fixed) {
+        for (int i = 0; i < nd; ++i) {
+            double sf = 0.0;
+            for (int b = 0; b < P; ++b) sf += fphys[(size_t)b * nd + i];
+            cf_acc[i] += sf / (double)P;
+        }
+        st->cf_samples += 1.0;
+    }
+    for (size_t i = 0; i < (size_t)P * nd; ++i) p[i] += s->halfdt * f[i];
+    st->step += 1;
     return e;
 }

@@ -75,6 +75,27 @@ double qo_update_class(const qo_sys *s, double *q, double *p, const double *mass
 double qo_update_pimd(const qo_sys *s, double *q, double *p, const double *mass, double *f,
                       double *fphys, const double *charge, int *point, int *list, double *disp,
                       int is_nvt, const double *noise, double *heat, double *pot_est, int trotter);
+/* ---- the device stepper's propagation (new paths; no reference counterpart) ----
+ * Counter-based noise (Philox4x32-10), PILE-G / PILE-L thermostats and the
+ * centroid constraint as the library's device-resident stepper applies them. */
+typedef struct qo_stepper {
+    unsigned long long seed; /* the system's seed */
+    int sys;                 /* the system's index in its context */
+    int thermostat;          /* 0 none, 1 PILE-G, 2 PILE-L */
+    int trotter;             /* 1 second-order assembly, 0 Suzuki-Chin */
+    int centroid_fixed;      /* 1: centroid-constrained PIMD */
+    double tau0_fs;          /* PILE-L centroid time constant */
+    unsigned long long step; /* counter while the next step runs (1 after the first force evaluation) */
+    double cf_samples;       /* steps accumulated into the mean centroid force */
+} qo_stepper;
+void qo_philox4x32_10(const unsigned int ctr[4], unsigned int k0, unsigned int k1, unsigned int out[4]);
+double qo_stepper_normal_f32(unsigned int v0, unsigned int v1);
+int qo_stepper_centroid_draw(unsigned long long seed, int sys, int n_dof, unsigned long long st, double *R,
+                             double *g2);
+double qo_stepper_step(const qo_sys *s, qo_stepper *st, double *q, double *p, const double *mass, double *f,
+                       double *fphys, const double *charge, int *point, int *list, double *disp, int is_nvt,
+                       double *cf_acc, double *pot_est);
+
 /* number of k-vectors forces.cpp:251-445 visits (each +/- combination counted once). */
 int qo_count_kvectors(const qo_sys *s);
 

@@ -106,6 +106,7 @@ def load(build_if_missing: bool = True):
         "qtg_reset_estimators": ([V], C.c_int),
         "qtg_time_kernel": ([V, C.c_char_p, C.c_int, D], C.c_int),
         "qtg_fp32_peak": ([D], C.c_int),
+        "qtg_fp64_peak": ([D], C.c_int),
         "qtg_autotune": ([V, C.c_int, D, D], C.c_int),
         "qtg_transfer_bytes": ([V, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], C.c_int),
         "qtg_sym_descriptors": ([V, C.c_int, C.c_int, D, V, V], C.c_int),
@@ -249,6 +250,15 @@ def fp32_peak_tflops():
     st = load().qtg_fp32_peak(C.byref(t))
     if st != 0:
         raise QtgError(st, "fp32 probe failed")
+    return t.value
+
+
+def fp64_peak_tflops():
+    """Measured FP64 FMA throughput of the current device (TFLOP/s)."""
+    t = C.c_double(0.0)
+    st = load().qtg_fp64_peak(C.byref(t))
+    if st != 0:
+        raise QtgError(st, "fp64 probe failed")
     return t.value
 
 

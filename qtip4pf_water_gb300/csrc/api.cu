@@ -604,8 +604,11 @@ void enqueue_step(qtg_ctx *c, int sys, int nvt, int ext_noise, bool pile_g) {
     r.noise = ext_noise ? c->noise : nullptr;
     r.pile_g = pile_g ? 1 : 0;
     // the finalize below draws from (seed, system, step) only: its draws are made
-    // here by extra ring blocks, off the step's critical path
-    const bool ahead = nvt && sys < 0 && !ext_noise;
+    // here by extra ring blocks, off the step's critical path. NVE steps draw and
+    // set the next centroid factor too, so that an NVT step after NVE steps
+    // rescales with the factor of its own step (draws at the step before it and
+    // the current centroid kinetic energy), never a stale one.
+    const bool ahead = sys < 0 && !ext_noise;
     r.n_draw = ahead ? c->n_sys : 0;
     launch_ring(r, c->stream, &c->launches);
     const int jb = sys < 0 ? 0 : c->sys_h[sys].job_base;
@@ -621,7 +624,7 @@ void enqueue_step(qtg_ctx *c, int sys, int nvt, int ext_noise, bool pile_g) {
     }
     enqueue_forces(c, sys, false);
     if (beside) cudaStreamWaitEvent(c->stream, c->ev_join, 0);
-    FinalizeArgs fa = fin_args(c, sys, 1, nvt);
+    FinalizeArgs fa = fin_args(c, sys, 1, 1);
     fa.noise = nullptr;
     fa.pile_g = pile_g ? 1 : 0;
     fa.pre_drawn = ahead ? 1 : 0;
@@ -761,6 +764,36 @@ qtg_status time_on_stream(qtg_ctx *ctx, int iters, F fn, double *ms_out) {
 }
 
 }  // namespace
+
+// Throughput of a dependent-FMA probe filling every SM (eight blocks of 256
+// threads an SM, eight chains a thread), after one short untimed launch.
+template <typename T, typename L>
+qtg_status fma_peak(double *tflops, int iters, L launch) {
+    if (!tflops) return QTG_ERR_ARG;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return QTG_ERR_NODEVICE;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return QTG_ERR_NODEVICE;
+    T *out = nullptr;
+    if (cudaMalloc(&out, sizeof(T)) != cudaSuccess) return QTG_ERR_CUDA;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = sms * 8;
+    launch(out, blocks, 256);
+    cudaEventRecord(e0, nullptr);
+    launch(out, blocks, iters);
+    cudaEventRecord(e1, nullptr);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (e != cudaSuccess || ms <= 0.f) return QTG_ERR_CUDA;
+    const double flops = 2.0 * 8.0 * (double)iters * blocks * 256.0;
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    return QTG_OK;
+}
 
 extern "C" {
 
@@ -2205,30 +2238,11 @@ qtg_status qtg_autotune(qtg_ctx *ctx, int iters, double *ms_heuristic, double *m
 }
 
 qtg_status qtg_fp32_peak(double *tflops) {
-    if (!tflops) return QTG_ERR_ARG;
-    int dev = 0, sms = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return QTG_ERR_NODEVICE;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return QTG_ERR_NODEVICE;
-    float *out = nullptr;
-    if (cudaMalloc(&out, sizeof(float)) != cudaSuccess) return QTG_ERR_CUDA;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    const int blocks = sms * 8, iters = 1 << 16;
-    launch_fp32_probe(out, blocks, 1024, nullptr);
-    cudaEventRecord(e0, nullptr);
-    launch_fp32_probe(out, blocks, iters, nullptr);
-    cudaEventRecord(e1, nullptr);
-    cudaError_t e = cudaEventSynchronize(e1);
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaFree(out);
-    if (e != cudaSuccess || ms <= 0.f) return QTG_ERR_CUDA;
-    const double flops = 2.0 * 8.0 * (double)iters * blocks * 256.0;
-    *tflops = flops / (ms * 1e-3) / 1e12;
-    return QTG_OK;
+    return fma_peak<float>(tflops, 1 << 16, [](float *o, int b, int it) { launch_fp32_probe(o, b, it, nullptr); });
+}
+
+qtg_status qtg_fp64_peak(double *tflops) {
+    return fma_peak<double>(tflops, 1 << 11, [](double *o, int b, int it) { launch_fp64_probe(o, b, it, nullptr); });
 }
 
 qtg_status qtg_reset_estimators(qtg_ctx *ctx) {

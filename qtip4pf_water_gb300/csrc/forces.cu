@@ -1921,6 +1921,22 @@ __global__ void __launch_bounds__(256) k_fp32_probe(float *out, int iters) {
     if (t == 12345.f) out[0] = t;  // keeps the chains live
 }
 
+// FP64 counterpart: eight independent dependent chains of double FMAs a thread.
+__global__ void __launch_bounds__(256) k_fp64_probe(double *out, int iters) {
+    double v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = 1.0 + 1e-15 * (threadIdx.x + k);
+    const double b = 0.9999999999999, c = 1e-15;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = fma(v[k], b, c);
+    }
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) t += v[k];
+    if (t == 12345.0) out[0] = t;  // keeps the chains live
+}
+
 template <typename R>
 size_t ksk_smem(int kmax) {
     return 2 * (CH * sizeof(V4<R>) + (size_t)3 * (kmax + 1) * (CH + 1) * sizeof(V2<R>));
@@ -2052,6 +2068,10 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
 
 void launch_fp32_probe(float *out, int blocks, int iters, cudaStream_t s) {
     k_fp32_probe<<<blocks, 256, 0, s>>>(out, iters);
+}
+
+void launch_fp64_probe(double *out, int blocks, int iters, cudaStream_t s) {
+    k_fp64_probe<<<blocks, 256, 0, s>>>(out, iters);
 }
 
 void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaStream_t s) {

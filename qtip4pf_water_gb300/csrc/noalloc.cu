@@ -5,20 +5,21 @@
 //
 // Who needs this: code that gets its GPU memory handed to it and must not call
 // cudaMalloc -- a molecular-dynamics engine or framework plugin that owns the
-// device memory budget and calls force routines with preallocated buffers,
-// work issued while another library is capturing a stream into a CUDA graph
-// (allocation is not allowed inside such a capture), and loops that cannot
-// afford allocator latency or fragmentation on every call. A qtg_ctx cannot
-// serve them: qtg_create allocates all of its memory up front.
+// device memory budget and calls force routines with preallocated buffers (an
+// allocation of its own would escape the engine's accounting, or fail under
+// the engine's memory cap), and loops that cannot afford allocator latency or
+// fragmentation on every call. A qtg_ctx cannot serve them: qtg_create
+// allocates all of its memory up front.
 //
 // Limits: at most QTG_NOALLOC_MAX_SITES charge sites and k_max <=
-// QTG_NOALLOC_MAX_KMAX; the array is 2.76 MiB (2,895,616 bytes) and every GPU that loads the
+// QTG_NOALLOC_MAX_KMAX; the array is 2.76 MiB (2,895,872 bytes) and every GPU that loads the
 // library holds it until the process exits.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "../../include/qtip4pf_gb300.h"
 #include "qtg_internal.h"
@@ -52,6 +53,7 @@ constexpr size_t NA_BYTES = OFF_STATUS + 256;
 // All scratch of qtg_kwald_noalloc. In host code this name is only a host-side
 // stand-in for the symbol: the device address comes from cudaGetSymbolAddress.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+static_assert(NA_BYTES == 2895872, "the scratch size stated in the header and comments is out of date");
 
 constexpr int NA_MAX_DEVICES = 64;
 unsigned char *g_scratch_ptr[NA_MAX_DEVICES] = {nullptr};
@@ -213,11 +215,15 @@ __global__ void __launch_bounds__(512) k_noalloc_setup(NAParams p, unsigned char
     }
 }
 
+std::mutex g_setup_mutex;
+
 // Once per device, with that device current: the device address of the
-// scratch array and the kernels' shared-memory limits.
+// scratch array and the kernels' shared-memory limits. The lock makes a first
+// call made by several host threads at once set the device up once.
 qtg_status scratch_for_current_device(unsigned char **out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) return QTG_ERR_NODEVICE;
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
     if (!g_scratch_ptr[dev]) {
         void *p = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return QTG_ERR_CUDA;
@@ -240,6 +246,9 @@ extern "C" qtg_status qtg_kwald_noalloc(const double *sites, const double *charg
     if (n_sites < 3 || n_sites % 3 != 0 || n_sites > NA_MAX_SITES) return QTG_ERR_ARG;
     if (!(box_bohr[0] > 0 && box_bohr[1] > 0 && box_bohr[2] > 0)) return QTG_ERR_ARG;
     if (!(eps_ewald > 0 && eps_ewald < 1)) return QTG_ERR_ARG;
+    // an error left pending by the caller's own CUDA work is theirs: report it
+    // without clearing it, and launch nothing
+    if (cudaPeekAtLastError() != cudaSuccess) return QTG_ERR_CUDA;
     // Ewald parameters exactly as forces.cpp:574-584 derives them
     NAParams p;
     memset(&p, 0, sizeof(p));

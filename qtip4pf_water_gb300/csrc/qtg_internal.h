@@ -529,6 +529,7 @@ void init_surrogate_kernel_attributes();
 // forces.cu: individual Ewald kernels (for timing)
 void launch_ewald_kernel(const EvalArgs &a, bool mixed, const char *name, cudaStream_t s);
 void launch_fp32_probe(float *out, int blocks, int iters, cudaStream_t s);
+void launch_fp64_probe(double *out, int blocks, int iters, cudaStream_t s);
 
 // forces.cu
 void launch_eval_fp64(const EvalArgs &a, cudaStream_t s, unsigned long long *launches);
