@@ -244,6 +244,11 @@ def run_gpu(args):
     # ---- end to end through the drop-in C-ABI call with pinned host buffers --------------
     e2e = run_e2e(q, st, min(args.steps, 200), flush)
 
+    try:
+        e2e_dropin = run_e2e_dropin(st)
+    except (subprocess.SubprocessError, OSError, ValueError, IndexError) as exc:
+        e2e_dropin = {"error": str(exc)[-300:]}
+
     # ---- roofline of the dominant kernel -----------------------------------------------------
     roof = roofline(q, st, mix, t64 / k2)
     line = {
@@ -265,6 +270,7 @@ def run_gpu(args):
         "estimators_finite": fin,
         "gpu_launches": launches,
         "e2e": e2e,
+        "e2e_dropin_sc": e2e_dropin,
         "roofline": roof["main"], "roofline_secondary": roof["secondary"], "kernel_ms": roof["kernel_ms"],
         "roofline_fp64_form": roof.get("fp64_form"), "fp64_peak_tflops": roof["fp64_peak_tflops"],
         "clocks": sampler.summary(),
@@ -334,6 +340,34 @@ def ring_fp64_flop(P, n_dof):
     else:
         tr = (P - 1) + (P + 1) * P
     return n_dof * (4 * tr + 26 * P)
+
+
+def run_e2e_dropin(st, warmup=5, steps=40):
+    """The drop-in as simulation.cpp drives it: update_sc_nospline on new[] arrays
+    with the caller's std::mt19937 (host draws included), mixed precision."""
+    import struct
+    import tempfile
+
+    from qtip4pf_water_gb300 import build as qb
+
+    qb.build()
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "start.bin")
+        with open(path, "wb") as f:
+            f.write(struct.pack("<2i", st.n_mols, st.n_beads))
+            f.write(struct.pack("<7d", *st.box_bohr, TEMP, DT_FS, 1e-6, 1e-5))
+            f.write(np.ascontiguousarray(st.q, dtype="<f8").tobytes())
+            f.write(np.ascontiguousarray(st.p, dtype="<f8").tobytes())
+        env = dict(os.environ, QTG_PRECISION="mixed")
+        out = subprocess.check_output([qb.DROPIN_BENCH, path, str(warmup), str(steps), str(SEED)], text=True,
+                                      env=env, timeout=600).split()
+    ms, draw_ms = float(out[0]), float(out[1])
+    return {"value": ns_per_day(ms * 1e-3), "unit": "ns/day", "ms_per_step": ms, "host_draw_ms_per_step": draw_ms,
+            "call": "update_sc_nospline through libqtip_compat.so (the reference's signature) from a C++ loop as "
+                    "simulation.cpp:936-961 runs it: new[] state arrays (registered with the library on the first "
+                    "call), PILE-G noise drawn on the host from the caller's std::mt19937 as thermostat.cpp draws it",
+            "workload": "512 H2O, P=32, Suzuki-Chin (the reference's PIMD step), mixed precision, 298 K, 0.25 fs",
+            "steps": steps, "warmup": warmup}
 
 
 def roofline(q, st, mix, t64_step=None):

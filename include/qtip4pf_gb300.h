@@ -242,6 +242,50 @@ qtg_status qtg_fp32_peak(double *tflops);
  * FP64 normal-mode / integrator kernels). */
 qtg_status qtg_fp64_peak(double *tflops);
 
+/* ---- host-side helpers of the drop-in --------------------------------------- */
+/* The qTIP4P/F constants in atomic units, derived as qtip4pfparams.h:41-133
+ * derives them (same values, same operation order): for host code that has to
+ * agree with the library to the last bit (the drop-in's per-pair helpers). */
+typedef struct qtg_constants {
+    double angs2bohr, fs2au, K2au, mo, mh, qo, qh, gamma_vs;
+    double epslj, sigmalj6, sigmalj12, e_cut, r_cut, r_skin;
+    double roheq, ar2, ar3, ar4fac, Dr, theta_eq, ktheta, pi;
+} qtg_constants;
+qtg_status qtg_get_constants(qtg_constants *out);
+/* Page-locks and maps a caller's host array (cudaHostRegister, portable and
+ * mapped) so that per-call steps move it inside their graph instead of by copy
+ * calls; an array already registered is accepted as it is. The caller keeps the
+ * memory registered until qtg_unregister_host or process exit. No counterpart
+ * in the reference (its arrays are plain new[] memory). */
+qtg_status qtg_register_host(void *ptr, size_t bytes);
+qtg_status qtg_unregister_host(void *ptr);
+
+/* ---- tabulated pair corrections ("fast-CMD" splines) ------------------------ */
+/* Replaces the spline part of get_forces_wspline / force_eval_sc_wspline
+ * (forces.cpp:452-466, :634-691, :791-882): every atom pair of a configuration
+ * whose minimum-image separation r has r^2 < cut_sq for its type adds s(r) to
+ * the energy and -s'(r) r_ij / r to atom i (+ to atom j). s is the clamped
+ * uniform cubic B-spline interpolant of values[0 .. n-1] on the knots
+ * start + i step (the construction of boost::math::cubic_b_spline, which the
+ * reference builds from oo/oh/hh_spline.txt with start 0 and step 0.01 bohr,
+ * simulation.cpp:36-116); an end slope given as NaN is estimated by five-point
+ * one-sided differences. Units: bohr and Hartree. */
+typedef struct qtg_pair_spline {
+    const double *values; /* host, n >= 5 values at the knots */
+    int n;
+    double start, step;   /* first knot and spacing (bohr) */
+    double left_deriv, right_deriv; /* end slopes (Hartree / bohr), NaN: estimated */
+    double cut_sq;        /* pairs with r^2 < cut_sq; at most (start + step (n-1))^2 */
+} qtg_pair_spline;
+/* Attaches (any table non-NULL) or removes (all NULL) the tables of one
+ * system; a NULL type adds nothing. Every later force evaluation of the system
+ * -- tier-1 entries, per-call steps, the device stepper, the Suzuki-Chin
+ * displaced evaluations -- includes them (the reference's *_wspline
+ * functions). Allocates the tables; qtg_init_forces must precede the next
+ * qtg_run_steps. */
+qtg_status qtg_set_pair_splines(qtg_ctx *ctx, int sys, const qtg_pair_spline *oo, const qtg_pair_spline *oh,
+                                const qtg_pair_spline *hh);
+
 /* ---- centroid-constrained PIMD (no reference counterpart) ------------------- */
 /* With the centroid fixed, the device stepper holds each atom's bead centroid
  * where it is (the centroid normal mode carries no momentum and is not

@@ -32,7 +32,17 @@ class QoSys(C.Structure):
         ("r_cut", C.c_double), ("r_cut_sq", C.c_double), ("r_skin", C.c_double), ("r_skin_sq", C.c_double),
         ("mo", C.c_double), ("mh", C.c_double), ("qo", C.c_double), ("qh", C.c_double),
         ("gamma_m", C.c_double),
+        ("spl", C.c_void_p),
     ]
+
+
+class QoSpline(C.Structure):
+    _fields_ = [("n", C.c_int), ("start", C.c_double), ("step", C.c_double), ("cut_sq", C.c_double),
+                ("c", C.POINTER(C.c_double))]
+
+
+class QoSplines(C.Structure):
+    _fields_ = [("t", QoSpline * 3)]
 
 
 class QoStepper(C.Structure):
@@ -90,6 +100,11 @@ def lib():
         L.qo_stepper_centroid_draw.restype = C.c_int
         L.qo_stepper_step.argtypes = [S, C.POINTER(QoStepper), D, D, D, D, D, D, I, I, D, C.c_int, D, D]
         L.qo_stepper_step.restype = C.c_double
+        L.qo_spline_build.argtypes = [D, C.c_int, C.c_double, C.c_double, C.c_double, D]
+        L.qo_spline_build.restype = C.c_int
+        L.qo_spline_eval.argtypes = [D, C.c_int, C.c_double, C.c_double, C.c_double, D]
+        L.qo_spline_eval.restype = C.c_double
+        L.qo_set_splines.argtypes = [S, C.POINTER(QoSplines)]
         L.qo_count_kvectors.argtypes = [S]
         L.qo_count_kvectors.restype = C.c_int
         _lib = L
@@ -103,6 +118,23 @@ def philox4x32_10(ctr, key):
     o = (C.c_uint * 4)()
     L.qo_philox4x32_10(c, int(key[0]) & 0xFFFFFFFF, int(key[1]) & 0xFFFFFFFF, o)
     return [int(x) for x in o]
+
+
+def spline_eval(c, n, start, step, x):
+    """Value and derivative of the oracle's spline with coefficients c at x."""
+    L = lib()
+    d = C.c_double(0.0)
+    c = np.ascontiguousarray(c, dtype=np.float64)
+    v = L.qo_spline_eval(_d(c), int(n), float(start), float(step), float(x), C.byref(d))
+    return v, d.value
+
+
+def spline_coefficients(y, step, dl=float("nan"), dr=float("nan")):
+    L = lib()
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    c = np.zeros(len(y) + 2)
+    assert L.qo_spline_build(_d(y), len(y), float(step), float(dl), float(dr), _d(c)) == 1
+    return c
 
 
 def _d(a):
@@ -208,6 +240,28 @@ class Oracle:
                                    _d(self.charge), _i(point), _i(lst), _d(disp), 1 if is_nvt else 0,
                                    None if cf_acc is None else _d(cf_acc), C.byref(pot))
         return e, pot.value
+
+    def set_splines(self, tables, start=0.0, step=0.01):
+        """Attach pair tables {"oo"|"oh"|"hh": values on start + i step}, cutoff at the
+        last knot (simulation.cpp:59-60), end slopes estimated; None removes them."""
+        if tables is None:
+            self.L.qo_set_splines(C.byref(self.s), None)
+            self._spl = None
+            return
+        spl = QoSplines()
+        keep = []
+        for t, key in enumerate(("oo", "oh", "hh")):
+            y = tables.get(key)
+            if y is None:
+                continue
+            y = np.ascontiguousarray(y, dtype=np.float64)
+            c = np.zeros(len(y) + 2)
+            assert self.L.qo_spline_build(_d(y), len(y), step, float("nan"), float("nan"), _d(c)) == 1
+            end = start + step * (len(y) - 1)
+            spl.t[t] = QoSpline(len(y), start, step, end * end, _d(c))
+            keep.append(c)
+        self._spl = (spl, keep)
+        self.L.qo_set_splines(C.byref(self.s), C.byref(spl))
 
     def count_kvectors(self):
         return self.L.qo_count_kvectors(C.byref(self.s))

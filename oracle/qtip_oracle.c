@@ -371,6 +371,106 @@ double qo_kwald(const qo_sys *s, const double *sites_all, double *f_all, const d
 }
 
 /* ---- one configuration: forces.cpp:468-630 -------------------------------- */
+/* ---- tabulated pair corrections: forces.cpp:452-466, :634-691 ---------------
+ * The reference's spline is boost::math::cubic_b_spline (not installed here):
+ * restated as the clamped uniform cubic B-spline interpolant that type
+ * documents. s(x) = sum_{j=-1}^{n} c_j B(t - j), t = (x - start)/step, B the
+ * centred cubic B-spline; (c_{i-1} + 4 c_i + c_{i+1})/6 = y_i at the knots and
+ * (c_1 - c_{-1})/(2 step), (c_n - c_{n-2})/(2 step) the end slopes. */
+int qo_spline_build(const double *y, int n, double step, double dl, double dr, double *c) {
+    if (n < 5 || !(step > 0)) return 0;
+    if (isnan(dl)) dl = (-25.0 * y[0] + 48.0 * y[1] - 36.0 * y[2] + 16.0 * y[3] - 3.0 * y[4]) / (12.0 * step);
+    if (isnan(dr))
+        dr = (25.0 * y[n - 1] - 48.0 * y[n - 2] + 36.0 * y[n - 3] - 16.0 * y[n - 4] + 3.0 * y[n - 5]) / (12.0 * step);
+    /* tridiagonal system for x_i = c_i, i = 0..n-1: rows 1..n-2 are (1, 4, 1) = 6 y_i,
+     * row 0 is 4 x_0 + 2 x_1 = 6 y_0 + 2 step dl, row n-1 is 2 x_{n-2} + 4 x_{n-1} =
+     * 6 y_{n-1} - 2 step dr; forward elimination into (d, r), back substitution */
+    double *d = (double *)malloc(sizeof(double) * (size_t)n);
+    double *r = (double *)malloc(sizeof(double) * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const double lo = i == 0 ? 0.0 : (i == n - 1 ? 2.0 : 1.0);
+        const double up_prev = i == 1 ? 2.0 : 1.0;
+        double rhs = 6.0 * y[i];
+        if (i == 0) rhs += 2.0 * step * dl;
+        if (i == n - 1) rhs -= 2.0 * step * dr;
+        if (i == 0) {
+            d[0] = 4.0;
+            r[0] = rhs;
+        } else {
+            const double w = lo / d[i - 1];
+            d[i] = 4.0 - w * up_prev;
+            r[i] = rhs - w * r[i - 1];
+        }
+    }
+    double *x = c + 1;
+    x[n - 1] = r[n - 1] / d[n - 1];
+    for (int i = n - 2; i >= 0; --i) x[i] = (r[i] - (i == 0 ? 2.0 : 1.0) * x[i + 1]) / d[i];
+    c[0] = x[1] - 2.0 * step * dl;
+    c[n + 1] = x[n - 2] + 2.0 * step * dr;
+    free(d);
+    free(r);
+    return 1;
+}
+
+/* the centred cubic B-spline */
+static double bspl3(double t) {
+    t = fabs(t);
+    if (t >= 2.0) return 0.0;
+    if (t >= 1.0) return (2.0 - t) * (2.0 - t) * (2.0 - t) / 6.0;
+    return (4.0 - 6.0 * t * t + 3.0 * t * t * t) / 6.0;
+}
+static double bspl3_prime(double t) {
+    const double a = fabs(t), sg = t < 0.0 ? -1.0 : 1.0;
+    if (a >= 2.0) return 0.0;
+    if (a >= 1.0) return -0.5 * sg * (2.0 - a) * (2.0 - a);
+    return sg * (-2.0 * a + 1.5 * a * a);
+}
+
+double qo_spline_eval(const double *c, int n, double start, double step, double x, double *deriv) {
+    const double t = (x - start) / step;
+    int i0 = (int)floor(t);
+    if (i0 < 0) i0 = 0;
+    if (i0 > n - 2) i0 = n - 2;
+    double v = 0.0, dv = 0.0;
+    for (int j = i0 - 1; j <= i0 + 2; ++j) {
+        v += c[j + 1] * bspl3(t - j);
+        dv += c[j + 1] * bspl3_prime(t - j);
+    }
+    if (deriv) *deriv = dv / step;
+    return v;
+}
+
+void qo_set_splines(qo_sys *s, const qo_splines *spl) { s->spl = spl; }
+
+/* get_forces_wspline's pair loop (forces.cpp:644-688): every atom pair i < j,
+ * minimum image, the type's spline inside its cutoff, get_spline's force
+ * (forces.cpp:454-463: F_i -= s'(r)/r r_ij, F_j += s'(r)/r r_ij) */
+static double spline_pairs(const qo_sys *s, const double *q, double *f) {
+    const int na = s->n_atoms;
+    double energy = 0.0;
+    for (int i = 0; i < na; ++i)
+        for (int j = i + 1; j < na; ++j) {
+            double r[3];
+            for (int d = 0; d < 3; ++d) {
+                r[d] = q[3 * i + d] - q[3 * j + d];
+                r[d] -= s->box[d] * round(r[d] / s->box[d]);
+            }
+            const double rsq = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+            const int t = (i % 3 == 0 ? 0 : 1) + (j % 3 == 0 ? 0 : 1);
+            const qo_spline *sp = &s->spl->t[t];
+            if (!sp->c || !(rsq < sp->cut_sq)) continue;
+            const double rij = sqrt(rsq);
+            double dv;
+            energy += qo_spline_eval(sp->c, sp->n, sp->start, sp->step, rij, &dv);
+            const double fp = dv / rij;
+            for (int d = 0; d < 3; ++d) {
+                f[3 * i + d] -= fp * r[d];
+                f[3 * j + d] += fp * r[d];
+            }
+        }
+    return energy;
+}
+
 double qo_get_forces(const qo_sys *s, const double *pos, double *f_all, const double *charge,
                      const int *point, const int *list, int bead) {
     const int N = s->n_mols, ns = s->n_atoms, nd = s->n_dof;
@@ -434,6 +534,7 @@ double qo_get_forces(const qo_sys *s, const double *pos, double *f_all, const do
     for (int i = 0; i < ns; ++i) energy -= 0.5 * s->ewald_pref * charge[i] * charge[i];
     free(site);
     free(fs);
+    if (s->spl) energy += spline_pairs(s, q, f);
     return energy;
 }
 

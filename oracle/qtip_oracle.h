@@ -28,7 +28,27 @@ typedef struct qo_sys {
     double acc, kappa, rc_sq, kc_sq, k_pref, ewald_pref;
     double r_cut, r_cut_sq, r_skin, r_skin_sq;
     double mo, mh, qo, qh, gamma_m;
+    const struct qo_splines *spl; /* tabulated pair corrections, or NULL (qo_set_splines) */
 } qo_sys;
+
+/* ---- tabulated pair corrections (forces.cpp:452-466, :634-691) ----------------
+ * A clamped uniform cubic B-spline per pair type: c holds c_{-1} .. c_n
+ * (n + 2 values) for knots start + i step; pairs with r^2 < cut_sq. */
+typedef struct qo_spline {
+    int n;
+    double start, step, cut_sq;
+    const double *c;
+} qo_spline;
+typedef struct qo_splines {
+    qo_spline t[3]; /* O-O, O-H, H-H */
+} qo_splines;
+/* coefficients of the interpolant of y_0 .. y_{n-1} with end slopes dl, dr (NaN:
+ * five-point one-sided estimates); returns 0 on bad input */
+int qo_spline_build(const double *y, int n, double step, double dl, double dr, double *c);
+/* value at x (and the derivative into *deriv when not NULL) */
+double qo_spline_eval(const double *c, int n, double start, double step, double x, double *deriv);
+/* attach (NULL: remove) the tables used by every force evaluation of s */
+void qo_set_splines(qo_sys *s, const qo_splines *spl);
 
 /* derived parameters: water.cpp:76-157 and forces.cpp:574-584 */
 void qo_init(qo_sys *s, int n_mols, int n_beads, const double box_bohr[3], double temp_K,

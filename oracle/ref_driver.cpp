@@ -218,4 +218,49 @@ double ref_bussi(double *p, unsigned seed, double *noise) {
     return heat;
 }
 
+// ---- the spline ("fast-CMD") path: forces.cpp:634-691, :791-882; update.cpp
+// :16-75, :139-269. Tables as simulation.cpp:36-116 builds them: values on the
+// knots 0, 0.01, ... bohr, cutoff^2 = (0.01 (n - 1))^2, end slopes estimated.
+static boost::math::cubic_b_spline<double> g_spl[3];
+static double g_spl_cutsq[3];
+
+void ref_set_splines(const double *oo, int n_oo, const double *oh, int n_oh, const double *hh, int n_hh) {
+    const double *v[3] = {oo, oh, hh};
+    const int n[3] = {n_oo, n_oh, n_hh};
+    for (int t = 0; t < 3; ++t) {
+        g_spl[t] = boost::math::cubic_b_spline<double>(v[t], v[t] + n[t], 0.0, 0.01);
+        const double cut = 0.0 + 0.01 * (n[t] - 1);
+        g_spl_cutsq[t] = cut * cut;
+    }
+}
+
+double ref_get_forces_wspline(const double *pos, double *f, const int *point, const int *list, int bead) {
+    return get_forces_wspline(pos, f, g_charge.data(), point, list, g_spl[0], g_spl[1], g_spl[2], g_spl_cutsq[0],
+                              g_spl_cutsq[1], g_spl_cutsq[2], bead);
+}
+
+double ref_force_eval_sc_wspline(const double *pos, double *f, const int *point, const int *list, double *sc_pot,
+                                 double *fphys) {
+    double scp = 0.0;
+    double e = force_eval_sc_wspline(pos, f, g_charge.data(), g_mass.data(), point, list, g_spl[0], g_spl[1],
+                                     g_spl[2], g_spl_cutsq[0], g_spl_cutsq[1], g_spl_cutsq[2], scp, fphys);
+    *sc_pot = scp;
+    return e;
+}
+
+double ref_update_class_wspline(double *q, double *p, double *f, int *point, int *list, double *disp) {
+    return update_trajectory_class_wspline(q, p, g_mass.data(), f, g_charge.data(), point, list, disp, g_spl[0],
+                                           g_spl[1], g_spl[2], g_spl_cutsq[0], g_spl_cutsq[1], g_spl_cutsq[2]);
+}
+
+double ref_update_sc_wspline(double *q, double *p, double *f, double *fphys, int *point, int *list, double *disp,
+                             double *sc_pot) {
+    std::mt19937 rng(1);
+    double h = 0.0, scp = 0.0;
+    double e = update_sc_wspline(q, p, g_mass.data(), f, fphys, g_charge.data(), point, list, disp, rng, false, h,
+                                 scp, g_spl[0], g_spl[1], g_spl[2], g_spl_cutsq[0], g_spl_cutsq[1], g_spl_cutsq[2]);
+    *sc_pot = scp;
+    return e;
+}
+
 }  // extern "C"

@@ -57,6 +57,12 @@ I = C.POINTER(C.c_int)
 V = C.c_void_p
 
 
+class PairSpline(C.Structure):
+    """qtg_pair_spline: one pair type's table (values on start + i step)."""
+    _fields_ = [("values", D), ("n", C.c_int), ("start", C.c_double), ("step", C.c_double),
+                ("left_deriv", C.c_double), ("right_deriv", C.c_double), ("cut_sq", C.c_double)]
+
+
 class MlpWeights(C.Structure):
     """qtg_mlp_weights: device pointers of the BF16 weights and FP32 biases."""
     _fields_ = [("w1", V), ("w2", V), ("w3", V), ("b1", V), ("b2", V), ("b3", V)]
@@ -118,6 +124,8 @@ def load(build_if_missing: bool = True):
         "qtg_adam_step": ([V, V, V, V, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, V, C.c_int, V],
                           C.c_int),
         "qtg_set_centroid_fixed": ([V, C.c_int, C.c_int], C.c_int),
+        "qtg_set_pair_splines": ([V, C.c_int, C.POINTER(PairSpline), C.POINTER(PairSpline),
+                                  C.POINTER(PairSpline)], C.c_int),
         "qtg_reset_centroid_force": ([V, C.c_int], C.c_int),
         "qtg_get_centroid_force": ([V, C.c_int, D, D], C.c_int),
         "qtg_set_tuning": ([V, C.c_int, C.c_int, C.c_int], C.c_int),
@@ -443,6 +451,21 @@ class System:
         disp = np.zeros(self.P * 3 * self.N)
         self._c(self.ctx.L.qtg_get_state(self.ctx.h, self.idx, _d(q), _d(p), _d(f), _d(fp), _d(disp)))
         return dict(q=q, p=p, f=f, fphys=fp, disp=disp)
+
+    def set_pair_splines(self, oo=None, oh=None, hh=None, start=0.0, step=0.01):
+        """Attach tabulated pair corrections (the reference's *_wspline force path):
+        values on the knots start + i step (bohr, Hartree), cutoff at the last knot
+        (simulation.cpp:59-60), end slopes estimated. All None removes them."""
+        keep, args = [], []
+        for y in (oo, oh, hh):
+            if y is None:
+                args.append(None)
+                continue
+            y = np.ascontiguousarray(y, dtype=np.float64)
+            keep.append(y)
+            end = start + step * (len(y) - 1)
+            args.append(C.byref(PairSpline(_d(y), len(y), start, step, float("nan"), float("nan"), end * end)))
+        self._c(self.ctx.L.qtg_set_pair_splines(self.ctx.h, self.idx, *args))
 
     def set_centroid_fixed(self, fixed=True):
         """Centroid-constrained PIMD: hold the bead centroid fixed (Trotter systems)."""

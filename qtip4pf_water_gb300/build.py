@@ -23,7 +23,11 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libqtipgpu.so")
 COMPAT = os.path.join(BUILD, "libqtip_compat.so")
+DROPIN_BENCH = os.path.join(BUILD, "dropin_bench")
 INCLUDE = os.path.join(ROOT, "include")
+# boost::math::cubic_b_spline for drop-in builds without Boost (the reference's
+# spline signatures name that type)
+COMPAT_INCLUDE = os.path.join(CSRC, "compat", "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no floating-point contraction, so the host-side parameter derivations
@@ -84,10 +88,19 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if force or jobs or _stale(LIB, objs):
         _run([nv] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs, verbose)
     compat_src = os.path.join(CSRC, "compat", "compat.cpp")
-    if os.path.exists(compat_src) and (force or _stale(COMPAT, [compat_src, LIB] + hdrs)):
+    compat_hdrs = glob.glob(os.path.join(COMPAT_INCLUDE, "**", "*.hpp"), recursive=True)
+    if os.path.exists(compat_src) and (force or _stale(COMPAT, [compat_src, LIB] + hdrs + compat_hdrs)):
         cxx = shutil.which("g++") or "g++"
-        _run([cxx, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-shared", "-I", INCLUDE, compat_src, "-o", COMPAT,
+        # an installed Boost.Math takes precedence over the stand-in spline header
+        _run([cxx, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-shared", "-I", INCLUDE,
+              "-idirafter", COMPAT_INCLUDE, compat_src, "-o", COMPAT,
               "-L", BUILD, "-lqtipgpu", "-Wl,-rpath,$ORIGIN"], verbose)
+    # the drop-in's end-to-end timing driver (simulation.cpp's sampling loop)
+    bench_src = os.path.join(CSRC, "compat", "dropin_bench.cpp")
+    if os.path.exists(bench_src) and (force or _stale(DROPIN_BENCH, [bench_src, COMPAT])):
+        cxx = shutil.which("g++") or "g++"
+        _run([cxx, "-O2", "-std=c++17", bench_src, "-o", DROPIN_BENCH, "-L", BUILD, "-lqtip_compat", "-lqtipgpu",
+              "-Wl,-rpath,$ORIGIN"], verbose)
     return LIB
 
 

@@ -305,6 +305,13 @@ struct qtg_ctx {
         float4 *wrapped = nullptr;
     };
     std::vector<Surrogate> surrogates;
+    // tabulated pair corrections: per-system tables (device), their coefficients,
+    // the host copy of both, and whether any system carries one
+    PairSplines *spl = nullptr;
+    double *spl_coef = nullptr;
+    std::vector<PairSplines> spl_h;
+    std::vector<std::vector<double>> spl_coef_h;  // per system: the three types' coefficients back to back
+    bool spl_any = false;
     int n_sm = 148;
     unsigned long long h2d_bytes = 0, d2h_bytes = 0;  // host <-> device traffic of the per-call entries
     // per-call ring-polymer steps captured as graphs, by (system, NVT, caller noise): graph, kernels in it
@@ -396,9 +403,27 @@ EvalArgs aux_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, do
     return a;
 }
 
+// A force evaluation; with tabulated pair corrections attached, their forces and
+// energies are added to the evaluation's output afterwards (forces and
+// short-range finite-difference evaluations alike; not to the Ewald-derivative
+// jobs of mode 1, nor to reciprocal-space-only calls).
 void launch_eval(qtg_ctx *c, const EvalArgs &a) {
     if (c->mixed) launch_eval_mixed(a, c->stream, &c->launches, &c->forks);
     else launch_eval_fp64(a, c->stream, &c->launches);
+    if (c->spl_any && a.mode == 0 && !a.sites_are_input) {
+        SplineArgs s;
+        s.sys = c->sys_d;
+        s.jobs = a.jobs;
+        s.n_jobs = a.n_jobs;
+        s.max_mols = a.max_mols;
+        s.pos = a.pos;
+        s.out = a.out;
+        s.out_prop = a.out_prop;
+        s.energy = a.energy;
+        s.tables = c->spl;
+        s.coef = c->spl_coef;
+        launch_pair_splines(s, c->mixed, c->stream, &c->launches);
+    }
 }
 
 RingArgs ring_args(qtg_ctx *c, int sys, int flags) {
@@ -1322,6 +1347,8 @@ void qtg_destroy(qtg_ctx *ctx) {
         if (p) cudaFree(p);
     if (ctx->box) cudaFreeHost(ctx->box);
     for (auto &g : ctx->surrogates) free_surrogate(g);
+    if (ctx->spl) cudaFree(ctx->spl);
+    if (ctx->spl_coef) cudaFree(ctx->spl_coef);
     for (auto &g : ctx->call_graphs) cudaGraphExecDestroy(g.second.first);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
@@ -1396,6 +1423,113 @@ qtg_status qtg_get_centroid_force(qtg_ctx *ctx, int sys, double *f_mean, double 
     CK(cudaMemcpy(&ns, &ctx->run[sys].cf_samples, sizeof(double), cudaMemcpyDeviceToHost));
     for (int i = 0; i < S.n_dof; ++i) f_mean[i] = ns > 0.0 ? acc[i] / ns : 0.0;
     *n_samples = ns;
+    return QTG_OK;
+}
+
+qtg_status qtg_get_constants(qtg_constants *out) {
+    if (!out) return QTG_ERR_ARG;
+    const Consts K = make_consts();
+    out->angs2bohr = K.angs2bohr;
+    out->fs2au = K.fs2au;
+    out->K2au = K.K2au;
+    out->mo = K.mo;
+    out->mh = K.mh;
+    out->qo = K.qo;
+    out->qh = K.qh;
+    out->gamma_vs = K.gamma_vs;
+    out->epslj = K.epslj;
+    out->sigmalj6 = K.sigmalj6;
+    out->sigmalj12 = K.sigmalj12;
+    out->e_cut = K.e_cut;
+    out->r_cut = K.r_cut;
+    out->r_skin = K.r_skin;
+    out->roheq = K.roheq;
+    out->ar2 = K.ar2;
+    out->ar3 = K.ar3;
+    out->ar4fac = K.ar4fac;
+    out->Dr = K.Dr;
+    out->theta_eq = K.theta_eq;
+    out->ktheta = K.ktheta;
+    out->pi = PI_REF;
+    return QTG_OK;
+}
+
+qtg_status qtg_register_host(void *ptr, size_t bytes) {
+    if (!ptr || bytes == 0) return QTG_ERR_ARG;
+    const cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterPortable | cudaHostRegisterMapped);
+    if (e == cudaErrorHostMemoryAlreadyRegistered) {
+        cudaGetLastError();
+        return QTG_OK;
+    }
+    return e == cudaSuccess ? QTG_OK : QTG_ERR_CUDA;
+}
+
+qtg_status qtg_unregister_host(void *ptr) {
+    if (!ptr) return QTG_ERR_ARG;
+    const cudaError_t e = cudaHostUnregister(ptr);
+    if (e == cudaErrorHostMemoryNotRegistered) {
+        cudaGetLastError();
+        return QTG_OK;
+    }
+    return e == cudaSuccess ? QTG_OK : QTG_ERR_CUDA;
+}
+
+qtg_status qtg_set_pair_splines(qtg_ctx *ctx, int sys, const qtg_pair_spline *oo, const qtg_pair_spline *oh,
+                                const qtg_pair_spline *hh) {
+    CKS(check_sys(ctx, sys));
+    const qtg_pair_spline *in[3] = {oo, oh, hh};
+    const bool on = oo || oh || hh;
+    PairSplines T;
+    memset(&T, 0, sizeof(T));
+    std::vector<double> coef;
+    for (int t = 0; t < 3; ++t) {
+        if (!in[t]) continue;
+        const qtg_pair_spline &p = *in[t];
+        if (!p.values || p.n < 5 || !(p.step > 0) || !(p.cut_sq >= 0) || !std::isfinite(p.start))
+            return fail(ctx, QTG_ERR_ARG, "pair spline: need >= 5 values, a positive step, a cutoff");
+        // a pair inside the cutoff must lie on the table (as the reference's
+        // cutoffs do: cut = start + step (n - 1))
+        const double end = p.start + p.step * (p.n - 1);
+        if (p.cut_sq > end * end * (1.0 + 1e-12))
+            return fail(ctx, QTG_ERR_ARG, "pair spline: cutoff beyond the last knot");
+        const size_t off = coef.size();
+        coef.resize(off + (size_t)p.n + 2);
+        if (!bspline_coefficients(p.values, p.n, p.step, p.left_deriv, p.right_deriv, coef.data() + off))
+            return fail(ctx, QTG_ERR_ARG, "pair spline: coefficient solve failed");
+        T.t[t].coef_off = (long long)off;  // relative to the system's block, rebased below
+        T.t[t].n = p.n;
+        T.t[t].start = p.start;
+        T.t[t].inv_step = 1.0 / p.step;
+        T.t[t].cut_sq = p.cut_sq;
+    }
+    T.on = on ? 1 : 0;
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->spl_h.empty()) {
+        ctx->spl_h.assign(ctx->n_sys, PairSplines{});
+        ctx->spl_coef_h.assign(ctx->n_sys, {});
+    }
+    ctx->spl_h[sys] = T;
+    ctx->spl_coef_h[sys] = coef;
+    // all systems' tables back to back, offsets rebased
+    std::vector<PairSplines> all = ctx->spl_h;
+    std::vector<double> cf;
+    bool any = false;
+    for (int k = 0; k < ctx->n_sys; ++k) {
+        for (int t = 0; t < 3; ++t) all[k].t[t].coef_off += (long long)cf.size();
+        cf.insert(cf.end(), ctx->spl_coef_h[k].begin(), ctx->spl_coef_h[k].end());
+        any = any || all[k].on;
+    }
+    if (ctx->spl) cudaFree(ctx->spl);
+    if (ctx->spl_coef) cudaFree(ctx->spl_coef);
+    ctx->spl = nullptr;
+    ctx->spl_coef = nullptr;
+    CK(cudaMalloc(&ctx->spl, sizeof(PairSplines) * ctx->n_sys));
+    CK(cudaMalloc(&ctx->spl_coef, sizeof(double) * std::max<size_t>(cf.size(), 1)));
+    CK(cudaMemcpy(ctx->spl, all.data(), sizeof(PairSplines) * ctx->n_sys, cudaMemcpyHostToDevice));
+    if (!cf.empty()) CK(cudaMemcpy(ctx->spl_coef, cf.data(), sizeof(double) * cf.size(), cudaMemcpyHostToDevice));
+    ctx->spl_any = any;
+    drop_graphs(ctx);
+    ctx->forces_ready = false;
     return QTG_OK;
 }
 

@@ -506,6 +506,31 @@ struct EvalArgs {
     Consts c;
 };
 
+// splines.cu: tabulated pair corrections (forces.cpp:452-466, :634-691). One
+// table per pair type: coefficients c_{-1} .. c_n at coef[coef_off ..], knots
+// start + i / inv_step, pairs with r^2 < cut_sq.
+struct SplineType {
+    long long coef_off;
+    int n, pad;
+    double start, inv_step, cut_sq;
+};
+struct PairSplines {
+    SplineType t[3];  // O-O, O-H, H-H
+    int on, pad;
+};
+struct SplineArgs {
+    const SysDev *sys;
+    const Job *jobs;
+    int n_jobs, max_mols;
+    const double *pos;          // position base (jobs' pos_off)
+    double *out, *out_prop;     // force bases the spline forces are added to (out_prop optional)
+    double *energy;             // per slot
+    const PairSplines *tables;  // per system
+    const double *coef;
+};
+void launch_pair_splines(const SplineArgs &a, bool mixed, cudaStream_t s, unsigned long long *launches);
+bool bspline_coefficients(const double *y, int n, double h, double dl, double dr, double *c);
+
 // surrogate.cu: the learned centroid correction of one P = 1 system, added to
 // its forces inside a force evaluation (descriptors, features, tensor-core
 // forward pass, frames, lab-frame correction)

@@ -6,15 +6,23 @@
 // the reference's own sources (to record the expected output) or against
 // libqtip_compat.so (the GPU drop-in), and prints one line per step.
 //
-// usage: dropin_driver <start.bin> <n_steps> <seed>
+// With a fourth argument "spline" it runs the spline ("fast-CMD") path instead:
+// force_eval_sc_wspline and update_sc_wspline with three synthetic pair tables
+// y(r) = A exp(-r / lam) (1 - (r / r_end)^2)^2 on the reference's grid (knots
+// 0, 0.01, ... bohr; simulation.cpp:36-116), built as boost::math::cubic_b_spline.
+//
+// usage: dropin_driver <start.bin> <n_steps> <seed> [spline]
 // start.bin: int32 n_mols, int32 n_beads, double box[3], double T_K, double dt_fs,
 //            double eps_ewald, double eps_sc, then q[P][9N], p[P][9N] (doubles)
 #include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <random>
 #include <vector>
+
+#include <boost/math/interpolators/cubic_b_spline.hpp>
 
 // the reference's configuration globals (declared extern in qtip4pfparams.h)
 double T_K, epsilonsc, rho_inp, dtfs, eps, a_cell_angs, a_cell, b_cell, c_cell, rnn;
@@ -36,6 +44,16 @@ double update_sc_nospline(double position_array[], double momentum_array[], cons
                           double force_array[], double fphys[], double charge_array[], int point[], int list[],
                           double disp_array[], std::mt19937 &rng, bool is_nvt, double &heat, double &sc_pot);
 double get_kcv(const double position_array[], const double force_array[]);
+using spline_t = boost::math::cubic_b_spline<double>;
+double force_eval_sc_wspline(const double position_array[], double force_array[], const double charge_array[],
+                             const double mass_array[], const int point[], const int list[], const spline_t &oo,
+                             const spline_t &oh, const spline_t &hh, const double oo_cutsq, const double oh_cutsq,
+                             const double hh_cutsq, double &sc_pot, double fphys[]);
+double update_sc_wspline(double position_array[], double momentum_array[], const double mass_array[],
+                         double force_array[], double fphys[], double charge_array[], int point[], int list[],
+                         double disp_array[], std::mt19937 &rng, bool is_nvt, double &heat, double &sc_pot,
+                         const spline_t &oo, const spline_t &oh, const spline_t &hh, const double oo_cutsq,
+                         const double oh_cutsq, const double hh_cutsq);
 double get_conserved(double position_array[], double momentum_array[], const double mass_array[], double energy);
 
 int main(int argc, char **argv) {
@@ -99,15 +117,37 @@ int main(int argc, char **argv) {
         }
     }
     for (int b = 0; b < n_beads; ++b) neighbour_list(q.data(), point.data(), list.data(), disp.data(), b);
+    const bool spline = argc > 4 && std::strcmp(argv[4], "spline") == 0;
+    const double tabs[3][3] = {{5e-3, 1.2, 7.0}, {-3e-3, 1.0, 5.5}, {2e-3, 0.8, 4.5}};  // A, lam, r_end
+    std::vector<spline_t> spl;
+    double cutsq[3];
+    for (int t = 0; t < 3; ++t) {
+        const int n = (int)std::lround(tabs[t][2] / 0.01) + 1;
+        std::vector<double> y(n);
+        for (int i = 0; i < n; ++i) {
+            const double r = 0.01 * i, x = r / tabs[t][2];
+            y[i] = tabs[t][0] * std::exp(-r / tabs[t][1]) * (1.0 - x * x) * (1.0 - x * x);
+        }
+        spl.emplace_back(y.begin(), y.end(), 0.0, 0.01);
+        cutsq[t] = (0.01 * (n - 1)) * (0.01 * (n - 1));  // simulation.cpp:59-60
+    }
     double sc_pot = 0.0, heat = 0.0;
-    double e = force_eval_sc_nospline(q.data(), f.data(), charge.data(), mass.data(), point.data(), list.data(),
-                                      sc_pot, fphys.data());
+    double e = spline ? force_eval_sc_wspline(q.data(), f.data(), charge.data(), mass.data(), point.data(),
+                                              list.data(), spl[0], spl[1], spl[2], cutsq[0], cutsq[1], cutsq[2],
+                                              sc_pot, fphys.data())
+                      : force_eval_sc_nospline(q.data(), f.data(), charge.data(), mass.data(), point.data(),
+                                               list.data(), sc_pot, fphys.data());
     std::printf("init %.15e %.15e\n", e, sc_pot);
     std::mt19937 rng((unsigned)std::atoi(argv[3]));
     const int n_steps = std::atoi(argv[2]);
     for (int s = 0; s < n_steps; ++s) {
-        e = update_sc_nospline(q.data(), p.data(), mass.data(), f.data(), fphys.data(), charge.data(), point.data(),
-                               list.data(), disp.data(), rng, true, heat, sc_pot);
+        if (spline)
+            e = update_sc_wspline(q.data(), p.data(), mass.data(), f.data(), fphys.data(), charge.data(),
+                                  point.data(), list.data(), disp.data(), rng, true, heat, sc_pot, spl[0], spl[1],
+                                  spl[2], cutsq[0], cutsq[1], cutsq[2]);
+        else
+            e = update_sc_nospline(q.data(), p.data(), mass.data(), f.data(), fphys.data(), charge.data(),
+                                   point.data(), list.data(), disp.data(), rng, true, heat, sc_pot);
         std::printf("step %d %.15e %.15e %.15e %.15e\n", s, e, sc_pot, heat, get_kcv(q.data(), fphys.data()));
     }
     double qsum = 0.0, psum = 0.0;

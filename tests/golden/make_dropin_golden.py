@@ -20,7 +20,9 @@ from qtip4pf_water_gb300.start import seeded_start  # noqa: E402
 
 REF_DIR = os.environ.get("REF_DIR", "/root/reference")
 REF_SRCS = ["forces.cpp", "neighbour.cpp", "fourier.cpp", "update.cpp", "thermostat.cpp", "path_integrals.cpp"]
-CASES = {"dropin_n64_p4": (64, 4, 298.0, 0.25, 31, 6, 77)}
+# name: (n_mols, n_beads, temp_K, dt_fs, start seed, steps, mt19937 seed[, "spline"])
+CASES = {"dropin_n64_p4": (64, 4, 298.0, 0.25, 31, 6, 77),
+         "dropin_spline_n64_p4": (64, 4, 298.0, 0.25, 32, 4, 78, "spline")}
 
 
 def write_start(path, st, dt_fs, eps_ewald=1e-6, eps_sc=1e-5):
@@ -35,15 +37,21 @@ def main():
     drv = os.path.join(ROOT, "tests", "compat", "dropin_driver.cpp")
     with tempfile.TemporaryDirectory() as tmp:
         exe = os.path.join(tmp, "dropin_ref")
+        # the oracle's Boost stand-in evaluates splines with liboracle.so's restatement
+        odir = os.path.join(ROOT, "oracle", "_build")
+        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
         subprocess.check_call(["g++", "-O2", "-std=c++17", "-w", "-fopenmp", "-I", os.path.join(ROOT, "oracle", "shim"),
-                               "-I", REF_DIR, drv] + [os.path.join(REF_DIR, s) for s in REF_SRCS] + ["-o", exe])
-        for name, (N, P, T, dt, seed, steps, rng) in CASES.items():
+                               "-I", REF_DIR, drv] + [os.path.join(REF_DIR, s) for s in REF_SRCS] +
+                              ["-L", odir, "-loracle", f"-Wl,-rpath,{odir}", "-o", exe])
+        for name, spec in CASES.items():
+            N, P, T, dt, seed, steps, rng = spec[:7]
+            mode = list(spec[7:])
             st = seeded_start(N, P, T, seed=seed)
             binp = os.path.join(HERE, name + ".bin")
             write_start(binp, st, dt)
-            out = subprocess.check_output([exe, binp, str(steps), str(rng)], text=True)
+            out = subprocess.check_output([exe, binp, str(steps), str(rng)] + mode, text=True)
             with open(os.path.join(HERE, name + ".txt"), "w") as f:
-                f.write(f"# {steps} {rng}\n" + out)
+                f.write(f"# {steps} {rng}{' ' + mode[0] if mode else ''}\n" + out)
             print(name, out.splitlines()[-1])
 
 
