@@ -7,7 +7,9 @@ stepper against the oracle.
 Tolerances as the other parity tests: FP64 1e-9 relative RMS (Suzuki-Chin
 forces 1e-8: the finite difference amplifies round-off by 1/eps_sc), mixed
 1e-4; the spline part of the forces alone (wspline minus nospline) within 1e-9
-(FP64) and 1e-4 (mixed) of its own size.
+(FP64) and 1e-4 (mixed) of its own size. Positions after the steps: FP64 to
+round-off; mixed within 1e-7 relative RMS (forces within 1e-4 move a 0.25 fs
+step's positions by at most ~1e-6 bohr).
 """
 import glob
 import os
@@ -82,7 +84,7 @@ def test_spline_steps_match_the_reference(gpu_lib, case, precision):
         es = [s.update_trajectory_class_nospline(x, p, s.masses(), f, s.charges(), point, lst, disp)
               for _ in range(3)]
         np.testing.assert_allclose(es, g["vv_energy"], rtol=tol)
-        assert rel_rms(x, g["vv_q"]) < (1e-14 if precision == "fp64" else 1e-10)
+        assert rel_rms(x, g["vv_q"]) < (1e-14 if precision == "fp64" else 1e-8)
         assert rel_rms(f, g["vv_f"]) < tol
     else:
         fsc = np.zeros(P * 9 * N)
@@ -98,7 +100,7 @@ def test_spline_steps_match_the_reference(gpu_lib, case, precision):
             e, heat, _ = s.update_sc_nospline(x, p, s.masses(), f, fp, s.charges(), point, lst, disp, False, heat)
             es.append(e)
         np.testing.assert_allclose(es, g["nve_energy"], rtol=1e-8 if precision == "fp64" else 1e-5)
-        assert rel_rms(x, g["nve_q"]) < (1e-13 if precision == "fp64" else 1e-9)
+        assert rel_rms(x, g["nve_q"]) < (1e-13 if precision == "fp64" else 1e-7)
         assert rel_rms(fp, g["nve_fphys"]) < tol
 
 
