@@ -260,6 +260,21 @@ qtg_status qtg_get_constants(qtg_constants *out);
 qtg_status qtg_register_host(void *ptr, size_t bytes);
 qtg_status qtg_unregister_host(void *ptr);
 
+/* ---- starting configurations (host) ----------------------------------------- */
+/* initialise.cpp:19-95  initialise_fcc(): nx x ny x nz fcc cells of 4 waters at
+ * density rho (g/cm^3; cell side as water.cpp:90-97), every molecule at the
+ * equilibrium geometry in one orientation; pos: double[n_beads][9 n_mols] with
+ * n_mols = 4 nx ny nz, every bead identical; box_bohr (may be NULL) receives
+ * the box. */
+qtg_status qtg_lattice_fcc(int nx, int ny, int nz, double rho_g_cm3, int n_beads, double *pos, double *box_bohr);
+/* initialise.cpp:137-541  initialise_orth(rng, outfile): proton-disordered ice Ih
+ * in nx x ny x nz orthorhombic cells of 8 waters (water.cpp:99-108), obeying
+ * the ice rules with zero dipole moment, drawn from std::mt19937(seed) in the
+ * reference's order (the same seed gives the reference's configuration);
+ * n_mols = 8 nx ny nz. */
+qtg_status qtg_lattice_ice_ih(int nx, int ny, int nz, double rho_g_cm3, int n_beads, unsigned int seed,
+                              double *pos, double *box_bohr);
+
 /* ---- tabulated pair corrections ("fast-CMD" splines) ------------------------ */
 /* Replaces the spline part of get_forces_wspline / force_eval_sc_wspline
  * (forces.cpp:452-466, :634-691, :791-882): every atom pair of a configuration

@@ -12,6 +12,7 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <fstream>
 #include <random>
 #include <string>
 #include <vector>
@@ -25,6 +26,7 @@
 #include "update.h"
 #include "thermostat.h"
 #include "path_integrals.h"
+#include "initialise.h"
 
 // ---- the reference's configuration globals (declared extern in qtip4pfparams.h)
 double T_K, epsilonsc, rho_inp, dtfs, eps, a_cell_angs, a_cell, b_cell, c_cell, rnn;
@@ -216,6 +218,57 @@ double ref_bussi(double *p, unsigned seed, double *noise) {
     noise[0] = R;
     noise[1] = g2;
     return heat;
+}
+
+// ---- starting configurations: initialise.cpp -------------------------------
+// The cell globals as water.cpp:76-114 derives them for "fcc" (cell 0) or
+// "orth" (cell 1) from nx x ny x nz cells at density rho (g/cm^3).
+void ref_setup_cells(int nx, int ny, int nz, double rho_g_cm3, int orth, int nbeads) {
+    n_beads = nbeads;
+    n_cell_x = nx;
+    n_cell_y = ny;
+    n_cell_z = nz;
+    n_cells = nx * ny * nz;
+    rho_inp = rho_g_cm3;
+    if (!orth) {
+        n_mols = 4 * n_cells;
+        a_cell_angs = 1e8 * std::cbrt(4 * mh2o / rho_inp);
+        a_cell = a_cell_angs * angs2bohr;
+        b_cell = a_cell;
+        c_cell = a_cell;
+    } else {
+        n_mols = 8 * n_cells;
+        a_cell_angs = 1e8 * std::cbrt(4 * mh2o / (sqrt(2.0) * rho_inp));
+        a_cell = a_cell_angs * angs2bohr;
+        b_cell = sqrt3 * a_cell;
+        c_cell = 2.0 * sqrt(2.0 / 3.0) * a_cell;
+        rnn = (0.5 - 2.0 * zo) * c_cell;
+    }
+    n_atoms = 3 * n_mols;
+    n_dof = 3 * n_atoms;
+    boxl = {n_cell_x * a_cell, n_cell_y * b_cell, n_cell_z * c_cell};
+}
+
+int ref_n_mols(void) { return n_mols; }
+void ref_box(double *out) {
+    out[0] = boxl[0];
+    out[1] = boxl[1];
+    out[2] = boxl[2];
+}
+
+void ref_initialise_fcc(double *out) {
+    double *p = initialise_fcc();
+    std::memcpy(out, p, sizeof(double) * (size_t)n_beads * n_dof);
+    delete[] p;
+}
+
+// initialise_orth with std::mt19937(seed); its log lines go to `logpath`
+void ref_initialise_orth(unsigned seed, const char *logpath, double *out) {
+    std::mt19937 rng(seed);
+    std::ofstream log(logpath);
+    double *p = initialise_orth(rng, log);
+    std::memcpy(out, p, sizeof(double) * (size_t)n_beads * n_dof);
+    delete[] p;
 }
 
 // ---- the spline ("fast-CMD") path: forces.cpp:634-691, :791-882; update.cpp

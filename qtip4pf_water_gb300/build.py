@@ -24,6 +24,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libqtipgpu.so")
 COMPAT = os.path.join(BUILD, "libqtip_compat.so")
 DROPIN_BENCH = os.path.join(BUILD, "dropin_bench")
+RUN_DRIVER = os.path.join(BUILD, "qtg_water")
 INCLUDE = os.path.join(ROOT, "include")
 # boost::math::cubic_b_spline for drop-in builds without Boost (the reference's
 # spline signatures name that type)
@@ -44,7 +45,7 @@ def nvcc() -> str:
 
 
 def _sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
 def _headers():
@@ -76,11 +77,15 @@ def build(force: bool = False, verbose: bool = False) -> str:
     hdrs = _headers()
     objs = []
     jobs = []
+    cxx = shutil.which("g++") or "g++"
     for s in srcs:
-        o = os.path.join(BUILD, os.path.basename(s)[:-3] + ".o")
+        o = os.path.join(BUILD, os.path.splitext(os.path.basename(s))[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
-            jobs.append([nv] + ARCH + NVFLAGS + ["-I", INCLUDE, "-c", s, "-o", o])
+            if s.endswith(".cpp"):  # host-only C++
+                jobs.append([cxx, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", INCLUDE, "-c", s, "-o", o])
+            else:
+                jobs.append([nv] + ARCH + NVFLAGS + ["-I", INCLUDE, "-c", s, "-o", o])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             for f in [ex.submit(_run, j, verbose) for j in jobs]:
@@ -101,6 +106,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
         cxx = shutil.which("g++") or "g++"
         _run([cxx, "-O2", "-std=c++17", bench_src, "-o", DROPIN_BENCH, "-L", BUILD, "-lqtip_compat", "-lqtipgpu",
               "-Wl,-rpath,$ORIGIN"], verbose)
+    # the run driver: config.txt in, the reference's output files out (device-resident steps)
+    drv_src = os.path.join(CSRC, "driver", "qtg_water.cpp")
+    if os.path.exists(drv_src) and (force or _stale(RUN_DRIVER, [drv_src, LIB, os.path.join(CSRC, "lattice.h")] + hdrs)):
+        cxx = shutil.which("g++") or "g++"
+        _run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", INCLUDE, drv_src, "-o", RUN_DRIVER, "-L", BUILD,
+              "-lqtipgpu", "-Wl,-rpath,$ORIGIN"], verbose)
     return LIB
 
 
