@@ -246,6 +246,10 @@ struct qtg_ctx {
     double *box_energy = nullptr, *box_energy_d = nullptr;  // [max_p] per-bead energies
     int *box_rebuilt = nullptr, *box_rebuilt_d = nullptr;    // [max_p] per-bead rebuild flags
     size_t total_point_full = 0, total_list_full = 0;
+    // Verlet-list build scratch
+    size_t total_cells = 0;
+    int *list_flag = nullptr, *cnt_half = nullptr, *cnt_full = nullptr, *cell_start = nullptr, *cell_mol = nullptr;
+    float4 *wpos = nullptr;
     double *charge = nullptr, *mass = nullptr, *inv_mass = nullptr, *sqrt_mass = nullptr;
     double *cf_acc = nullptr;  // mean-centroid-force sums of constrained systems, per dof (like mass)
     size_t n_cf = 0;
@@ -516,6 +520,12 @@ ListArgs list_args(qtg_ctx *c, int first_job, int n_jobs, int force) {
     l.acc = c->acc;
     l.run = c->run;
     l.rebuilt = c->rebuilt;
+    l.flag = c->list_flag;
+    l.wpos = c->wpos;
+    l.cnt_half = c->cnt_half;
+    l.cnt_full = c->cnt_full;
+    l.cell_start = c->cell_start;
+    l.cell_mol = c->cell_mol;
     l.status = c->status;
     l.force_rebuild = force;
     l.max_mols = c->max_mols;
@@ -876,6 +886,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     std::vector<ModeCoef> mode_all;
     std::vector<double> chg_all, mass_all;
     long long q_off = 0, d_off = 0, pt_off = 0, ls_off = 0, chg_off = 0, mass_off = 0, pf_off = 0, lf_off = 0;
+    long long lc_off = 0;
     long long nm_off = 0, mode_off = 0;
     int job_base = 0;
     for (int s = 0; s < n_systems; ++s) {
@@ -976,6 +987,20 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         S.ls_off = ls_off;
         S.pf_off = pf_off;
         S.lf_off = lf_off;
+        // Verlet-list cell grid: side >= r_skin / 2 (with a margin over the FP32 pair
+        // test's band), five or more cells a side, at most 20
+        {
+            const double cell_min = 0.5 * K.r_skin * (1.0 + 1e-3);
+            bool cells = true;
+            for (int k = 0; k < 3; ++k) {
+                S.lc_n[k] = std::min(20, (int)std::floor(S.box[k] / cell_min));
+                cells = cells && S.lc_n[k] >= 5;
+            }
+            S.lc_cells = cells ? S.lc_n[0] * S.lc_n[1] * S.lc_n[2] : 0;
+            if (!cells) S.lc_n[0] = S.lc_n[1] = S.lc_n[2] = 1;
+            S.lc_off = lc_off;
+            lc_off += (long long)P * (S.lc_cells + 1);
+        }
         S.chg_off = chg_off;
         S.mass_off = mass_off;
         S.nm_off = nm_off;
@@ -1069,6 +1094,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     ctx->total_point = (size_t)pt_off;
     ctx->total_list = (size_t)ls_off;
     ctx->total_point_full = (size_t)pf_off;
+    ctx->total_cells = (size_t)lc_off;
     ctx->total_list_full = (size_t)lf_off;
     ctx->total_nm = (size_t)nm_off;
     ctx->total_modes = (size_t)mode_off;
@@ -1188,6 +1214,11 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->point, ctx->total_point);
     AL(ctx->list, ctx->total_list);
     AL(ctx->point_full, ctx->total_point_full);
+    AL(ctx->wpos, ctx->total_point);
+    AL(ctx->cnt_half, ctx->total_point);
+    AL(ctx->cnt_full, ctx->total_point);
+    AL(ctx->cell_mol, ctx->total_point);
+    AL(ctx->cell_start, ctx->total_cells);
     AL(ctx->list_full, ctx->total_list_full);
     AL(ctx->charge, chg_all.size());
     AL(ctx->mass, mass_all.size());
@@ -1236,6 +1267,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->energy_aux, ctx->total_slots);
     AL(ctx->base.d, ctx->base.h.size());
     AL(ctx->rebuilt, ctx->base.h.size());
+    AL(ctx->list_flag, ctx->base.h.size());
     if (e == cudaSuccess) {
         void *pin = nullptr;
         const size_t bytes = sizeof(CallBox) + (sizeof(double) + sizeof(int)) * ctx->max_p;
@@ -1342,7 +1374,8 @@ void qtg_destroy(qtg_ctx *ctx) {
                     ctx->phase, ctx->opos, ctx->part, ctx->skp, ctx->dskp, ctx->wsk, ctx->wdsk, ctx->energy, ctx->energy_aux,
                     ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
-                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf, ctx->fin_ticket, ctx->sites_fix, ctx->intra, ctx->kfc, ctx->kfb, ctx->wpk};
+                    ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf, ctx->fin_ticket, ctx->sites_fix, ctx->intra, ctx->kfc, ctx->kfb, ctx->wpk,
+                    ctx->wpos, ctx->cnt_half, ctx->cnt_full, ctx->cell_start, ctx->cell_mol, ctx->list_flag};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->box) cudaFreeHost(ctx->box);

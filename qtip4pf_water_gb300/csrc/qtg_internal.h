@@ -33,6 +33,11 @@ struct SysDev {
     // those columns come last, so the kept groups, batches and k entries are prefixes
     int n_grp_half, n_batch_half, n_kvec_half, n_col_half;
     int centroid_fixed;          // 1: the centroid is held fixed (centroid-constrained PIMD)
+    // Verlet-list build: cell grid of side >= r_skin / 2 (lc_n cells a side, lc_cells in
+    // all; 0 cells: boxes under five cells a side scan every molecule), cell starts of
+    // bead b at lc_off + b (lc_cells + 1)
+    int lc_n[3], lc_cells;
+    long long lc_off;
     int lj_tie_mask;             // bit d: half of box side d lies within r_cut (a half-box tie can matter)
     long long nm_off;   // doubles: P x P bead->normal-mode matrix C (y = C x)
     long long mode_off; // ModeCoef entries: P per system
@@ -590,8 +595,15 @@ struct ListArgs {
     unsigned *status;
     int force_rebuild;  // 1: rebuild unconditionally (initial build / per-call API)
     int max_mols;
+    // build scratch, indexed like point (pt_off + bead N) unless noted
+    int *flag;          // per base job: 1 while a rebuild of that bead is under way this launch
+    float4 *wpos;       // oxygen positions wrapped into the box (FP32)
+    int *cnt_half, *cnt_full;  // per-row neighbour counts
+    int *cell_start;    // per bead lc_cells + 1 (lc_off)
+    int *cell_mol;      // molecules by cell
 };
 void launch_skin_rebuild(const ListArgs &a, cudaStream_t s, unsigned long long *launches);
+constexpr int LC_MAX_CELLS = 8000;  // cells of the Verlet-list build's grid (20 a side at most)
 
 // stage.cu: the per-call mailbox and the kernels that move a per-call step's
 // arrays between the caller's page-locked host memory and the device
