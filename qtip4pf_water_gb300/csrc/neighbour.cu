@@ -201,7 +201,14 @@ __device__ void row_bitmap(const ListArgs &a, const SysDev &S, int bead, int i, 
         if (j != i && pair_in(pi, wp[j], qb + 9 * i, qb + 9 * j, S, rs2)) atomicOr(&bm[j >> 5], 1u << (j & 31));
     };
     if (S.lc_cells == 0) {
-        for (int j = lane; j < N; j += 32) test(j);
+        // every molecule in order: the 32 lanes test the 32 molecules of one bitmap
+        // word, which a ballot assembles (no atomics on a shared word)
+        for (int j0 = 0; j0 < N; j0 += 32) {
+            const int j = j0 + lane;
+            const bool in = j < N && j != i && pair_in(pi, wp[j], qb + 9 * i, qb + 9 * j, S, rs2);
+            const unsigned word = __ballot_sync(0xffffffffu, in);
+            if (lane == 0) bm[j0 >> 5] = word;
+        }
     } else {
         const int *cs = a.cell_start + S.lc_off + (size_t)bead * (S.lc_cells + 1);
         const int *cm = a.cell_mol + S.pt_off + (size_t)bead * N;

@@ -191,14 +191,18 @@ def replica_set(seed=48, n=48):
             for k, (a, b, c) in enumerate(u)]
 
 
-def replicas48(steps=200, seed=48, warm=10):
+def replicas48(steps=200, seed=48, warm=10, compare=1, autotune=1):
+    """The 48 uneven replicas in one context (one graph replay a step); with
+    compare=1 also the same systems one context at a time; autotune=0 keeps the
+    launcher's heuristic shapes (fewer launches ahead of the steps, for
+    launch-list captures)."""
     reps = replica_set(seed)
     starts = [seeded_start(N, P, T, seed=s) for N, P, T, s in reps]
     descs = [system_desc(N, P, st.box_bohr, temp_K=T, dt_fs=0.25, propagator=TROTTER, thermostat=PILE_G, seed=s)
              for (N, P, T, s), st in zip(reps, starts)]
     bead_steps = sum(P for _, P, _, _ in reps) * steps
     # all replicas in one context
-    ctx, tuned = make_ctx(descs, starts, MIXED, autotune=True)
+    ctx, tuned = make_ctx(descs, starts, MIXED, autotune=bool(autotune))
     ctx.run_steps(warm, is_nvt=True)
     ctx.sync()
     l0 = ctx.kernel_launches()
@@ -211,7 +215,7 @@ def replicas48(steps=200, seed=48, warm=10):
     ctx.close()
     # the same systems, one context at a time
     t_single = 0.0
-    for d, st in zip(descs, starts):
+    for d, st in zip(descs, starts) if compare else ():
         c1, _ = make_ctx([d], [st], MIXED, autotune=True)
         c1.run_steps(warm, is_nvt=True)
         c1.sync()
@@ -223,19 +227,27 @@ def replicas48(steps=200, seed=48, warm=10):
     return {"workload": "replicas48", "replicas": len(reps), "steps": steps,
             "systems": [{"n_mols": N, "n_beads": P, "temp_K": round(T, 2)} for N, P, T, _ in reps],
             "total_beads": sum(P for _, P, _, _ in reps), "total_waters": sum(N for N, _, _, _ in reps),
-            "batched_bead_steps_per_s": bead_steps / t_batch, "one_at_a_time_bead_steps_per_s": bead_steps / t_single,
-            "batched_speedup": t_single / t_batch, "batched_ms_per_step": t_batch / steps * 1e3,
+            "batched_bead_steps_per_s": bead_steps / t_batch,
+            "one_at_a_time_bead_steps_per_s": bead_steps / t_single if compare else None,
+            "batched_speedup": t_single / t_batch if compare else None, "batched_ms_per_step": t_batch / steps * 1e3,
             "autotune_ms_heuristic_vs_tuned": tuned, "tuned_chunks_rj_sc_kc": shape,
             "launches_per_step": launches_per_step}
 
 
 def cmd(n_configs=4096, constrained_steps=2000, replicas=64, fit_steps=2000, deploy_mols=4096, deploy_beads=32,
-        fresh_configs=2, fresh_steps=1000, timing_steps=50, seed=5, train_mols=216, train_beads=32, held_out=256):
+        fresh_configs=8, fresh_steps=2000, fresh_repeats=2, timing_steps=50, seed=5, train_mols=216, train_beads=32,
+        held_out=256):
     """Learned centroid correction: training data from constrained PIMD of
     train_mols waters (train_beads beads), training on the tensor cores, held-out
     error; then surrogate CMD of deploy_mols waters against plain PIMD centroid
     sampling (deploy_beads beads), and the surrogate's centroid-force error
-    judged against fresh constrained-PIMD samples of the deployed system."""
+    judged against fresh constrained-PIMD samples of the deployed system.
+
+    Each fresh centroid gets fresh_repeats independent constrained runs
+    (different internal-mode starts and noise); the target is their mean, and
+    the targets' own sampling noise is reported beside the errors: the noise
+    floor is the RMS error a perfect predictor would show against the averaged
+    target, RMS(run a - run b) / 2 over RMS(target) for two runs."""
     from . import surrogate as sg
     from .start import spread_beads
 
@@ -291,29 +303,47 @@ def cmd(n_configs=4096, constrained_steps=2000, replicas=64, fit_steps=2000, dep
     p_ctx.run_steps(timing_steps, is_nvt=True)
     p_ctx.sync()
     t_pimd = (time.perf_counter() - t0) / timing_steps
-    # fresh constrained-PIMD mean centroid forces at the surrogate-CMD centroids
-    fmean, fclass = [], []
+    # fresh constrained-PIMD mean centroid forces at the surrogate-CMD centroids,
+    # fresh_repeats independent runs each (own bead spread; the stepper's noise
+    # counter moves on between runs)
+    runs = []
     for k, c in enumerate(snaps):
-        q, p = spread_beads(c, deploy_beads, 298.0, seed=seed * 100 + k)
-        ps.set_state(q, p)
-        ps.set_centroid_fixed(True)
-        p_ctx.init_forces()
-        p_ctx.run_steps(200, is_nvt=True)  # internal modes relax around the fixed centroid
-        ps.reset_centroid_force()
-        p_ctx.run_steps(fresh_steps, is_nvt=True)
-        p_ctx.sync()
-        f, n = ps.centroid_force()
-        fmean.append(f)
-        ps.set_centroid_fixed(False)
+        per = []
+        for r in range(fresh_repeats):
+            q, p = spread_beads(c, deploy_beads, 298.0, seed=seed * 100 + 17 * k + r)
+            ps.set_state(q, p)
+            ps.set_centroid_fixed(True)
+            p_ctx.init_forces()
+            p_ctx.run_steps(200, is_nvt=True)  # internal modes relax around the fixed centroid
+            ps.reset_centroid_force()
+            p_ctx.run_steps(fresh_steps, is_nvt=True)
+            p_ctx.sync()
+            f, n = ps.centroid_force()
+            per.append(f)
+            ps.set_centroid_fixed(False)
+        runs.append(per)
     p_ctx.close()
-    snaps, fmean = np.array(snaps), np.array(fmean)
+    runs = np.array(runs)  # [config][repeat][9N]
+    snaps, fmean = np.array(snaps), runs.mean(axis=1)
     fclass = sg.classical_forces(snaps, deploy_mols, box)
     fresh = sg.Dataset(deploy_mols, box, snaps, fmean, fclass, {})
+    den = float(np.sqrt(np.mean(fmean ** 2)))
+    noise = None
+    if fresh_repeats >= 2:
+        diff = runs[:, 0] - runs[:, 1]
+        # one run's noise is RMS(diff) / sqrt 2; the mean of R runs carries 1 / sqrt R of it
+        noise = float(np.sqrt(np.mean(diff ** 2)) / np.sqrt(2.0) / np.sqrt(fresh_repeats) / den)
     rep["deploy"] = {"n_mols": deploy_mols, "box_angstrom": float(box[0] * 0.529177210903),
                      "surrogate_cmd_ms_per_step": t_cmd * 1e3, "surrogate_cmd_ns_day": ns_per_day(t_cmd, 0.25),
                      "pimd_ms_per_step": t_pimd * 1e3, "pimd_beads": deploy_beads,
                      "pimd_ns_day": ns_per_day(t_pimd, 0.25), "speedup_over_pimd": t_pimd / t_cmd,
-                     "fresh_constrained_pimd": dict(model.evaluate(fresh), steps=fresh_steps, beads=deploy_beads)}
+                     "fresh_constrained_pimd": dict(model.evaluate(fresh), steps=fresh_steps, beads=deploy_beads,
+                                                    repeats=fresh_repeats, target_noise_floor=noise)}
+    ev = rep["deploy"]["fresh_constrained_pimd"]
+    if noise is not None:
+        # the error left once the targets' own noise is taken out (independent errors add in squares)
+        ev["rms_rel_err_corrected_noise_removed"] = float(np.sqrt(max(ev["rms_rel_err_corrected"] ** 2 - noise ** 2,
+                                                                      0.0)))
     return rep
 
 
