@@ -235,6 +235,10 @@ qtg_status qtg_kwald_noalloc(const double *sites, const double *charge, int n_si
  * "kforce", "combine", "lj", "rebuild", "ring", "end_step". Overwrites the
  * context's forces and may move its state: call after the measured run. */
 qtg_status qtg_time_kernel(qtg_ctx *ctx, const char *name, int iters, double *avg_ms);
+/* Writes a device buffer larger than the L2 cache (256 MiB, allocated on the
+ * first call and kept) on the context's stream and waits for it: timing loops
+ * call it between timed calls so that no call finds its data in L2. */
+qtg_status qtg_flush_l2(qtg_ctx *ctx);
 /* FP32 fused-multiply-add throughput of the current device (TFLOP/s, 2 flops
  * per FMA) from a dependent-chain kernel filling every SM. */
 qtg_status qtg_fp32_peak(double *tflops);

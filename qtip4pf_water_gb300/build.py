@@ -25,6 +25,7 @@ LIB = os.path.join(BUILD, "libqtipgpu.so")
 COMPAT = os.path.join(BUILD, "libqtip_compat.so")
 DROPIN_BENCH = os.path.join(BUILD, "dropin_bench")
 RUN_DRIVER = os.path.join(BUILD, "qtg_water")
+E2E_BENCH = os.path.join(BUILD, "e2e_bench")
 INCLUDE = os.path.join(ROOT, "include")
 # boost::math::cubic_b_spline for drop-in builds without Boost (the reference's
 # spline signatures name that type)
@@ -112,6 +113,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
         cxx = shutil.which("g++") or "g++"
         _run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", INCLUDE, drv_src, "-o", RUN_DRIVER, "-L", BUILD,
               "-lqtipgpu", "-Wl,-rpath,$ORIGIN"], verbose)
+    # the per-call end-to-end timing driver (C ABI from host C++)
+    e2e_src = os.path.join(CSRC, "driver", "e2e_bench.cpp")
+    if os.path.exists(e2e_src) and (force or _stale(E2E_BENCH, [e2e_src, LIB] + hdrs)):
+        cxx = shutil.which("g++") or "g++"
+        _run([cxx, "-O2", "-std=c++17", "-I", INCLUDE, e2e_src, "-o", E2E_BENCH, "-L", BUILD, "-lqtipgpu",
+              "-Wl,-rpath,$ORIGIN"], verbose)
     return LIB
 
 

@@ -316,6 +316,8 @@ struct qtg_ctx {
     std::vector<PairSplines> spl_h;
     std::vector<std::vector<double>> spl_coef_h;  // per system: the three types' coefficients back to back
     bool spl_any = false;
+    void *flush_buf = nullptr;  // qtg_flush_l2's buffer
+    int flush_val = 1;
     int n_sm = 148;
     unsigned long long h2d_bytes = 0, d2h_bytes = 0;  // host <-> device traffic of the per-call entries
     // per-call ring-polymer steps captured as graphs, by (system, NVT, caller noise): graph, kernels in it
@@ -1053,23 +1055,43 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         if (d.propagator == QTG_SUZUKI_CHIN && P > 1) ctx->any_sc = true;
     }
     // Structure-factor groups: runs of <= kz |kz| values of one column (each |kz|
-    // standing for +kz and -kz), one thread each, 128 threads a block. The width
-    // (3 or 4) is the one whose launch does less work by a simple model: whole
-    // blocks of threads, each paying the column factor (~7 instructions a site) and
-    // ~9 a |kz| (mixed, the three-multiplication form: ~8 and ~5), over every
-    // system's half set, sites and beads.
+    // standing for +kz and -kz), one thread each, 128 threads a block; a thread
+    // stops at its group's last |kz| and the groups are sorted by size, so warps
+    // run groups of one size. The width is the one whose launch does the least
+    // work by a simple model: whole blocks of threads, each paying the column
+    // factor once a site (~7 instructions; mixed ~8) and ~9 a |kz| (mixed, the
+    // three-multiplication form: ~5). Widths 6 and 8 (the column factor shared by
+    // more |kz|, more registers a thread) only for mixed contexts without
+    // Suzuki-Chin systems, whose derivative jobs keep 3 or 4; QTG_KSK_GROUP
+    // (3, 4, 6, 8) fixes the width.
     {
         const double per_col = ctx->mixed ? 8.0 : 7.0, per_kz = ctx->mixed ? 5.0 : 9.0;
-        double cost[2] = {0.0, 0.0};
-        for (int w = 0; w < 2; ++w) {
-            const int kz = 3 + w;
+        const int widths[4] = {3, 4, 6, 8};
+        const int n_w = (ctx->mixed && !ctx->any_sc) ? 4 : 2;
+        double best = 0.0;
+        ctx->kz = 3;
+        for (int w = 0; w < n_w; ++w) {
+            const int kz = widths[w];
+            double cost = 0.0;
             for (const SysDev &S : ctx->sys_h) {
-                long long g = 0;
-                for (int c = 0; c < S.n_col_half; ++c) g += (call[S.col_off + c].m + kz) / kz;
-                cost[w] += (double)((g + 127) / 128 * 128) * (per_col + per_kz * kz) * S.n_sites * S.n_beads;
+                long long g = 0, work = 0;
+                for (int c = 0; c < S.n_col_half; ++c) {
+                    const int m = call[S.col_off + c].m;
+                    g += (m + kz) / kz;
+                    work += (long long)((m + kz) / kz) * per_col + (long long)(m + 1) * per_kz;
+                }
+                // idle lanes of the last block
+                cost += ((double)work + (double)((g + 127) / 128 * 128 - g) * per_col) * S.n_sites * S.n_beads;
+            }
+            if (w == 0 || cost < best) {
+                best = cost;
+                ctx->kz = kz;
             }
         }
-        ctx->kz = cost[0] < cost[1] ? 3 : 4;
+        if (const char *e = getenv("QTG_KSK_GROUP")) {
+            const int v = atoi(e);
+            if (v == 3 || v == 4 || ((v == 6 || v == 8) && n_w == 4)) ctx->kz = v;
+        }
         for (SysDev &S : ctx->sys_h) {
             S.grp_off = (int)gall.size();
             for (int c = 0; c < S.n_col; ++c) {
@@ -1086,6 +1108,11 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
             }
             S.n_grp = (int)gall.size() - S.grp_off;
             if (S.n_col_half == S.n_col) S.n_grp_half = S.n_grp;
+            // larger groups first (the half set and the rest separately): a warp's
+            // threads stop at the same |kz|
+            auto by_size = [](const KGroup &x, const KGroup &y) { return x.n > y.n; };
+            std::stable_sort(gall.begin() + S.grp_off, gall.begin() + S.grp_off + S.n_grp_half, by_size);
+            std::stable_sort(gall.begin() + S.grp_off + S.n_grp_half, gall.end(), by_size);
             ctx->max_grp = std::max(ctx->max_grp, S.n_grp);
         }
     }
@@ -1382,6 +1409,7 @@ void qtg_destroy(qtg_ctx *ctx) {
     for (auto &g : ctx->surrogates) free_surrogate(g);
     if (ctx->spl) cudaFree(ctx->spl);
     if (ctx->spl_coef) cudaFree(ctx->spl_coef);
+    if (ctx->flush_buf) cudaFree(ctx->flush_buf);
     for (auto &g : ctx->call_graphs) cudaGraphExecDestroy(g.second.first);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
@@ -2410,6 +2438,15 @@ qtg_status qtg_fp32_peak(double *tflops) {
 
 qtg_status qtg_fp64_peak(double *tflops) {
     return fma_peak<double>(tflops, 1 << 11, [](double *o, int b, int it) { launch_fp64_probe(o, b, it, nullptr); });
+}
+
+qtg_status qtg_flush_l2(qtg_ctx *ctx) {
+    if (!ctx) return QTG_ERR_ARG;
+    constexpr size_t bytes = (size_t)256 << 20;
+    if (!ctx->flush_buf) CK(cudaMalloc(&ctx->flush_buf, bytes));
+    CK(cudaMemsetAsync(ctx->flush_buf, ctx->flush_val++ & 0xff, bytes, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return QTG_OK;
 }
 
 qtg_status qtg_reset_estimators(qtg_ctx *ctx) {
