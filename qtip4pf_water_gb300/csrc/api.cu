@@ -1070,7 +1070,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         const int n_w = (ctx->mixed && !ctx->any_sc) ? 4 : 2;
         double best = 0.0;
         ctx->kz = 3;
-        for (int w = 0; w < n_w; ++w) {
+        for (int w = 0; w < 2; ++w) {
             const int kz = widths[w];
             double cost = 0.0;
             for (const SysDev &S : ctx->sys_h) {
