@@ -26,6 +26,8 @@
 //  4. k_list_rows (fill): the bitmap again, read word by word in ascending j, so
 //     the rows come out in the reference's order whatever order the cells gave.
 // Rows spread over many blocks per bead (the build is O(N) candidates a row).
+#include <algorithm>
+
 #include "qtg_internal.h"
 
 namespace qtg {
@@ -227,18 +229,34 @@ __device__ void row_bitmap(const ListArgs &a, const SysDev &S, int bead, int i, 
 }
 
 // FILL = false: the rows' counts; true: the rows' entries (after k_list_scan).
+// Work items are (job, block of ROWS rows); a fixed grid loops over them and
+// skips the jobs that do not rebuild, so a step without rebuilds costs one
+// flag load per item instead of one empty block per item.
 template <bool FILL>
-__global__ void __launch_bounds__(32 * ROWS) k_list_rows(ListArgs a) {
-    const int job = blockIdx.y;
+__device__ void list_row(const ListArgs &a, int job, int i, unsigned *bms);
+
+template <bool FILL>
+__global__ void __launch_bounds__(32 * ROWS) k_list_rows(ListArgs a, int row_blocks) {
+    extern __shared__ unsigned bms[];
+    const int w = threadIdx.x >> 5;
+    const long long n_items = (long long)a.n_jobs * row_blocks;
+    for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const int job = (int)(it / row_blocks), rb = (int)(it % row_blocks);
+        const SysDev &S = a.sys[a.job_sys[job]];
+        if (!a.flag[S.job_base + a.job_bead[job]]) continue;
+        const int i = rb * ROWS + w;
+        if (i >= S.n_mols) continue;
+        list_row<FILL>(a, job, i, bms + (size_t)w * ((S.n_mols + 31) >> 5));
+        __syncwarp();
+    }
+}
+
+template <bool FILL>
+__device__ void list_row(const ListArgs &a, int job, int i, unsigned *bm) {
     const int sid = a.job_sys[job], bead = a.job_bead[job];
     const SysDev &S = a.sys[sid];
-    if (!a.flag[S.job_base + bead]) return;
     const int N = S.n_mols, W = (N + 31) >> 5;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int i = blockIdx.x * ROWS + w;
-    if (i >= N) return;
-    extern __shared__ unsigned bms[];
-    unsigned *bm = bms + (size_t)w * W;
+    const int lane = threadIdx.x & 31;
     row_bitmap(a, S, bead, i, bm);
     if (!FILL) {
         int full = 0, half = 0;
@@ -351,11 +369,14 @@ void launch_skin_rebuild(const ListArgs &a, cudaStream_t s, unsigned long long *
     if (a.n_jobs <= 0) return;
     const int W = (a.max_mols + 31) / 32;
     k_skin_test<<<a.n_jobs, 256, (size_t)LC_MAX_CELLS * sizeof(int), s>>>(a);
-    const dim3 g((a.max_mols + ROWS - 1) / ROWS, a.n_jobs);
+    const int row_blocks = (a.max_mols + ROWS - 1) / ROWS;
+    const long long items = (long long)row_blocks * a.n_jobs;
+    // eight resident blocks on each of the 152 SMs at most
+    const int grid = (int)std::min<long long>(items, 152LL * 8);
     const size_t bm = (size_t)ROWS * W * sizeof(unsigned);
-    k_list_rows<false><<<g, 32 * ROWS, bm, s>>>(a);
+    k_list_rows<false><<<grid, 32 * ROWS, bm, s>>>(a, row_blocks);
     k_list_scan<<<a.n_jobs, 512, (size_t)a.max_mols * sizeof(int), s>>>(a);
-    k_list_rows<true><<<g, 32 * ROWS, bm, s>>>(a);
+    k_list_rows<true><<<grid, 32 * ROWS, bm, s>>>(a, row_blocks);
     if (launches) *launches += 4;
 }
 
