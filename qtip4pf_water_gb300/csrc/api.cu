@@ -248,7 +248,8 @@ struct qtg_ctx {
     size_t total_point_full = 0, total_list_full = 0;
     // Verlet-list build scratch
     size_t total_cells = 0;
-    int *list_flag = nullptr, *cnt_half = nullptr, *cnt_full = nullptr, *cell_start = nullptr, *cell_mol = nullptr;
+    int *cnt_half = nullptr, *cnt_full = nullptr, *cell_start = nullptr, *cell_mol = nullptr;
+    int *rb_jobs = nullptr, *rb_count = nullptr;
     float4 *wpos = nullptr;
     double *charge = nullptr, *mass = nullptr, *inv_mass = nullptr, *sqrt_mass = nullptr;
     double *cf_acc = nullptr;  // mean-centroid-force sums of constrained systems, per dof (like mass)
@@ -522,7 +523,8 @@ ListArgs list_args(qtg_ctx *c, int first_job, int n_jobs, int force) {
     l.acc = c->acc;
     l.run = c->run;
     l.rebuilt = c->rebuilt;
-    l.flag = c->list_flag;
+    l.rb_jobs = c->rb_jobs;
+    l.rb_count = c->rb_count;
     l.wpos = c->wpos;
     l.cnt_half = c->cnt_half;
     l.cnt_full = c->cnt_full;
@@ -1294,7 +1296,8 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->energy_aux, ctx->total_slots);
     AL(ctx->base.d, ctx->base.h.size());
     AL(ctx->rebuilt, ctx->base.h.size());
-    AL(ctx->list_flag, ctx->base.h.size());
+    AL(ctx->rb_jobs, ctx->base.h.size());
+    AL(ctx->rb_count, 1);
     if (e == cudaSuccess) {
         void *pin = nullptr;
         const size_t bytes = sizeof(CallBox) + (sizeof(double) + sizeof(int)) * ctx->max_p;
@@ -1402,7 +1405,8 @@ void qtg_destroy(qtg_ctx *ctx) {
                     ctx->base.d, ctx->fd.d, ctx->tan.d, ctx->fd_sc.d, ctx->tan_sc.d, ctx->base_sys, ctx->base_bead, ctx->odd_sys, ctx->odd_bead, ctx->sc_sys,
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
                     ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf, ctx->fin_ticket, ctx->sites_fix, ctx->intra, ctx->kfc, ctx->kfb, ctx->wpk,
-                    ctx->wpos, ctx->cnt_half, ctx->cnt_full, ctx->cell_start, ctx->cell_mol, ctx->list_flag};
+                    ctx->wpos, ctx->cnt_half, ctx->cnt_full, ctx->cell_start, ctx->cell_mol,
+                    ctx->rb_jobs, ctx->rb_count};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->box) cudaFreeHost(ctx->box);

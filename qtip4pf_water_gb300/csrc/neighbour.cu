@@ -22,7 +22,8 @@
 //     the 5 x 5 x 5 cells around i's cell, or every molecule in smaller boxes --
 //     are tested and marked in a per-row bitmap of all N molecules in shared
 //     memory; its population (all, and j > i) gives the row's two counts.
-//  3. k_list_scan, a block per job: row starts by exclusive scans, overflow check.
+//  3. k_list_scan, a block per rebuilding job: row starts by exclusive scans,
+//     overflow check.
 //  4. k_list_rows (fill): the bitmap again, read word by word in ascending j, so
 //     the rows come out in the reference's order whatever order the cells gave.
 // Rows spread over many blocks per bead (the build is O(N) candidates a row).
@@ -157,7 +158,8 @@ __global__ void __launch_bounds__(256) k_skin_test(ListArgs a) {
         __syncthreads();
         build = do_build;
     }
-    if (threadIdx.x == 0) a.flag[S.job_base + bead] = build;
+    // the rebuilding beads, in arrival order (each one's build is independent)
+    if (threadIdx.x == 0 && build) a.rb_jobs[atomicAdd(a.rb_count, 1)] = job;
     if (!build) return;
     const double *qb = a.q + S.q_off + (size_t)bead * S.n_dof;
     float4 *wp = a.wpos + S.pt_off + (size_t)bead * N;
@@ -229,9 +231,9 @@ __device__ void row_bitmap(const ListArgs &a, const SysDev &S, int bead, int i, 
 }
 
 // FILL = false: the rows' counts; true: the rows' entries (after k_list_scan).
-// Work items are (job, block of ROWS rows); a fixed grid loops over them and
-// skips the jobs that do not rebuild, so a step without rebuilds costs one
-// flag load per item instead of one empty block per item.
+// Work items are (rebuilding job, block of ROWS rows) over the list k_skin_test
+// made; a fixed grid loops over them, so a step without rebuilds costs each
+// block one load of the count.
 template <bool FILL>
 __device__ void list_row(const ListArgs &a, int job, int i, unsigned *bms);
 
@@ -239,11 +241,11 @@ template <bool FILL>
 __global__ void __launch_bounds__(32 * ROWS) k_list_rows(ListArgs a, int row_blocks) {
     extern __shared__ unsigned bms[];
     const int w = threadIdx.x >> 5;
-    const long long n_items = (long long)a.n_jobs * row_blocks;
+    // work items (rebuilding job, block of ROWS rows); none when no bead rebuilds
+    const long long n_items = (long long)(*a.rb_count) * row_blocks;
     for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {
-        const int job = (int)(it / row_blocks), rb = (int)(it % row_blocks);
+        const int job = a.rb_jobs[it / row_blocks], rb = (int)(it % row_blocks);
         const SysDev &S = a.sys[a.job_sys[job]];
-        if (!a.flag[S.job_base + a.job_bead[job]]) continue;
         const int i = rb * ROWS + w;
         if (i >= S.n_mols) continue;
         list_row<FILL>(a, job, i, bms + (size_t)w * ((S.n_mols + 31) >> 5));
@@ -322,10 +324,10 @@ __device__ void list_row(const ListArgs &a, int job, int i, unsigned *bm) {
 }
 
 __global__ void __launch_bounds__(512) k_list_scan(ListArgs a) {
-    const int job = blockIdx.x;
+    if ((int)blockIdx.x >= *a.rb_count) return;
+    const int job = a.rb_jobs[blockIdx.x];
     const int sid = a.job_sys[job], bead = a.job_bead[job];
     const SysDev &S = a.sys[sid];
-    if (!a.flag[S.job_base + bead]) return;
     const int N = S.n_mols;
     extern __shared__ int cnt[];
     __shared__ int wtot[33];
@@ -368,6 +370,7 @@ void init_list_kernel_attributes() {
 void launch_skin_rebuild(const ListArgs &a, cudaStream_t s, unsigned long long *launches) {
     if (a.n_jobs <= 0) return;
     const int W = (a.max_mols + 31) / 32;
+    cudaMemsetAsync(a.rb_count, 0, sizeof(int), s);
     k_skin_test<<<a.n_jobs, 256, (size_t)LC_MAX_CELLS * sizeof(int), s>>>(a);
     const int row_blocks = (a.max_mols + ROWS - 1) / ROWS;
     const long long items = (long long)row_blocks * a.n_jobs;

@@ -596,7 +596,8 @@ struct ListArgs {
     int force_rebuild;  // 1: rebuild unconditionally (initial build / per-call API)
     int max_mols;
     // build scratch, indexed like point (pt_off + bead N) unless noted
-    int *flag;          // per base job: 1 while a rebuild of that bead is under way this launch
+    int *rb_jobs;       // the launch's rebuilding jobs (launch-local indices), rb_count of them
+    int *rb_count;      // zeroed before every launch
     float4 *wpos;       // oxygen positions wrapped into the box (FP32)
     int *cnt_half, *cnt_full;  // per-row neighbour counts
     int *cell_start;    // per bead lc_cells + 1 (lc_off)
