@@ -1057,43 +1057,23 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
         if (d.propagator == QTG_SUZUKI_CHIN && P > 1) ctx->any_sc = true;
     }
     // Structure-factor groups: runs of <= kz |kz| values of one column (each |kz|
-    // standing for +kz and -kz), one thread each, 128 threads a block; a thread
-    // stops at its group's last |kz| and the groups are sorted by size, so warps
-    // run groups of one size. The width is the one whose launch does the least
-    // work by a simple model: whole blocks of threads, each paying the column
-    // factor once a site (~7 instructions; mixed ~8) and ~9 a |kz| (mixed, the
-    // three-multiplication form: ~5). Widths 6 and 8 (the column factor shared by
-    // more |kz|, more registers a thread) only for mixed contexts without
-    // Suzuki-Chin systems, whose derivative jobs keep 3 or 4; QTG_KSK_GROUP
-    // (3, 4, 6, 8) fixes the width.
+    // standing for +kz and -kz), one thread each, 128 threads a block. The width
+    // (3 or 4) is the one whose launch does less work by a simple model: whole
+    // blocks of threads, each paying the column factor (~7 instructions a site) and
+    // ~9 a |kz| (mixed, the three-multiplication form: ~8 and ~5), over every
+    // system's half set, sites and beads.
     {
         const double per_col = ctx->mixed ? 8.0 : 7.0, per_kz = ctx->mixed ? 5.0 : 9.0;
-        const int widths[4] = {3, 4, 6, 8};
-        const int n_w = (ctx->mixed && !ctx->any_sc) ? 4 : 2;
-        double best = 0.0;
-        ctx->kz = 3;
+        double cost[2] = {0.0, 0.0};
         for (int w = 0; w < 2; ++w) {
-            const int kz = widths[w];
-            double cost = 0.0;
+            const int kz = 3 + w;
             for (const SysDev &S : ctx->sys_h) {
-                long long g = 0, work = 0;
-                for (int c = 0; c < S.n_col_half; ++c) {
-                    const int m = call[S.col_off + c].m;
-                    g += (m + kz) / kz;
-                    work += (long long)((m + kz) / kz) * per_col + (long long)(m + 1) * per_kz;
-                }
-                // idle lanes of the last block
-                cost += ((double)work + (double)((g + 127) / 128 * 128 - g) * per_col) * S.n_sites * S.n_beads;
-            }
-            if (w == 0 || cost < best) {
-                best = cost;
-                ctx->kz = kz;
+                long long g = 0;
+                for (int c = 0; c < S.n_col_half; ++c) g += (call[S.col_off + c].m + kz) / kz;
+                cost[w] += (double)((g + 127) / 128 * 128) * (per_col + per_kz * kz) * S.n_sites * S.n_beads;
             }
         }
-        if (const char *e = getenv("QTG_KSK_GROUP")) {
-            const int v = atoi(e);
-            if (v == 3 || v == 4 || ((v == 6 || v == 8) && n_w == 4)) ctx->kz = v;
-        }
+        ctx->kz = cost[0] < cost[1] ? 3 : 4;
         for (SysDev &S : ctx->sys_h) {
             S.grp_off = (int)gall.size();
             for (int c = 0; c < S.n_col; ++c) {
@@ -1110,11 +1090,6 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
             }
             S.n_grp = (int)gall.size() - S.grp_off;
             if (S.n_col_half == S.n_col) S.n_grp_half = S.n_grp;
-            // larger groups first (the half set and the rest separately): a warp's
-            // threads stop at the same |kz|
-            auto by_size = [](const KGroup &x, const KGroup &y) { return x.n > y.n; };
-            std::stable_sort(gall.begin() + S.grp_off, gall.begin() + S.grp_off + S.n_grp_half, by_size);
-            std::stable_sort(gall.begin() + S.grp_off + S.n_grp_half, gall.end(), by_size);
             ctx->max_grp = std::max(ctx->max_grp, S.n_grp);
         }
     }

@@ -790,7 +790,6 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
                 const float ps = (float)(pr + pi);
 #pragma unroll
                 for (int g = 0; g < KZ; ++g) {
-                    if (g >= G.n) break;  // a short group (groups are sorted by size: warp-uniform)
                     const V2<R> z = tab_c[zrow[g] + c];
                     sr[g][0] = fmaf((float)pr, (float)z.x, sr[g][0]);  // T1
                     sr[g][1] = fmaf((float)pi, (float)z.y, sr[g][1]);  // T2
@@ -842,8 +841,7 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
             for (int c = 0; c < nc; ++c) site(c);
         }
 #pragma unroll
-        for (int g = 0; g < KZ; ++g) {
-            if (G3 && g >= G.n) break;
+        for (int g = 0; g < KZ; ++g)
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 kahan_add(Sr[g][h], Cr[g][h], sr[g][h]);
@@ -853,7 +851,6 @@ __global__ void __launch_bounds__(KT) k_ksk(EvalArgs a) {
                     kahan_add(dSi[g][h], dCi[g][h], dsi[g][h]);
                 }
             }
-        }
     }
     if (act) {
 #pragma unroll
@@ -1245,18 +1242,6 @@ size_t ksk_smem(int kmax);
 // k_ksk for the context's structure-factor group width
 template <typename R, int MODE>
 void launch_ksk(const EvalArgs &a, dim3 grid, cudaStream_t s) {
-    // groups wider than 4 are built only for mixed contexts without derivative
-    // (Suzuki-Chin) jobs, whose only structure-factor launches are this form's
-    if constexpr (sizeof(R) == 4 && MODE == 0) {
-        if (a.kz == 6) {
-            k_ksk<float, 0, 6><<<grid, KT, ksk_smem<float>(a.max_kmax), s>>>(a);
-            return;
-        }
-        if (a.kz == 8) {
-            k_ksk<float, 0, 8><<<grid, KT, ksk_smem<float>(a.max_kmax), s>>>(a);
-            return;
-        }
-    }
     if (a.kz == 3) k_ksk<R, MODE, 3><<<grid, KT, ksk_smem<R>(a.max_kmax), s>>>(a);
     else k_ksk<R, MODE, 4><<<grid, KT, ksk_smem<R>(a.max_kmax), s>>>(a);
 }
@@ -1973,10 +1958,6 @@ void set_attrs() {
     cudaFuncSetAttribute(k_ksk<R, 1, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_ksk<R, 0, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_ksk<R, 1, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    if (sizeof(R) == 4) {  // the mixed energy/force form's wider groups
-        cudaFuncSetAttribute(k_ksk<float, 0, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-        cudaFuncSetAttribute(k_ksk<float, 0, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    }
     cudaFuncSetAttribute(k_kforce<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_kforce<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
 }
