@@ -1142,17 +1142,15 @@ __global__ void __launch_bounds__(FT) k_kforce_f32(EvalArgs a) {
     __shared__ float4 P1[KB], P2[KB];
     __shared__ int4 cs[KB];      // kx, ky, m, packed slot of kz = 0
     __shared__ float2 cb[KB];    // b_x kx, b_y ky
-    extern __shared__ float2 xrow[];  // [km1][NS]: this block's sites' X(0 .. k_max)
+    extern __shared__ float2 xyrow[];  // [2 km1][NS]: this block's sites' X(0 .. k_max), Y(0 .. k_max)
     const float2 *ph = reinterpret_cast<const float2 *>(a.phase) + J.phase_off;
-    // the sites' Y rows are read through the L1 cache (each |ky| row serves every
-    // column of that |ky| in a batch), which halves the block's shared memory
     int site[SPT];
     float2 z[SPT][ZM];
 #pragma unroll
     for (int u = 0; u < SPT; ++u) {
         site[u] = blockIdx.x * NS + u * FT + threadIdx.x;
         const int ii = site[u] < ns ? site[u] : 0;
-        for (int r = 0; r < km1; ++r) xrow[r * NS + u * FT + threadIdx.x] = ph[(size_t)r * ns + ii];
+        for (int r = 0; r < 2 * km1; ++r) xyrow[r * NS + u * FT + threadIdx.x] = ph[(size_t)r * ns + ii];
 #pragma unroll
         for (int az = 1; az <= ZM; ++az) {
             z[u][az - 1] = make_float2(0.f, 0.f);
@@ -1190,9 +1188,8 @@ __global__ void __launch_bounds__(FT) k_kforce_f32(EvalArgs a) {
             float pr[SPT], pi[SPT], u1[SPT], u2[SPT], u3[SPT], u4[SPT];
 #pragma unroll
             for (int u = 0; u < SPT; ++u) {
-                const float2 x = xrow[C.x * NS + u * FT + threadIdx.x];
-                const int su = site[u] < ns ? site[u] : 0;
-                const float2 y = __ldg(ph + (size_t)(km1 + abs(C.y)) * ns + su);
+                const float2 x = xyrow[C.x * NS + u * FT + threadIdx.x];
+                const float2 y = xyrow[(km1 + abs(C.y)) * NS + u * FT + threadIdx.x];
                 const float yi = C.y < 0 ? -y.y : y.y;
                 pr[u] = x.x * y.x - x.y * yi;
                 pi[u] = x.x * yi + x.y * y.x;
@@ -1252,11 +1249,10 @@ void launch_ksk(const EvalArgs &a, dim3 grid, cudaStream_t s) {
 // the FP32 k-force kernel for the largest |kz| of the batch (the general form beyond 32)
 void launch_kforce_f32(const EvalArgs &a, dim3 grid, cudaStream_t s) {
     // two sites a thread (the block covers 2 FT sites: grid.x halves)
-    const size_t sm = (size_t)(a.max_kmax + 1) * 2 * FT * sizeof(float2);
+    const size_t sm = (size_t)2 * (a.max_kmax + 1) * 2 * FT * sizeof(float2);
     dim3 g2 = grid;
     g2.x = (grid.x + 1) / 2;
     if (a.kpk && a.max_kmax <= 8) launch_pdl(k_kforce_f32<8, 2>, g2, dim3(FT), sm, s, a);
-    else if (a.kpk && a.max_kmax <= 10) launch_pdl(k_kforce_f32<10, 2>, g2, dim3(FT), sm, s, a);
     else if (a.kpk && a.max_kmax <= 12) launch_pdl(k_kforce_f32<12, 2>, g2, dim3(FT), sm, s, a);
     else if (a.kpk && a.max_kmax <= 16) launch_pdl(k_kforce_f32<16, 2>, g2, dim3(FT), sm, s, a);
     else if (a.kpk && a.max_kmax <= 24) launch_pdl(k_kforce_f32<24, 2>, g2, dim3(FT), sm, s, a);
@@ -1954,7 +1950,6 @@ template <typename R>
 void set_attrs() {
     const int big = 200 * 1024;
     cudaFuncSetAttribute(k_kforce_f32<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(k_kforce_f32<10, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_kforce_f32<12, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_kforce_f32<16, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     cudaFuncSetAttribute(k_kforce_f32<24, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
