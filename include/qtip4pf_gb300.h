@@ -391,6 +391,16 @@ qtg_status qtg_transfer_bytes(qtg_ctx *ctx, unsigned long long *h2d, unsigned lo
 qtg_status qtg_autotune(qtg_ctx *ctx, int iters, double *ms_heuristic, double *ms_tuned);
 qtg_status qtg_set_tuning(qtg_ctx *ctx, int n_rj, int n_sc, int n_kc);
 qtg_status qtg_get_tuning(qtg_ctx *ctx, int *n_rj, int *n_sc, int *n_kc);
+/* Real-space form of the mixed precision (no reference counterpart; the reference
+ * visits every site pair, forces.cpp:589-608). In contexts whose beads are too
+ * large for the half-interaction kernel (more than 2048 charge sites) and whose
+ * boxes satisfy r_c + 6 bohr <= L/2 ("list eligible"), form 0 (the default) finds
+ * the site pairs within r_c through a per-configuration list of molecule pairs
+ * (rebuilt by a site displacement test with a 2 bohr skin); form 1 evaluates every
+ * site pair. Both give the same pair set. qtg_autotune keeps the faster form of
+ * an eligible context. A changed form takes effect at the next step graph capture. */
+qtg_status qtg_set_real_space(qtg_ctx *ctx, int form);
+qtg_status qtg_get_real_space(qtg_ctx *ctx, int *form, int *list_eligible);
 
 #ifdef __cplusplus
 }

@@ -130,6 +130,8 @@ def load(build_if_missing: bool = True):
         "qtg_get_centroid_force": ([V, C.c_int, D, D], C.c_int),
         "qtg_set_tuning": ([V, C.c_int, C.c_int, C.c_int], C.c_int),
         "qtg_get_tuning": ([V, I, I, I], C.c_int),
+        "qtg_set_real_space": ([V, C.c_int], C.c_int),
+        "qtg_get_real_space": ([V, I, I], C.c_int),
         "qtg_kwald_noalloc": ([V, V, C.c_int, D, C.c_double, V, V, V], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -235,6 +237,16 @@ class Context:
         a, b, c = C.c_int(0), C.c_int(0), C.c_int(0)
         self.check(self.L.qtg_get_tuning(self.h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
+
+    def set_real_space(self, form):
+        """Mixed real space of large beads: 0 over the pair list (where eligible), 1 over all pairs."""
+        self.check(self.L.qtg_set_real_space(self.h, int(form)))
+
+    def real_space(self):
+        """(form, list_eligible) of the context's mixed real space."""
+        a, b = C.c_int(0), C.c_int(0)
+        self.check(self.L.qtg_get_real_space(self.h, C.byref(a), C.byref(b)))
+        return a.value, bool(b.value)
 
     def run_steps(self, n_steps, is_nvt=True):
         self.check(self.L.qtg_run_steps(self.h, int(n_steps), 1 if is_nvt else 0))

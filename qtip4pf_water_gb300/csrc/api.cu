@@ -222,6 +222,14 @@ struct qtg_ctx {
     float4 *ljf = nullptr;    // dense LJ oxygen forces per molecule and slot
     float *intra = nullptr;   // intramolecular forces, 18 floats per molecule and slot
     int4 *sites_fix = nullptr;  // fixed-point site fractions per slot (half-interaction real space)
+    // real-space pair list (mixed contexts with beads beyond the half-interaction
+    // kernel in boxes with r_c + 2 RL_SPREAD <= L/2): rl_ok marks the context
+    // eligible, rl_form 0 runs the real space over the list there, 1 over all pairs
+    bool rl_ok = false;
+    int rl_form = 0, rl_cap = 0;
+    unsigned short *rl_list = nullptr;
+    int *rl_cnt = nullptr, *rl_jobs = nullptr, *rl_count = nullptr, *rl_wide = nullptr;
+    float4 *rl_ref = nullptr;
     std::string err;
     Consts K;
     std::vector<qtg_system_desc> desc;
@@ -400,6 +408,14 @@ EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, d
     a.tune_rj = c->tune[0];
     a.tune_sc = c->tune[1];
     a.tune_kc = c->tune[2];
+    a.rl_on = (c->rl_ok && c->rl_form == 0) ? 1 : 0;
+    a.rl_cap = c->rl_cap;
+    a.rl_list = c->rl_list;
+    a.rl_cnt = c->rl_cnt;
+    a.rl_ref = c->rl_ref;
+    a.rl_jobs = c->rl_jobs;
+    a.rl_count = c->rl_count;
+    a.rl_wide = c->rl_wide;
     a.c = c->K;
     return a;
 }
@@ -691,6 +707,8 @@ qtg_status status_error(qtg_ctx *ctx, unsigned st) {
         if (st & ST_GAMMA_LIMIT) return fail(ctx, QTG_ERR_NONFINITE, "gamma variate iteration limit reached");
         if (st & ST_DESC_OVERFLOW) return fail(ctx, QTG_ERR_ARG, "more than 256 atoms within the descriptor cutoff");
         if (st & ST_MMA_TIMEOUT) return fail(ctx, QTG_ERR_CUDA, "tensor-core completion wait ran out");
+        if (st & ST_RLIST_OVERFLOW)
+            return fail(ctx, QTG_ERR_LIST_OVERFLOW, "real-space pair list row exceeded its capacity");
     }
     return QTG_OK;
 }
@@ -1261,6 +1279,31 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->ljf, ctx->total_sites / 3);
     AL(ctx->intra, 6 * ctx->total_sites);
     AL(ctx->sites_fix, ctx->total_sites);
+    {
+        // real-space pair list: rows hold the molecules whose M sites lie within
+        // r_c + RL_SKIN + 2 RL_SPREAD (the prefilter radius of k_rlist_rows), at the
+        // mean density and 15 % above it, plus 32
+        ctx->rl_ok = ctx->mixed && (3 * ctx->max_mols + 31) / 32 > HALF_MAX_TILES;
+        for (const SysDev &S : ctx->sys_h) {
+            const double rc = sqrt(S.rc_sq), min_box = std::min(std::min(S.box[0], S.box[1]), S.box[2]);
+            if (rc + 2.0 * RL_SPREAD > 0.5 * min_box || S.n_mols > 65535) ctx->rl_ok = false;
+            const double R = rc + RL_SKIN + 2.0 * RL_SPREAD;
+            const double nb = 1.15 * (4.0 / 3.0) * PI_REF * R * R * R * S.n_mols / (S.box[0] * S.box[1] * S.box[2]);
+            const int cap = std::min(S.n_mols - 1, (int)std::ceil(nb) + 32);
+            ctx->rl_cap = std::max(ctx->rl_cap, (cap + 7) / 8 * 8);
+        }
+        if (ctx->rl_ok) {
+            const size_t n_jobs_max = std::max(std::max(ctx->base.h.size(), ctx->fd.h.size()), ctx->tan.h.size());
+            AL(ctx->rl_list, (ctx->total_sites / 3) * (size_t)ctx->rl_cap);
+            AL(ctx->rl_cnt, ctx->total_sites / 3);
+            AL(ctx->rl_ref, ctx->total_sites);
+            AL(ctx->rl_jobs, n_jobs_max);
+            AL(ctx->rl_count, 1);
+            AL(ctx->rl_wide, ctx->total_slots);
+            // NaN reference positions: the first evaluation of every slot builds its list
+            if (e == cudaSuccess) e = cudaMemset(ctx->rl_ref, 0xff, sizeof(float4) * ctx->total_sites);
+        }
+    }
     AL(ctx->part, (size_t)MAX_PART * 3 * ctx->total_sites);
     AL(ctx->skp, (size_t)MAX_SC * ctx->total_k);
     AL(ctx->dskp, (size_t)MAX_SC * ctx->total_k);
@@ -1381,7 +1424,7 @@ void qtg_destroy(qtg_ctx *ctx) {
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
                     ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf, ctx->fin_ticket, ctx->sites_fix, ctx->intra, ctx->kfc, ctx->kfb, ctx->wpk,
                     ctx->wpos, ctx->cnt_half, ctx->cnt_full, ctx->cell_start, ctx->cell_mol,
-                    ctx->rb_jobs, ctx->rb_count};
+                    ctx->rb_jobs, ctx->rb_count, ctx->rl_list, ctx->rl_cnt, ctx->rl_ref, ctx->rl_jobs, ctx->rl_count, ctx->rl_wide};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->box) cudaFreeHost(ctx->box);
@@ -2347,6 +2390,20 @@ qtg_status qtg_get_tuning(qtg_ctx *ctx, int *n_rj, int *n_sc, int *n_kc) {
     return QTG_OK;
 }
 
+qtg_status qtg_set_real_space(qtg_ctx *ctx, int form) {
+    if (!ctx || form < 0 || form > 1) return fail(ctx, QTG_ERR_ARG, "real-space form must be 0 (pair list) or 1 (all pairs)");
+    ctx->rl_form = form;
+    drop_graphs(ctx);
+    return QTG_OK;
+}
+
+qtg_status qtg_get_real_space(qtg_ctx *ctx, int *form, int *list_eligible) {
+    if (!ctx || !form || !list_eligible) return QTG_ERR_ARG;
+    *form = ctx->rl_form;
+    *list_eligible = ctx->rl_ok ? 1 : 0;
+    return QTG_OK;
+}
+
 qtg_status qtg_transfer_bytes(qtg_ctx *ctx, unsigned long long *h2d, unsigned long long *d2h) {
     if (!ctx || !h2d || !d2h) return QTG_ERR_ARG;
     *h2d = ctx->h2d_bytes;
@@ -2375,6 +2432,17 @@ qtg_status qtg_autotune(qtg_ctx *ctx, int iters, double *ms_heuristic, double *m
     static const int cand_sc[] = {0, 1, 2, 4, 6, 8, 12, 16, 24, 32};  // k_ksk
     int best[3] = {0, 0, 0};
     double best_ms = 0.0;
+    if (ctx->rl_ok) {
+        // the real-space form first (pair list or all pairs, heuristic counts); the
+        // list's first evaluation builds it, the timed ones find it valid
+        double ms_form[2];
+        for (int f = 0; f < 2; ++f) {
+            ctx->rl_form = f;
+            CKS(eval_ms(best, &ms_form[f]));
+            CKS(eval_ms(best, &ms_form[f]));
+        }
+        ctx->rl_form = ms_form[1] < ms_form[0] ? 1 : 0;
+    }
     CKS(eval_ms(best, &best_ms));  // fills the scratch arrays, warms the kernels
     CKS(eval_ms(best, &best_ms));
     for (int sweep = 0; sweep < 2; ++sweep) {

@@ -239,7 +239,17 @@ __global__ void __launch_bounds__(128) k_prep_f32(EvalArgs a) {
     }
     const unsigned F = (unsigned)__double2ll_rn(x * S.fix_scale[d]);
     float *sv = reinterpret_cast<float *>(a.sites) + 4 * ((size_t)J.site_off + s);
-    sv[d] = (float)F * S.fixf[d];
+    float xf = (float)F * S.fixf[d];
+    if (!a.sites_are_input && kind != 0) {
+        // an H site follows its molecule's wrapped M site across the box boundary
+        // (the wrapped fixed-point difference is the M-H minimum image), so the
+        // FP32 positions of a molecule's sites stay together: one minimum image per
+        // molecule pair serves all nine site pairs in k_real_list
+        const double xm = fma(g, q[9 * mol + d], h * (q[9 * mol + 3 + d] + q[9 * mol + 6 + d]));
+        const unsigned FM = (unsigned)__double2ll_rn(xm * S.fix_scale[d]);
+        xf = fmaf((float)(int)(F - FM), S.fixf[d], (float)FM * S.fixf[d]);
+    }
+    sv[d] = xf;
     int *fx = reinterpret_cast<int *>(a.sites_fix + J.site_off + s);
     fx[d] = (int)F;
     float cf = 1.f;
@@ -457,6 +467,278 @@ __global__ void __launch_bounds__(RT) k_real_f32(EvalArgs a) {
                            si.w * (Sy - Cy), si.w * (Sz - Cz));
     const double t = block_sum(0.5 * qi * ((double)Se - (double)Ce), red);
     if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], t);
+}
+
+// ---- real-space pair list (mixed form, beads beyond the half-interaction kernel) ----
+// The reference's real-space sum (forces.cpp:589-608) visits every site pair of
+// different molecules and keeps those within r_c. For large beads the pairs
+// within r_c are found through a list per (slot) configuration: row i holds, in
+// ascending order, every molecule j != i that had a site pair within r_c + RL_SKIN
+// when the list was built. The list stays complete while no two sites have moved
+// by more than RL_SKIN between them since the build, the Verlet argument of
+// neighbour.cpp applied to sites: k_rlist_test rebuilds it when the two largest
+// site displacements sum to more than the skin (or were never measured).
+// k_prep_f32 keeps a molecule's FP32 sites together (H sites follow the wrapped M
+// site). While every site lies within RL_SPREAD of its M site and r_c +
+// 2 RL_SPREAD <= L/2 (the context's eligibility test), the M-M minimum image of a
+// molecule pair is the minimum image of each of its site pairs within r_c, so one
+// image serves nine pairs; a configuration with a wider molecule ("wide", found by
+// k_rlist_test) takes a minimum image per site pair instead, in the build and in
+// the force sum.
+constexpr int RL_ROWS = 8;  // rows (warps) per block of k_rlist_rows
+constexpr int RLW = 4;      // molecules (warps) per block of k_real_list
+
+struct RlBox {
+    float L0, L1, L2, I0, I1, I2;
+};
+__device__ __forceinline__ RlBox rl_box(const SysDev &S) {
+    return {S.boxf[0], S.boxf[1], S.boxf[2], S.inv_boxf[0], S.inv_boxf[1], S.inv_boxf[2]};
+}
+// minimum image of a difference vector
+__device__ __forceinline__ void rl_image(const RlBox &B, float &dx, float &dy, float &dz) {
+    dx = fmaf(-B.L0, rintf(dx * B.I0), dx);
+    dy = fmaf(-B.L1, rintf(dy * B.I1), dy);
+    dz = fmaf(-B.L2, rintf(dz * B.I2), dz);
+}
+
+// Block per job: the list's validity (two largest site displacements since the
+// build, compared as the bit patterns of their non-negative squares, a NaN above
+// all) and the spread of the molecules; a rebuilding job joins the launch's list
+// of rebuilding jobs and records the positions of the build.
+__global__ void __launch_bounds__(256) k_rlist_test(EvalArgs a) {
+    const Job J = a.jobs[blockIdx.x];
+    const SysDev &S = a.sys[J.sys];
+    const int ns = S.n_sites;
+    const float4 *sites = reinterpret_cast<const float4 *>(a.sites) + J.site_off;
+    float4 *ref = a.rl_ref + J.site_off;
+    const RlBox B = rl_box(S);
+    constexpr float sp2 = RL_SPREAD * RL_SPREAD;
+    unsigned m1 = 0u, m2 = 0u;
+    int wide = 0;
+    for (int k = threadIdx.x; k < ns; k += blockDim.x) {
+        const float4 p = sites[k], r = ref[k];
+        float dx = p.x - r.x, dy = p.y - r.y, dz = p.z - r.z;
+        rl_image(B, dx, dy, dz);
+        const unsigned d2 = __float_as_uint(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+        if (d2 > m1) {
+            m2 = m1;
+            m1 = d2;
+        } else if (d2 > m2) {
+            m2 = d2;
+        }
+        const int kind = k % 3;
+        if (kind) {
+            const float4 m = sites[k - kind];
+            const float hx = p.x - m.x, hy = p.y - m.y, hz = p.z - m.z;
+            if (!(fmaf(hx, hx, fmaf(hy, hy, hz * hz)) <= sp2)) wide = 1;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned b1 = __shfl_xor_sync(0xffffffffu, m1, o), b2 = __shfl_xor_sync(0xffffffffu, m2, o);
+        const unsigned n1 = max(m1, b1), n2 = max(min(m1, b1), max(m2, b2));
+        m1 = n1;
+        m2 = n2;
+    }
+    __shared__ unsigned red[2][8];
+    __shared__ int build;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        red[0][w] = m1;
+        red[1][w] = m2;
+    }
+    wide = __syncthreads_or(wide);
+    if (threadIdx.x == 0) {
+        unsigned t1 = 0u, t2 = 0u;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+            const unsigned n1 = max(t1, red[0][k]), n2 = max(min(t1, red[0][k]), max(t2, red[1][k]));
+            t1 = n1;
+            t2 = n2;
+        }
+        build = !(sqrtf(__uint_as_float(t1)) + sqrtf(__uint_as_float(t2)) <= RL_SKIN);
+        a.rl_wide[J.slot] = wide;
+        if (build) a.rl_jobs[atomicAdd(a.rl_count, 1)] = blockIdx.x;
+    }
+    __syncthreads();
+    if (!build) return;
+    for (int k = threadIdx.x; k < ns; k += blockDim.x) ref[k] = sites[k];
+}
+
+// Whether some site pair of molecules (a0, a1, a2) and (b0, b1, b2) lies within
+// R (R2 = R^2). Not WIDE: the M-M image for all nine pairs, after an M-M
+// prefilter at R + 2 RL_SPREAD (P2); WIDE: a minimum image per pair.
+template <bool WIDE>
+__device__ __forceinline__ bool rl_near(const float4 *sites, int j, const float4 &a0, const float4 &a1,
+                                        const float4 &a2, const RlBox &B, float R2, float P2) {
+    const float4 b0 = sites[3 * j];
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    if (!WIDE) {
+        sx = B.L0 * rintf((a0.x - b0.x) * B.I0);
+        sy = B.L1 * rintf((a0.y - b0.y) * B.I1);
+        sz = B.L2 * rintf((a0.z - b0.z) * B.I2);
+        const float dx = a0.x - sx - b0.x, dy = a0.y - sy - b0.y, dz = a0.z - sz - b0.z;
+        if (!(fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < P2)) return false;
+    }
+    const float4 b1 = sites[3 * j + 1], b2 = sites[3 * j + 2];
+    const float4 ai[3] = {a0, a1, a2}, bj[3] = {b0, b1, b2};
+    float m = 3.4e38f;
+#pragma unroll
+    for (int u = 0; u < 3; ++u)
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {
+            float ex = ai[u].x - sx - bj[v].x, ey = ai[u].y - sy - bj[v].y, ez = ai[u].z - sz - bj[v].z;
+            if (WIDE) rl_image(B, ex, ey, ez);
+            m = fminf(m, fmaf(ex, ex, fmaf(ey, ey, ez * ez)));
+        }
+    return m < R2;
+}
+
+// Rows of the rebuilding jobs' lists, a warp per row i over a fixed grid of
+// (rebuilding job, RL_ROWS rows) items: the 32 lanes test 32 molecules j at a
+// time and a ballot places the hits in ascending j.
+__global__ void __launch_bounds__(32 * RL_ROWS) k_rlist_rows(EvalArgs a, int row_blocks) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long n_items = (long long)(*a.rl_count) * row_blocks;
+    for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const Job J = a.jobs[a.rl_jobs[it / row_blocks]];
+        const SysDev &S = a.sys[J.sys];
+        const int N = S.n_mols, i = (int)(it % row_blocks) * RL_ROWS + w;
+        if (i >= N) continue;
+        const float4 *sites = reinterpret_cast<const float4 *>(a.sites) + J.site_off;
+        const RlBox B = rl_box(S);
+        const float R = sqrtf(S.rc_sqf) + RL_SKIN, R2 = R * R;
+        const float P = R + 2.0f * RL_SPREAD, P2 = P * P;
+        const bool wide = a.rl_wide[J.slot] != 0;
+        const float4 a0 = sites[3 * i], a1 = sites[3 * i + 1], a2 = sites[3 * i + 2];
+        unsigned short *row = a.rl_list + ((size_t)J.site_off / 3 + i) * a.rl_cap;
+        int cnt = 0;
+        for (int j0 = 0; j0 < N; j0 += 32) {
+            const int j = j0 + lane;
+            bool hit = false;
+            if (j < N && j != i)
+                hit = wide ? rl_near<true>(sites, j, a0, a1, a2, B, R2, P2)
+                           : rl_near<false>(sites, j, a0, a1, a2, B, R2, P2);
+            const unsigned bal = __ballot_sync(0xffffffffu, hit);
+            if (hit) {
+                const int at = cnt + __popc(bal & ((1u << lane) - 1u));
+                if (at < a.rl_cap) row[at] = (unsigned short)j;
+            }
+            cnt += __popc(bal);
+        }
+        if (lane == 0) {
+            a.rl_cnt[(size_t)J.site_off / 3 + i] = min(cnt, a.rl_cap);
+            if (cnt > a.rl_cap) atomicOr(a.status, (unsigned)ST_RLIST_OVERFLOW);
+        }
+    }
+}
+
+// One site pair of k_real_list: the FP32 pair term of k_real_f32 with the
+// cutoff applied through the j charge (branch-free), accumulated into the i
+// site's sums; MI: the difference vector takes its own minimum image.
+struct RlPair {
+    float rc2, ka, cex, pref;
+};
+template <bool MI>
+__device__ __forceinline__ void rl_pair(float ax, float ay, float az, const float4 b, const RlBox &B,
+                                        const RlPair &K, float &fx, float &fy, float &fz, float &e) {
+    float dx = ax - b.x, dy = ay - b.y, dz = az - b.z;
+    if (MI) rl_image(B, dx, dy, dz);
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float iv = rsqrt_approx(r2);
+    const float ex = ex2_approx(K.cex * r2);
+    const float t = rcp_approx(fmaf(K.ka, r2 * iv, 1.0f));
+    const float A = (t * as_poly(t)) * ex * iv;
+    const float qb = r2 < K.rc2 ? b.w : 0.0f;
+    const float wq = qb * fmaf(K.pref, ex, A) * (iv * iv);
+    e = fmaf(qb, A, e);
+    fx = fmaf(wq, dx, fx);
+    fy = fmaf(wq, dy, fy);
+    fz = fmaf(wq, dz, fz);
+}
+
+// A lane's share of row i in k_real_list: listed molecules lo + lane, lo + lane
+// + 32, ... below hi; nine site pairs each (WIDE: a minimum image per pair, else
+// the i sites shifted by the M-M image once per j).
+template <bool WIDE>
+__device__ __forceinline__ void rl_row(const float4 *sites, const unsigned short *row, int lo, int hi,
+                                       const float4 &a0, const float4 &a1, const float4 &a2, const RlBox &B,
+                                       const RlPair &K, float (&f)[9], float &e0, float &e1, float &e2) {
+    for (int k = lo + (threadIdx.x & 31); k < hi; k += 32) {
+        const int j = row[k];
+        const float4 b0 = __ldg(sites + 3 * j), b1 = __ldg(sites + 3 * j + 1), b2 = __ldg(sites + 3 * j + 2);
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+        if (!WIDE) {
+            sx = B.L0 * rintf((a0.x - b0.x) * B.I0);
+            sy = B.L1 * rintf((a0.y - b0.y) * B.I1);
+            sz = B.L2 * rintf((a0.z - b0.z) * B.I2);
+        }
+        const float x0 = a0.x - sx, y0 = a0.y - sy, z0 = a0.z - sz;
+        const float x1 = a1.x - sx, y1 = a1.y - sy, z1 = a1.z - sz;
+        const float x2 = a2.x - sx, y2 = a2.y - sy, z2 = a2.z - sz;
+        rl_pair<WIDE>(x0, y0, z0, b0, B, K, f[0], f[1], f[2], e0);
+        rl_pair<WIDE>(x0, y0, z0, b1, B, K, f[0], f[1], f[2], e0);
+        rl_pair<WIDE>(x0, y0, z0, b2, B, K, f[0], f[1], f[2], e0);
+        rl_pair<WIDE>(x1, y1, z1, b0, B, K, f[3], f[4], f[5], e1);
+        rl_pair<WIDE>(x1, y1, z1, b1, B, K, f[3], f[4], f[5], e1);
+        rl_pair<WIDE>(x1, y1, z1, b2, B, K, f[3], f[4], f[5], e1);
+        rl_pair<WIDE>(x2, y2, z2, b0, B, K, f[6], f[7], f[8], e2);
+        rl_pair<WIDE>(x2, y2, z2, b1, B, K, f[6], f[7], f[8], e2);
+        rl_pair<WIDE>(x2, y2, z2, b2, B, K, f[6], f[7], f[8], e2);
+    }
+}
+
+// Real-space Ewald over the pair list (energies and forces): a warp per
+// (molecule i, chunk rj of its row), a lane per listed molecule j at a time. The
+// warp's sums are reduced by shuffles in a fixed order and written as plane rj
+// (deterministic, no atomics on forces).
+__global__ void __launch_bounds__(32 * RLW) k_real_list(EvalArgs a) {
+    const int rj = blockIdx.y, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const Job J = a.jobs[blockIdx.z];
+    const SysDev &S = a.sys[J.sys];
+    const int N = S.n_mols;
+    if ((int)blockIdx.x * RLW >= N) return;
+    const int i = blockIdx.x * RLW + w;
+    const bool act = i < N;
+    const float4 *sites = reinterpret_cast<const float4 *>(a.sites) + J.site_off;
+    const RlBox B = rl_box(S);
+    const RlPair K = {S.rc_sqf, S.kaf, S.cexf, S.ewald_preff};
+    float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0, a2 = a0;
+    int lo = 0, hi = 0;
+    if (act) {
+        a0 = sites[3 * i];
+        a1 = sites[3 * i + 1];
+        a2 = sites[3 * i + 2];
+        const int c = a.rl_cnt[(size_t)J.site_off / 3 + i];
+        lo = chunk_lo(c, rj, a.n_rj);
+        hi = chunk_lo(c, rj + 1, a.n_rj);
+    }
+    const unsigned short *row = a.rl_list + ((size_t)J.site_off / 3 + i) * a.rl_cap;
+    float f[9], e0 = 0.f, e1 = 0.f, e2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) f[k] = 0.f;
+    if (a.rl_wide[J.slot]) rl_row<true>(sites, row, lo, hi, a0, a1, a2, B, K, f, e0, e1, e2);
+    else rl_row<false>(sites, row, lo, hi, a0, a1, a2, B, K, f, e0, e1, e2);
+    float e = 0.5f * (a0.w * e0 + a1.w * e1 + a2.w * e2);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) f[k] = warp_sum(f[k]);
+    e = warp_sum(e);
+    if (act && lane < 3) {
+        // lane p stores site p (selects: a lane-dependent index into f would go
+        // through local memory)
+        const float q = lane == 0 ? a0.w : (lane == 1 ? a1.w : a2.w);
+        const float fx = lane == 0 ? f[0] : (lane == 1 ? f[3] : f[6]);
+        const float fy = lane == 0 ? f[1] : (lane == 1 ? f[4] : f[7]);
+        const float fz = lane == 0 ? f[2] : (lane == 1 ? f[5] : f[8]);
+        store_plane<float>(a.part, 3 * ((size_t)rj * a.total_sites + J.site_off + 3 * i + lane), q * fx, q * fy,
+                           q * fz);
+    }
+    __shared__ double red[RLW];
+    if (lane == 0) red[w] = act ? (double)e : 0.0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < RLW; ++k) t += red[k];
+        atomicAdd(&a.energy[J.slot], t);
+    }
 }
 
 // Half-interaction form of k_real_f32 (energies and forces, beads of at most
@@ -1995,6 +2277,25 @@ void launch_real_half(EvalArgs &a, cudaStream_t s) {
     k_real_half<<<dim3((T + HW - 1) / HW, n_ch, a.n_jobs), 32 * HW, 0, s>>>(a, n_ch);
 }
 
+// The pair-list real space (mixed, forces, beads beyond the half-interaction
+// kernel, when the context enabled it): its chunk count (planes) per row, sized
+// like the other force kernels' grids; three launches (test, rows, forces).
+bool list_ok(const EvalArgs &a) { return a.rl_on && a.mode == 0 && !half_ok(a); }
+int list_chunks(const EvalArgs &a) {
+    return chunks_or(a.tune_rj, (long long)((a.max_mols + RLW - 1) / RLW) * a.n_jobs, MAX_RJ);
+}
+void launch_real_list(EvalArgs &a, cudaStream_t s) {
+    a.n_rj = list_chunks(a);
+    cudaMemsetAsync(a.rl_count, 0, sizeof(int), s);
+    k_rlist_test<<<a.n_jobs, 256, 0, s>>>(a);
+    const int row_blocks = (a.max_mols + RL_ROWS - 1) / RL_ROWS;
+    // eight resident blocks on each of the 152 SMs at most; a launch without
+    // rebuilds costs each block one load of the count
+    const int grid = (int)std::min<long long>((long long)row_blocks * a.n_jobs, 152LL * 8);
+    k_rlist_rows<<<grid, 32 * RL_ROWS, 0, s>>>(a, row_blocks);
+    k_real_list<<<dim3((a.max_mols + RLW - 1) / RLW, a.n_rj, a.n_jobs), 32 * RLW, 0, s>>>(a);
+}
+
 template <typename R>
 void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks *forks = nullptr) {
     const int ns = 3 * a.max_mols;
@@ -2005,6 +2306,7 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
     if (sizeof(R) == 4 && forks && a.mode == 0 && a.lj_full && a.ljf) {
         // forked: prep; then real space | reciprocal chain | dense LJ; then combine
         if (half_ok(a)) a.n_rj = half_chunks(a) + (3 * a.max_mols + 31) / 32 / 2;
+        else if (list_ok(a)) a.n_rj = list_chunks(a);  // k_kforce_f32's planes follow the real-space ones
         a.lj_plane = 1;
         launch_prep_f32(a, s);
         cudaEventRecord(forks->fork, s);
@@ -2021,18 +2323,22 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
         }
         cudaEventRecord(forks->join[1], forks->side[1]);
         if (half_ok(a)) launch_real_half(a, s);
+        else if (list_ok(a)) launch_real_list(a, s);
         else k_real_f32<<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         cudaStreamWaitEvent(s, forks->join[0], 0);
         cudaStreamWaitEvent(s, forks->join[1], 0);
         k_combine_f32<<<dim3((a.max_mols + CMB - 1) / CMB, a.n_jobs), 128, 0, s>>>(a);
-        if (n) *n += a.intra_plane ? 8 : 7;
+        if (n) *n += (a.intra_plane ? 8 : 7) + (list_ok(a) ? 2 : 0);
         return;
     }
     if constexpr (sizeof(R) == 4) launch_prep_f32(a, s);
     else k_prep<R><<<dim3((ns + 127) / 128, a.n_jobs), 128, 0, s>>>(a);
     if (a.mode == 0) {
         if (sizeof(R) == 4 && half_ok(a)) launch_real_half(a, s);
-        else if (sizeof(R) == 4) k_real_f32<<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
+        else if (sizeof(R) == 4 && list_ok(a)) {
+            launch_real_list(a, s);
+            if (n) *n += 2;
+        } else if (sizeof(R) == 4) k_real_f32<<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         else k_real<R, 0><<<dim3(tiles, a.n_rj, a.n_jobs), RT, 0, s>>>(a);
         launch_ksk<R, 0>(a, dim3(ktiles, a.n_sc, a.n_jobs), s);
         launch_sk_reduce<R, 0>(a, s);
@@ -2090,6 +2396,7 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
         else k_prep<double><<<gs, 128, 0, s>>>(a);
     } else if (n == "real") {
         if (mixed && half_ok(a)) launch_real_half(a, s);
+        else if (mixed && list_ok(a)) launch_real_list(a, s);
         else if (mixed) k_real_f32<<<gr, RT, 0, s>>>(a);
         else k_real<double, 0><<<gr, RT, 0, s>>>(a);
     } else if (n == "ksk") {

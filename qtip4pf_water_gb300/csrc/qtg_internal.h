@@ -168,6 +168,7 @@ enum StatusBits : unsigned {
     ST_GAMMA_LIMIT = 4u,
     ST_DESC_OVERFLOW = 8u,   // an atom had more neighbours within the descriptor cutoff than kept
     ST_MMA_TIMEOUT = 16u,    // a tensor-core completion wait ran out of its iteration limit
+    ST_RLIST_OVERFLOW = 32u, // a real-space pair-list row needed more than rl_cap entries
 };
 
 // ---- device helpers ---------------------------------------------------------
@@ -457,6 +458,12 @@ constexpr int HALF_MAX_TILES = 64;  // half-interaction real space: beads of at 
 constexpr int HALF_MAX_CH = 8;      // its stationary-side chunks
 constexpr int MAX_RPLANES = HALF_MAX_CH + HALF_MAX_TILES / 2 > MAX_RJ ? HALF_MAX_CH + HALF_MAX_TILES / 2 : MAX_RJ;
 constexpr int MAX_PART = MAX_RPLANES + MAX_KC + 1;  // partial site-force planes
+// Real-space pair list (mixed form, beads beyond the half-interaction kernel):
+// the distance from its molecule's M site (bohr) within which every charge site
+// of a configuration must lie for one minimum image per molecule pair to serve
+// its nine site pairs, and the list's skin (bohr).
+constexpr float RL_SPREAD = 3.0f;
+constexpr float RL_SKIN = 2.0f;
 
 struct EvalArgs {
     const SysDev *sys;     // device array
@@ -503,6 +510,13 @@ struct EvalArgs {
     double *energy;        // per slot
     unsigned *status;
     int n_rj, n_sc, n_kc;  // chunk counts, chosen by the launcher
+    // real-space pair list, per slot (rl_on: the mixed real space runs over it)
+    int rl_on, rl_cap;     // rl_cap: entries a row holds
+    unsigned short *rl_list;  // [slot molecule][rl_cap]: molecules j with a site pair within r_c + RL_SKIN at the build
+    int *rl_cnt;           // entries per slot molecule
+    float4 *rl_ref;        // per slot site: the positions the list was built at (NaN: never built)
+    int *rl_jobs, *rl_count;  // the launch's jobs whose list is rebuilt, and their number
+    int *rl_wide;          // per slot: a site lies beyond RL_SPREAD of its M site (minimum image per site pair)
     int tune_rj, tune_sc, tune_kc;  // chunk counts fixed by the autotuner (0: launcher heuristic)
     int sites_are_input;   // 1: positions are charge sites (M,H1,H2) -> reciprocal space only
     int sr_only;           // 1: only the short-range terms (LJ, intramolecular,
