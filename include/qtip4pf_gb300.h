@@ -319,7 +319,7 @@ qtg_status qtg_get_centroid_force(qtg_ctx *ctx, int sys, double *f_mean, double 
 
 /* ---- learned centroid correction (no reference counterpart) ------------------ */
 /* A per-molecule network maps Behler-Parrinello symmetry functions of the
- * molecule's three atoms (G2 and G4 within 6 A, QTG_DESC_PER_ATOM per atom,
+ * molecule's three atoms (G2 and G5 within 6 A, QTG_DESC_PER_ATOM per atom,
  * O H1 H2 concatenated: QTG_MLP_IN inputs) through two hidden layers of
  * QTG_MLP_HIDDEN SiLU units to the centroid-force correction of its three atoms
  * in the molecule's frame (QTG_MLP_OUT values, padded to QTG_MLP_OUT_PAD). It

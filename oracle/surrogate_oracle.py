@@ -2,10 +2,12 @@
 
 FP64 numpy restatement of what qtip4pf_water_gb300/csrc/surrogate.cu computes:
 
-* sym_descriptors  Behler-Parrinello G2 / G4 symmetry functions within 6 A,
-  32 per atom, with the same parameter sets and layout as the device kernel
-  (Behler & Parrinello, Phys. Rev. Lett. 98, 146401 (2007); Behler, J. Chem.
-  Phys. 134, 074106 (2011));
+* sym_descriptors  Behler-Parrinello radial G2 and angular G5 symmetry
+  functions within 6 A, 32 per atom, with the same parameter sets and layout
+  as the device kernel (Behler & Parrinello, Phys. Rev. Lett. 98, 146401
+  (2007); Behler, J. Chem. Phys. 134, 074106 (2011), eq. 27: the angular form
+  without the r_jk terms), here as the explicit sum over neighbour pairs (the
+  device forms the same sums from per-atom moments);
 * mlp_forward / mlp_backward  the per-molecule network 96 -> 64 -> 64 -> 16
   (SiLU), with the device's BF16 rounding of inputs, weights and hidden
   activations emulated and everything else in FP64; the backward pass is the
@@ -22,9 +24,9 @@ import numpy as np
 BOHR_A = 0.529177210903
 RC_A = 6.0
 G2_ETA = np.array([0.001, 0.01, 0.03, 0.06, 0.15, 0.3, 0.7, 1.5])
-G4_ZETA = np.array([1, 1, 2, 2, 1, 1, 2, 2], dtype=np.float64)
-G4_LAMBDA = np.array([1, -1, 1, -1, 1, -1, 1, -1], dtype=np.float64)
-G4_ETA = np.array([0.005] * 4 + [0.02] * 4)
+G5_ZETA = np.array([1, 1, 2, 2, 1, 1, 2, 2], dtype=np.float64)
+G5_LAMBDA = np.array([1, -1, 1, -1, 1, -1, 1, -1], dtype=np.float64)
+G5_ETA = np.array([0.005] * 4 + [0.02] * 4)
 
 
 def fcut(r, rc=RC_A):
@@ -53,19 +55,17 @@ def sym_descriptors(pos_bohr: np.ndarray, box_bohr, rc=RC_A) -> np.ndarray:
         n = len(idx)
         if n < 2:
             continue
+        # G5_i = 2^(1 - zeta) sum_{j < k} (1 + lambda cos theta_jik)^zeta
+        #        exp(-eta (r_ij^2 + r_ik^2)) f_c(r_ij) f_c(r_ik), per pair class
         a, b = np.triu_indices(n, 1)
-        djk = dj[a] - dj[b]
-        rjk = np.sqrt((djk * djk).sum(1))
-        keep = rjk < rc
-        a, b, rjk = a[keep], b[keep], rjk[keep]
         cs = (dj[a] * dj[b]).sum(1) / (rj[a] * rj[b])
-        s2 = rj[a] ** 2 + rj[b] ** 2 + rjk ** 2
-        f3 = fc[a] * fc[b] * fcut(rjk, rc)
+        s2 = rj[a] ** 2 + rj[b] ** 2
+        f2 = fc[a] * fc[b]
         same = sj[a] == sj[b]
         for k in range(8):
-            base = 1.0 + G4_LAMBDA[k] * cs
-            ang = 2.0 ** (1.0 - G4_ZETA[k]) * base ** G4_ZETA[k]
-            v = ang * np.exp(-G4_ETA[k] * s2) * f3
+            base = 1.0 + G5_LAMBDA[k] * cs
+            ang = 2.0 ** (1.0 - G5_ZETA[k]) * base ** G5_ZETA[k]
+            v = ang * np.exp(-G5_ETA[k] * s2) * f2
             out[i, 16 + k] = v[same].sum()
             out[i, 24 + k] = v[~same].sum()
     return out

@@ -217,6 +217,9 @@ struct qtg_ctx {
     // a second stream and fork / join events: inside the captured per-call step, the
     // stage-out of arrays that are final early runs beside the later kernels
     cudaStream_t side_stream = nullptr;
+    // learned corrections: their positions-only part runs on this branch beside the forces
+    cudaStream_t sur_stream = nullptr;
+    cudaEvent_t sur_fork = nullptr, sur_join = nullptr;
     cudaEvent_t ev_fork[2] = {nullptr, nullptr}, ev_join = nullptr;
     Forks forks{};            // branches of a mixed force evaluation (real | k-space | LJ)
     float4 *ljf = nullptr;    // dense LJ oxygen forces per molecule and slot
@@ -552,6 +555,13 @@ ListArgs list_args(qtg_ctx *c, int first_job, int n_jobs, int force) {
     return l;
 }
 
+// Mixed contexts whose beads are beyond the half-interaction real-space kernel,
+// with the stepper's symmetric Verlet lists: the Lennard-Jones term runs over the
+// list (k_lj) instead of every O-O pair (k_lj_dense, O(N^2) a bead).
+bool lj_list_ok(const qtg_ctx *c) {
+    return c->mixed && c->point_full && (3 * c->max_mols + 31) / 32 > HALF_MAX_TILES;
+}
+
 // Forces of the given systems (sys < 0: all): physical forces into fphys, the
 // propagating force into f (SC assembly for SC systems or force_sc; copy for
 // Trotter). Positions are read from q.
@@ -566,6 +576,7 @@ void enqueue_forces(qtg_ctx *c, int sys, bool force_sc) {
     const int full = sys < 0 ? 1 : 0;
     EvalArgs base = eval_args(c, c->base.d + jb, nj, c->q, c->fphys, 0, 0);
     base.lj_full = (full || c->mixed) ? 1 : 0;
+    base.lj_list = (full && lj_list_ok(c)) ? 1 : 0;
     // mixed, second-order assembly for every system in the evaluation: the combine
     // writes the propagating force too, and the assembly kernel is not launched
     bool all_trotter = c->mixed && !force_sc;
@@ -574,8 +585,11 @@ void enqueue_forces(qtg_ctx *c, int sys, bool force_sc) {
     for (const auto &g : c->surrogates)  // a learned correction is added to fphys after the combine
         if (sys < 0 || g.sys == sys) all_trotter = false;
     if (all_trotter) base.out_prop = c->f;
-    launch_eval(c, base);
-    // learned centroid corrections of the systems that carry one (P = 1)
+    // learned centroid corrections of the systems that carry one (P = 1): the
+    // descriptors, the network and the frames need the positions only and run
+    // on their own branch beside the force evaluation; the correction is added
+    // to fphys after the combine
+    std::vector<SurrogateRun> runs;
     for (const auto &g : c->surrogates) {
         if (sys >= 0 && g.sys != sys) continue;
         const SysDev &S = c->sys_h[g.sys];
@@ -595,7 +609,18 @@ void enqueue_forces(qtg_ctx *c, int sys, bool force_sc) {
         r.feat = g.feat;
         r.wrapped = g.wrapped;
         r.status = c->status;
-        launch_surrogate_correction(r, c->stream, &c->launches);
+        runs.push_back(r);
+    }
+    if (!runs.empty()) {
+        cudaEventRecord(c->sur_fork, c->stream);
+        cudaStreamWaitEvent(c->sur_stream, c->sur_fork, 0);
+        for (const auto &r : runs) launch_surrogate_prepare(r, c->sur_stream, &c->launches);
+        cudaEventRecord(c->sur_join, c->sur_stream);
+    }
+    launch_eval(c, base);
+    if (!runs.empty()) {
+        cudaStreamWaitEvent(c->stream, c->sur_join, 0);
+        for (const auto &r : runs) launch_surrogate_apply(r, c->stream, &c->launches);
     }
     // odd beads that need the Suzuki-Chin force gradient
     const int *osys, *obead;
@@ -674,10 +699,12 @@ void enqueue_step(qtg_ctx *c, int sys, int nvt, int ext_noise, bool pile_g) {
         cudaStreamWaitEvent(c->side_stream, c->ev_fork[0], 0);
         launch_skin_rebuild(list_args(c, jb, nj, 0), c->side_stream, &c->launches);
         cudaEventRecord(c->ev_join, c->side_stream);
+        c->forks.lists_ready = c->ev_join;  // a Lennard-Jones term over the lists waits for them
     } else {
         launch_skin_rebuild(list_args(c, jb, nj, 0), c->stream, &c->launches);
     }
     enqueue_forces(c, sys, false);
+    c->forks.lists_ready = nullptr;
     if (beside) cudaStreamWaitEvent(c->stream, c->ev_join, 0);
     FinalizeArgs fa = fin_args(c, sys, 1, 1);
     fa.noise = nullptr;
@@ -1215,6 +1242,9 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
     ctx->stream = ctx->own_stream;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->sur_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->sur_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->sur_join, cudaEventDisableTiming);
     for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&ctx->ev_fork[k], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
     for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaStreamCreateWithFlags(&ctx->forks.side[k], cudaStreamNonBlocking);
@@ -1435,8 +1465,9 @@ void qtg_destroy(qtg_ctx *ctx) {
     for (auto &g : ctx->call_graphs) cudaGraphExecDestroy(g.second.first);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
+    if (ctx->sur_stream) cudaStreamDestroy(ctx->sur_stream);
     for (cudaEvent_t ev : {ctx->ev_fork[0], ctx->ev_fork[1], ctx->ev_join, ctx->forks.fork, ctx->forks.join[0],
-                           ctx->forks.join[1]})
+                           ctx->forks.join[1], ctx->sur_fork, ctx->sur_join})
         if (ev) cudaEventDestroy(ev);
     for (cudaStream_t st : {ctx->forks.side[0], ctx->forks.side[1]})
         if (st) cudaStreamDestroy(st);
@@ -2344,6 +2375,7 @@ qtg_status qtg_time_kernel(qtg_ctx *ctx, const char *name, int iters, double *av
     const int nj = (int)ctx->base.h.size();
     EvalArgs a = eval_args(ctx, ctx->base.d, nj, ctx->q, ctx->fphys, 0, 0);
     a.lj_full = 1;  // as the stepper evaluates
+    a.lj_list = lj_list_ok(ctx) ? 1 : 0;
     launch_eval(ctx, a);  // fills every scratch array the single kernels read
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -2422,6 +2454,7 @@ qtg_status qtg_autotune(qtg_ctx *ctx, int iters, double *ms_heuristic, double *m
         for (int k = 0; k < 3; ++k) ctx->tune[k] = t[k];
         EvalArgs a = eval_args(ctx, ctx->base.d, nj, ctx->q, ctx->fphys, 0, 0);
         a.lj_full = 1;
+        a.lj_list = lj_list_ok(ctx) ? 1 : 0;
         return time_on_stream(ctx, iters, [&] { launch_eval(ctx, a); }, ms);
     };
     // each count governs one kernel: k_real (n_rj), k_ksk (n_sc), k_kforce (n_kc), 0

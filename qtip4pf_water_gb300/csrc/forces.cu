@@ -2005,7 +2005,9 @@ __global__ void __launch_bounds__(128) k_lj(EvalArgs a) {
         const double d0 = warp_sum((double)fi0), d1 = warp_sum((double)fi1), d2 = warp_sum((double)fi2);
         e = warp_sum((double)el) * (FULL ? 0.5 : 1.0);
         if (lane == 0) {
-            if (FULL) {
+            if (FULL && a.lj_plane) {  // the mixed combine adds the oxygen force
+                a.ljf[J.site_off / 3 + i] = make_float4((float)d0, (float)d1, (float)d2, 0.f);
+            } else if (FULL) {
                 f[9 * i] += d0;
                 f[9 * i + 1] += d1;
                 f[9 * i + 2] += d2;
@@ -2257,6 +2259,10 @@ int chunks_or(int tuned, long long base_blocks, int maxc) {
 }
 
 void launch_lj_dense(const EvalArgs &a, cudaStream_t s) {
+    if (a.lj_list) {  // large beads: the symmetric Verlet list instead of every pair
+        k_lj<float, 1><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
+        return;
+    }
     const long long blocks8 = (long long)((a.max_mols + 15) / 16) * a.n_jobs;
     if (blocks8 >= 2LL * 152) k_lj_dense<8><<<dim3((a.max_mols + 15) / 16, a.n_jobs), 128, 0, s>>>(a);
     else k_lj_dense<32><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
@@ -2316,6 +2322,7 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
         launch_sk_reduce<R, 0>(a, forks->side[0]);
         launch_kforce_f32(a, dim3(tiles, a.n_kc, a.n_jobs), forks->side[0]);
         cudaEventRecord(forks->join[0], forks->side[0]);
+        if (a.lj_list && forks->lists_ready) cudaStreamWaitEvent(forks->side[1], forks->lists_ready, 0);
         launch_lj_dense(a, forks->side[1]);
         if (a.intra) {
             a.intra_plane = 1;

@@ -482,6 +482,7 @@ struct EvalArgs {
     const int *point, *list;
     const int *point_full, *list_full;  // symmetric lists built by the stepper's rebuild
     int lj_full;                        // 1: Lennard-Jones over the symmetric list (no atomics)
+    int lj_list;                        // mixed, symmetric lists valid: k_lj over them instead of every pair
     const KVec *kvec;
     const KCol *kcol;
     const KGroup *kgrp;
@@ -567,7 +568,11 @@ struct SurrogateRun {
     __nv_bfloat16 *feat;          // scratch: [2N][96]
     unsigned *status;
 };
-void launch_surrogate_correction(const SurrogateRun &r, cudaStream_t s, unsigned long long *launches);
+// The correction in two parts: prepare (wrapped atoms, descriptors, features,
+// the network, the molecular frames: positions only, so it may run beside the
+// force evaluation) and apply (the lab-frame correction added to f).
+void launch_surrogate_prepare(const SurrogateRun &r, cudaStream_t s, unsigned long long *launches);
+void launch_surrogate_apply(const SurrogateRun &r, cudaStream_t s, unsigned long long *launches);
 void init_surrogate_kernel_attributes();
 
 // forces.cu: individual Ewald kernels (for timing)
@@ -584,6 +589,7 @@ void launch_eval_fp64(const EvalArgs &a, cudaStream_t s, unsigned long long *lau
 struct Forks {
     cudaStream_t side[2];
     cudaEvent_t fork, join[2];
+    cudaEvent_t lists_ready;  // set: the Verlet-list rebuild runs beside the forces; the list LJ waits for it
 };
 void launch_eval_mixed(const EvalArgs &a, cudaStream_t s, unsigned long long *launches,
                        const Forks *forks = nullptr);

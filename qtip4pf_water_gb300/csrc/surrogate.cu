@@ -5,7 +5,7 @@
 // minus the classical qTIP4P/F force) on those atoms, expressed in the
 // molecule's own frame. This file holds its device side:
 //
-//   k_descriptors   Behler-Parrinello radial (G2) and angular (G4) symmetry
+//   k_descriptors   Behler-Parrinello radial (G2) and angular (G5) symmetry
 //                   functions within 6 A, 32 per atom, one warp per molecule
 //   k_mlp_fwd       the network's forward pass on the tensor cores: BF16
 //                   operands in shared memory, tcgen05.mma into FP32
@@ -31,21 +31,31 @@ namespace {
 
 // ---- symmetry-function descriptors ---------------------------------------------
 // Behler & Parrinello, Phys. Rev. Lett. 98, 146401 (2007); Behler, J. Chem. Phys.
-// 134, 074106 (2011). Cutoff f_c(r) = (cos(pi r / R_c) + 1) / 2 for r < R_c.
+// 134, 074106 (2011), eq. 27 (the angular form without r_jk terms). Cutoff
+// f_c(r) = (cos(pi r / R_c) + 1) / 2 for r < R_c.
 //   G2_i = sum_{j != i, species s} exp(-eta r_ij^2) f_c(r_ij)
-//   G4_i = 2^(1 - zeta) sum_{j < k, pair class c} (1 + lambda cos theta_jik)^zeta
-//          exp(-eta (r_ij^2 + r_ik^2 + r_jk^2)) f_c(r_ij) f_c(r_ik) f_c(r_jk)
+//   G5_i = 2^(1 - zeta) sum_{j < k, pair class c} (1 + lambda cos theta_jik)^zeta
+//          exp(-eta (r_ij^2 + r_ik^2)) f_c(r_ij) f_c(r_ik)
 // Layout of the 32 values of an atom:
 //   0..7    G2, neighbours O, eta = G2_ETA[0..7]
 //   8..15   G2, neighbours H
-//   16..23  G4, neighbour pair of one species (OO or HH), the eight G4 sets below
-//   24..31  G4, mixed neighbour pair (OH)
+//   16..23  G5, neighbour pair of one species (OO or HH), the eight G5 sets below
+//   24..31  G5, mixed neighbour pair (OH)
+// G5 without r_jk separates over the neighbours: with w_j = exp(-eta r_ij^2)
+// f_c(r_ij), u_j the unit vector to j and cos theta_jik = u_j . u_k, the
+// moments W = sum w, V = sum w u, M = sum w u u^T and Q = sum w^2 of a species
+// set give its pair sums
+//   sum_{j<k} w_j w_k = (W^2 - Q) / 2,  sum w_j w_k cos = (|V|^2 - Q) / 2,
+//   sum w_j w_k cos^2 = (|M|_F^2 - Q) / 2,
+// and the mixed (O, H) pairs W_O W_H, V_O . V_H, <M_O, M_H>_F; (1 + lambda cos)^zeta
+// for zeta = 1, 2 is a combination of those three. The cost is per neighbour,
+// not per neighbour pair.
 // Atoms are O, H1, H2 of each molecule in the reference's order; every atom
 // within R_c counts, the atom's own molecule included.
 constexpr int ND = QTG_DESC_PER_ATOM;
 constexpr int NB_MAX = 256;  // neighbours within R_c kept per atom
 __constant__ float G2_ETA[8] = {0.001f, 0.01f, 0.03f, 0.06f, 0.15f, 0.3f, 0.7f, 1.5f};  // 1/A^2
-// G4 sets, in this order: (zeta, lambda) = (1, +1), (1, -1), (2, +1), (2, -1) with
+// G5 sets, in this order: (zeta, lambda) = (1, +1), (1, -1), (2, +1), (2, -1) with
 // eta = 0.005 / A^2, then the same four with eta = 0.02 / A^2
 
 constexpr float BOHR_A = 0.529177210903f;
@@ -82,10 +92,11 @@ __global__ void k_wrap_atoms(DescArgs a) {
 // (an atom within R_c of one of this molecule's atoms belongs to such a
 // molecule: every H lies within CAND_MARGIN / 2 of its O); then, for each of
 // the three atoms in turn, the candidates' atoms within R_c are compacted into
-// shared memory (ballot + prefix), G2 is summed over them and G4 over their
-// pairs, and the sums are reduced over the warp. The G4 sets share one
-// Gaussian per pair (exp(-0.02 s) = exp(-0.005 s)^4) and two angular bases
-// (1 +- cos theta).
+// shared memory (ballot + prefix), G2 and the G5 moments are summed over them
+// (each lane over its share of the neighbours, for all of them and for the H
+// ones; the O sums are the difference), the sums are reduced over the warp and
+// lane 0 forms the 32 values. The two G5 widths share one Gaussian
+// (exp(-0.02 s) = exp(-0.005 s)^4).
 constexpr int DW = 4;            // warps per block
 constexpr int CAND_MAX = 256;    // candidate molecules kept per molecule
 constexpr float CAND_MARGIN = 3.2f;  // A
@@ -168,56 +179,96 @@ __global__ void __launch_bounds__(32 * DW) k_descriptors(DescArgs a) {
             n = NB_MAX;
         }
         __syncwarp();
-        float acc[ND];
+        // per lane: G2 of all neighbours and of the H ones; the G5 moments
+        // W, V (3), M (xx, yy, zz, xy, xz, yz), Q of the two widths, all and H
+        constexpr int NM = 11;
+        float g2a[8], g2h[8], mo[2][2][NM];
 #pragma unroll
-        for (int k = 0; k < ND; ++k) acc[k] = 0.f;
+        for (int k = 0; k < 8; ++k) g2a[k] = g2h[k] = 0.f;
+#pragma unroll
+        for (int e = 0; e < 2; ++e)
+#pragma unroll
+            for (int t = 0; t < 2; ++t)
+#pragma unroll
+                for (int k = 0; k < NM; ++k) mo[e][t][k] = 0.f;
         for (int jj = lane; jj < n; jj += 32) {
             const float4 d = nb[warp][jj];
             const float r2 = d.w * d.w, fc = nfc[warp][jj];
-            const bool h = sp[warp][jj];
+            const float h = sp[warp][jj] ? 1.f : 0.f;
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 const float v = __expf(-G2_ETA[k] * r2) * fc;
-                if (h) acc[8 + k] += v;
-                else acc[k] += v;
+                g2a[k] += v;
+                g2h[k] = fmaf(h, v, g2h[k]);
             }
-        }
-        for (int jj = lane; jj < n; jj += 32) {
-            const float4 dj = nb[warp][jj];
-            const float fj = nfc[warp][jj], rj2 = dj.w * dj.w, ij = 1.f / dj.w;
-            const unsigned char sj = sp[warp][jj];
-            for (int kk = jj + 1; kk < n; ++kk) {
-                const float4 dk = nb[warp][kk];
-                const float ex = dj.x - dk.x, ey = dj.y - dk.y, ez = dj.z - dk.z;
-                const float rjk2 = ex * ex + ey * ey + ez * ez;
-                if (rjk2 >= rc2) continue;
-                const float fjk = 0.5f * (__cosf(3.14159265358979f * sqrtf(rjk2) * irc) + 1.0f);
-                const float cs = (dj.x * dk.x + dj.y * dk.y + dj.z * dk.z) * ij / dk.w;
-                const float f3 = fj * nfc[warp][kk] * fjk;
-                const float e1 = __expf(-0.005f * (rj2 + dk.w * dk.w + rjk2)), e2 = e1 * e1;
-                const float ga = e1 * f3, gb = e2 * e2 * f3;  // eta = 0.005 and 0.02 / A^2
-                const float bp = 1.f + cs, bm = 1.f - cs;
-                // (zeta, lambda) = (1, +1), (1, -1), (2, +1), (2, -1); 2^(1-zeta) (1 + lambda cos)^zeta
-                const float t0 = bp, t1 = bm, t2 = 0.5f * bp * bp, t3 = 0.5f * bm * bm;
-                if (sj == sp[warp][kk]) {
-                    acc[16] += t0 * ga; acc[17] += t1 * ga; acc[18] += t2 * ga; acc[19] += t3 * ga;
-                    acc[20] += t0 * gb; acc[21] += t1 * gb; acc[22] += t2 * gb; acc[23] += t3 * gb;
-                } else {
-                    acc[24] += t0 * ga; acc[25] += t1 * ga; acc[26] += t2 * ga; acc[27] += t3 * ga;
-                    acc[28] += t0 * gb; acc[29] += t1 * gb; acc[30] += t2 * gb; acc[31] += t3 * gb;
+            const float ir = 1.f / d.w, ux = d.x * ir, uy = d.y * ir, uz = d.z * ir;
+            const float e1 = __expf(-0.005f * r2), e2 = e1 * e1;
+            const float wv[2] = {e1 * fc, e2 * e2 * fc};
+#pragma unroll
+            for (int e = 0; e < 2; ++e)
+#pragma unroll
+                for (int t = 0; t < 2; ++t) {
+                    const float w = t ? h * wv[e] : wv[e];
+                    const float wx = w * ux, wy = w * uy, wz = w * uz;
+                    float *m = mo[e][t];
+                    m[0] += w;
+                    m[1] += wx;
+                    m[2] += wy;
+                    m[3] += wz;
+                    m[4] = fmaf(wx, ux, m[4]);
+                    m[5] = fmaf(wy, uy, m[5]);
+                    m[6] = fmaf(wz, uz, m[6]);
+                    m[7] = fmaf(wx, uy, m[7]);
+                    m[8] = fmaf(wx, uz, m[8]);
+                    m[9] = fmaf(wy, uz, m[9]);
+                    m[10] = fmaf(w, wv[e], m[10]);
                 }
-            }
         }
 #pragma unroll
-        for (int k = 0; k < ND; ++k) {
-            float v = acc[k];
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            acc[k] = v;
+        for (int k = 0; k < 8; ++k) {
+            g2a[k] = warp_sum(g2a[k]);
+            g2h[k] = warp_sum(g2h[k]);
         }
+#pragma unroll
+        for (int e = 0; e < 2; ++e)
+#pragma unroll
+            for (int t = 0; t < 2; ++t)
+#pragma unroll
+                for (int k = 0; k < NM; ++k) mo[e][t][k] = warp_sum(mo[e][t][k]);
         if (lane == 0) {
             float *out = a.desc + ((size_t)conf * na + i) * ND;
 #pragma unroll
-            for (int k = 0; k < ND; ++k) out[k] = acc[k];
+            for (int k = 0; k < 8; ++k) {
+                out[k] = g2a[k] - g2h[k];
+                out[8 + k] = g2h[k];
+            }
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                float so[NM];  // the O moments: all minus H
+#pragma unroll
+                for (int k = 0; k < NM; ++k) so[k] = mo[e][0][k] - mo[e][1][k];
+                const float *sh = mo[e][1];
+                // same-species pair sums (OO + HH) and mixed ones (OH) of 1, cos, cos^2
+                auto frob = [](const float *x, const float *y) {
+                    return x[4] * y[4] + x[5] * y[5] + x[6] * y[6] + 2.f * (x[7] * y[7] + x[8] * y[8] + x[9] * y[9]);
+                };
+                auto dot3 = [](const float *x, const float *y) { return x[1] * y[1] + x[2] * y[2] + x[3] * y[3]; };
+                const float p0 = 0.5f * ((so[0] * so[0] - so[10]) + (sh[0] * sh[0] - sh[10]));
+                const float p1 = 0.5f * ((dot3(so, so) - so[10]) + (dot3(sh, sh) - sh[10]));
+                const float p2 = 0.5f * ((frob(so, so) - so[10]) + (frob(sh, sh) - sh[10]));
+                const float x0 = so[0] * sh[0], x1 = dot3(so, sh), x2 = frob(so, sh);
+                // (zeta, lambda) = (1, +1), (1, -1), (2, +1), (2, -1):
+                // 1 + c, 1 - c, (1 + 2c + c^2) / 2, (1 - 2c + c^2) / 2
+                float *g = out + 16 + 4 * e;
+                g[0] = p0 + p1;
+                g[1] = p0 - p1;
+                g[2] = 0.5f * (p0 + 2.f * p1 + p2);
+                g[3] = 0.5f * (p0 - 2.f * p1 + p2);
+                g[8] = x0 + x1;
+                g[9] = x0 - x1;
+                g[10] = 0.5f * (x0 + 2.f * x1 + x2);
+                g[11] = 0.5f * (x0 - 2.f * x1 + x2);
+            }
         }
         __syncwarp();
     }
@@ -802,7 +853,7 @@ __global__ void k_apply_correction(const float *frames, const float *y, int n_mo
 
 }  // namespace
 
-void launch_surrogate_correction(const SurrogateRun &r, cudaStream_t s, unsigned long long *launches) {
+void launch_surrogate_prepare(const SurrogateRun &r, cudaStream_t s, unsigned long long *launches) {
     const int N = r.n_mols;
     DescArgs d;
     d.pos = r.pos;
@@ -831,8 +882,12 @@ void launch_surrogate_correction(const SurrogateRun &r, cudaStream_t s, unsigned
     const int tiles = (2 * N + TM - 1) / TM;
     k_mlp_fwd<<<tiles < 2 * r.n_sm ? tiles : 2 * r.n_sm, TM, (size_t)F_END + 1024, s>>>(a);
     k_frames<<<(N + 127) / 128, 128, 0, s>>>(r.pos, N, r.box[0], r.box[1], r.box[2], r.frames);
-    k_apply_correction<<<(N + 127) / 128, 128, 0, s>>>(r.frames, r.y, N, r.out_scale, r.f);
-    if (launches) *launches += 6;
+    if (launches) *launches += 5;
+}
+
+void launch_surrogate_apply(const SurrogateRun &r, cudaStream_t s, unsigned long long *launches) {
+    k_apply_correction<<<(r.n_mols + 127) / 128, 128, 0, s>>>(r.frames, r.y, r.n_mols, r.out_scale, r.f);
+    if (launches) *launches += 1;
 }
 
 void init_surrogate_kernel_attributes() {

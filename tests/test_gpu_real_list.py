@@ -97,13 +97,23 @@ def test_list_forces_of_several_beads_match_the_oracle(gpu_lib):
 
 
 def test_list_stays_complete_while_the_system_moves(gpu_lib):
+    """Also the Lennard-Jones term of large beads, which the stepper takes over
+    its symmetric Verlet list (rebuilt beside the forces): the forces at the
+    positions a run reached against the oracle's at the same positions."""
+    from oracle.binding import Oracle
+
     q = gpu_lib
     st = q.seeded_start(1000, 2, 298.0, seed=45)
     ctx, s = _stepper(q, st, 2, 0, dt=0.5)
+    o = Oracle(1000, 2, st.box_bohr, 298.0, 0.5)
     for _ in range(3):
         ctx.run_steps(300, is_nvt=True)
         ctx.sync()
         state = s.get_state()
+        point, lst, _ = o.build_lists(state["q"])
+        fo = np.zeros_like(state["q"])
+        o.force_eval_trotter(state["q"].copy(), fo, point, lst)
+        assert rel_rms(state["fphys"], fo) < 1e-4
         ctx.set_real_space(1)
         ctx.init_forces()
         f_all = s.get_state()["fphys"]

@@ -62,3 +62,36 @@ def test_descriptors_are_translation_invariant_and_species_resolved():
     assert np.all(d0 >= 0.0) and np.all(d0[:, :8] > 0.0)
     # the O of a water sees its own two H at ~0.94 A in the H block of G2
     assert np.all(d0[0::3, 15] > 2 * np.exp(-1.5 * 0.95 ** 2) * so.fcut(0.95) * 0.9)
+
+
+def test_g5_pair_sums_equal_their_moment_form():
+    """The device forms G5 from per-atom moments of each species set (W = sum w,
+    V = sum w u, M = sum w u u^T, Q = sum w^2); the oracle sums the neighbour
+    pairs explicitly. Both forms of the same sums agree to round-off."""
+    from qtip4pf_water_gb300.start import seeded_start
+
+    st = seeded_start(64, 1, 298.0, seed=6)
+    d = so.sym_descriptors(st.q, st.box_bohr)
+    x = st.q.reshape(-1, 3) * so.BOHR_A
+    L = st.box_bohr * so.BOHR_A
+    h_atom = np.arange(len(x)) % 3 != 0
+    for i in (0, 1, 2, 50, 100, 191):
+        dd = x - x[i]
+        dd -= L * np.rint(dd / L)
+        r = np.sqrt((dd * dd).sum(1))
+        m = r < so.RC_A
+        m[i] = False
+        u, fc, h = dd[m] / r[m, None], so.fcut(r[m]), h_atom[m]
+        for e, eta in enumerate((0.005, 0.02)):
+            w = np.exp(-eta * r[m] ** 2) * fc
+            mom = {}
+            for name, sel in (("O", ~h), ("H", h)):
+                ws, us = w[sel], u[sel]
+                mom[name] = (ws.sum(), ws @ us, np.einsum("j,ja,jb->ab", ws, us, us), ws @ ws)
+            same = [sum(0.5 * (f(mom[s]) - mom[s][3]) for s in "OH")
+                    for f in (lambda t: t[0] ** 2, lambda t: t[1] @ t[1], lambda t: (t[2] * t[2]).sum())]
+            mixed = [mom["O"][0] * mom["H"][0], mom["O"][1] @ mom["H"][1], (mom["O"][2] * mom["H"][2]).sum()]
+            for k, (zeta, lam) in enumerate(((1, 1), (1, -1), (2, 1), (2, -1))):
+                for base, (v0, v1, v2) in ((16, same), (24, mixed)):
+                    g = v0 + lam * v1 if zeta == 1 else 0.5 * (v0 + 2 * lam * v1 + v2)
+                    assert abs(g - d[i, base + 4 * e + k]) <= 1e-10 * max(1.0, abs(g)), (i, base, e, k)
