@@ -232,6 +232,7 @@ struct qtg_ctx {
     int rl_form = 0, rl_cap = 0;
     unsigned short *rl_list = nullptr;
     int *rl_cnt = nullptr, *rl_jobs = nullptr, *rl_count = nullptr, *rl_wide = nullptr;
+    uint4 *rl_state = nullptr;
     float4 *rl_ref = nullptr;
     std::string err;
     Consts K;
@@ -419,6 +420,7 @@ EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, d
     a.rl_jobs = c->rl_jobs;
     a.rl_count = c->rl_count;
     a.rl_wide = c->rl_wide;
+    a.rl_state = c->rl_state;
     a.c = c->K;
     return a;
 }
@@ -1330,6 +1332,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
             AL(ctx->rl_jobs, n_jobs_max);
             AL(ctx->rl_count, 1);
             AL(ctx->rl_wide, ctx->total_slots);
+            AL(ctx->rl_state, ctx->total_slots);
             // NaN reference positions: the first evaluation of every slot builds its list
             if (e == cudaSuccess) e = cudaMemset(ctx->rl_ref, 0xff, sizeof(float4) * ctx->total_sites);
         }
@@ -1454,7 +1457,7 @@ void qtg_destroy(qtg_ctx *ctx) {
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
                     ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf, ctx->fin_ticket, ctx->sites_fix, ctx->intra, ctx->kfc, ctx->kfb, ctx->wpk,
                     ctx->wpos, ctx->cnt_half, ctx->cnt_full, ctx->cell_start, ctx->cell_mol,
-                    ctx->rb_jobs, ctx->rb_count, ctx->rl_list, ctx->rl_cnt, ctx->rl_ref, ctx->rl_jobs, ctx->rl_count, ctx->rl_wide};
+                    ctx->rb_jobs, ctx->rb_count, ctx->rl_list, ctx->rl_cnt, ctx->rl_ref, ctx->rl_jobs, ctx->rl_count, ctx->rl_wide, ctx->rl_state};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->box) cudaFreeHost(ctx->box);

@@ -501,21 +501,26 @@ __device__ __forceinline__ void rl_image(const RlBox &B, float &dx, float &dy, f
     dz = fmaf(-B.L2, rintf(dz * B.I2), dz);
 }
 
-// Block per job: the list's validity (two largest site displacements since the
-// build, compared as the bit patterns of their non-negative squares, a NaN above
-// all) and the spread of the molecules; a rebuilding job joins the launch's list
-// of rebuilding jobs and records the positions of the build.
+// The list's validity and the molecules' spread, RLT_SITES sites a block, any
+// number of blocks a configuration: the two largest site displacements since
+// the build (compared as the bit patterns of their non-negative squares, a NaN
+// above all) are merged over the blocks with two atomic maxima (a block's largest
+// either becomes the maximum or bids, through the smaller of itself and the
+// maximum it displaced, for the second), and the block that arrives last on the
+// configuration's ticket decides, re-arms the state and, when the list is
+// rebuilt, adds the configuration to the launch's list of rebuilding ones.
+constexpr int RLT_SITES = 2048;
 __global__ void __launch_bounds__(256) k_rlist_test(EvalArgs a) {
-    const Job J = a.jobs[blockIdx.x];
+    const Job J = a.jobs[blockIdx.y];
     const SysDev &S = a.sys[J.sys];
     const int ns = S.n_sites;
     const float4 *sites = reinterpret_cast<const float4 *>(a.sites) + J.site_off;
-    float4 *ref = a.rl_ref + J.site_off;
+    const float4 *ref = a.rl_ref + J.site_off;
     const RlBox B = rl_box(S);
     constexpr float sp2 = RL_SPREAD * RL_SPREAD;
     unsigned m1 = 0u, m2 = 0u;
     int wide = 0;
-    for (int k = threadIdx.x; k < ns; k += blockDim.x) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < ns; k += gridDim.x * blockDim.x) {
         const float4 p = sites[k], r = ref[k];
         float dx = p.x - r.x, dy = p.y - r.y, dz = p.z - r.z;
         rl_image(B, dx, dy, dz);
@@ -540,27 +545,31 @@ __global__ void __launch_bounds__(256) k_rlist_test(EvalArgs a) {
         m2 = n2;
     }
     __shared__ unsigned red[2][8];
-    __shared__ int build;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (lane == 0) {
         red[0][w] = m1;
         red[1][w] = m2;
     }
     wide = __syncthreads_or(wide);
-    if (threadIdx.x == 0) {
-        unsigned t1 = 0u, t2 = 0u;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-            const unsigned n1 = max(t1, red[0][k]), n2 = max(min(t1, red[0][k]), max(t2, red[1][k]));
-            t1 = n1;
-            t2 = n2;
-        }
-        build = !(sqrtf(__uint_as_float(t1)) + sqrtf(__uint_as_float(t2)) <= RL_SKIN);
-        a.rl_wide[J.slot] = wide;
-        if (build) a.rl_jobs[atomicAdd(a.rl_count, 1)] = blockIdx.x;
+    if (threadIdx.x != 0) return;
+    unsigned t1 = 0u, t2 = 0u;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+        const unsigned n1 = max(t1, red[0][k]), n2 = max(min(t1, red[0][k]), max(t2, red[1][k]));
+        t1 = n1;
+        t2 = n2;
     }
-    __syncthreads();
-    if (!build) return;
-    for (int k = threadIdx.x; k < ns; k += blockDim.x) ref[k] = sites[k];
+    uint4 *st = a.rl_state + J.slot;  // (largest, second, wide, ticket)
+    const unsigned o = atomicMax(&st->x, t1);
+    atomicMax(&st->y, max(t2, min(t1, o)));
+    if (wide) atomicOr(&st->z, 1u);
+    __threadfence();
+    if (atomicAdd(&st->w, 1u) != gridDim.x - 1) return;
+    __threadfence();
+    const unsigned g1 = atomicExch(&st->x, 0u), g2 = atomicExch(&st->y, 0u), wd = atomicExch(&st->z, 0u);
+    atomicExch(&st->w, 0u);
+    a.rl_wide[J.slot] = wd ? 1 : 0;
+    if (!(sqrtf(__uint_as_float(g1)) + sqrtf(__uint_as_float(g2)) <= RL_SKIN))
+        a.rl_jobs[atomicAdd(a.rl_count, 1)] = blockIdx.y;
 }
 
 // Whether some site pair of molecules (a0, a1, a2) and (b0, b1, b2) lies within
@@ -609,6 +618,8 @@ __global__ void __launch_bounds__(32 * RL_ROWS) k_rlist_rows(EvalArgs a, int row
         const float P = R + 2.0f * RL_SPREAD, P2 = P * P;
         const bool wide = a.rl_wide[J.slot] != 0;
         const float4 a0 = sites[3 * i], a1 = sites[3 * i + 1], a2 = sites[3 * i + 2];
+        // the build's positions, for the next displacement tests
+        if (lane < 3) a.rl_ref[J.site_off + 3 * i + lane] = lane == 0 ? a0 : (lane == 1 ? a1 : a2);
         unsigned short *row = a.rl_list + ((size_t)J.site_off / 3 + i) * a.rl_cap;
         int cnt = 0;
         for (int j0 = 0; j0 < N; j0 += 32) {
@@ -2176,6 +2187,112 @@ __global__ void __launch_bounds__(128) k_lj_dense(EvalArgs a) {
     if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], (double)(((redf[0] + redf[1]) + redf[2]) + redf[3]));
 }
 
+// O-O Lennard-Jones of large beads in the mixed stepper: a warp per row of the
+// stepper's symmetric Verlet list (every j != i with r < r_skin at the list's
+// build, which holds every pair inside r_cut while the skin test holds), the
+// pair classification and term of k_lj_dense in FP32 and, for the rare pairs in
+// the band around r_cut^2 or at a half-box tie, the reference's FP64 decision
+// inline. The row's force goes to the oxygen-force plane the combine adds; each
+// pair is seen from both ends and the energy halved.
+constexpr int LJL_U = 8;  // list entries a lane loads at a time in k_lj_list_f32
+__global__ void __launch_bounds__(128) k_lj_list_f32(EvalArgs a) {
+    const int jb = blockIdx.y;
+    const Job J = a.jobs[jb];
+    const SysDev &S = a.sys[J.sys];
+    const int N = S.n_mols;
+    if (blockIdx.x * 4 >= N) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int i = blockIdx.x * 4 + w;
+    const Consts &C = a.c;
+    LjdConst K;
+    for (int d = 0; d < 3; ++d) {
+        K.L[d] = S.boxf[d];
+        K.I[d] = S.inv_boxf[d];
+    }
+    K.rc2 = C.ljf[5];
+    K.band = 1e-5f * K.rc2;
+    K.tie = 1e-5f;
+    K.s6 = C.ljf[0];
+    K.s12 = C.ljf[1];
+    K.eps4 = C.ljf[2];
+    K.eps24 = C.ljf[3];
+    K.ecut = C.ljf[4];
+    K.tie_mask = S.lj_tie_mask;
+    float fx = 0.f, fy = 0.f, fz = 0.f, el = 0.f;
+    if (i < N) {
+        const int cap = 2 * S.list_size;
+        const int *pt = a.point_full + S.pf_off + (size_t)J.bead * (N + 1);
+        const int *ls = a.list_full + S.lf_off + (size_t)J.bead * cap;
+        // a row outside [0, capacity] or an index outside the bead is skipped and flagged
+        int n0 = pt[i], n1 = pt[i + 1];
+        if (n0 < 0 || n1 > cap || n0 > n1) {
+            if (lane == 0) atomicOr(a.status, (unsigned)ST_LIST_OVERFLOW);
+            n0 = max(0, min(n0, cap));
+            n1 = max(n0, min(n1, cap));
+        }
+        const float4 *opos = reinterpret_cast<const float4 *>(a.opos) + J.site_off / 3;
+        const float4 oi = opos[i];
+        // LJL_U entries a lane at a time: their indices, then their positions, then
+        // the pairs (the gathers of one batch in flight together)
+        bool flagged = false;
+        for (int base = n0; base < n1; base += 32 * LJL_U) {
+            int jv[LJL_U];
+            float4 ov[LJL_U];
+#pragma unroll
+            for (int u = 0; u < LJL_U; ++u) {
+                const int n = base + u * 32 + lane;
+                jv[u] = n < n1 ? ls[n] : -1;
+            }
+#pragma unroll
+            for (int u = 0; u < LJL_U; ++u) {
+                const bool ok = jv[u] >= 0 && jv[u] < N && jv[u] != i;
+                ov[u] = ok ? opos[jv[u]] : oi;
+            }
+#pragma unroll
+            for (int u = 0; u < LJL_U; ++u) {
+                const int j = jv[u];
+                if (base + u * 32 + lane >= n1) continue;
+                if (j == i || j < 0 || j >= N) {
+                    atomicOr(a.status, (unsigned)ST_LIST_OVERFLOW);
+                    continue;
+                }
+                float r[3], rr;
+                const int c = ljd_classify(oi, ov[u], K, r, &rr);
+                if (c == 1) ljd_pair(r, rr, K, fx, fy, fz, el);
+                flagged |= (c == 2);
+            }
+        }
+        // the pairs in the band around r_cut^2 or at a half-box tie, with the
+        // reference's FP64 decision, only in warps that met one
+        if (__any_sync(0xffffffffu, flagged) && flagged) {
+            const double *q = a.pos + J.pos_off;
+            for (int n = n0 + lane; n < n1; n += 32) {
+                const int j = ls[n];
+                float r[3], rr;
+                if (j == i || j < 0 || j >= N || ljd_classify(oi, opos[j], K, r, &rr) != 2) continue;
+                double rd[3];
+                const double r2d = lj_exact_disp(q + 9 * i, q + 9 * j, S, rd);
+                if (r2d < C.r_cut_sq) {
+                    r[0] = (float)rd[0];
+                    r[1] = (float)rd[1];
+                    r[2] = (float)rd[2];
+                    ljd_pair(r, (float)r2d, K, fx, fy, fz, el);
+                }
+            }
+        }
+        fx = warp_sum(fx);
+        fy = warp_sum(fy);
+        fz = warp_sum(fz);
+        el = warp_sum(el);
+        if (lane == 0) a.ljf[J.site_off / 3 + i] = make_float4(fx, fy, fz, 0.f);
+    }
+    // the block's FP32 partial (as k_lj_dense), added to the FP64 energy
+    __shared__ float redf[4];
+    if (lane == 0) redf[w] = i < N ? 0.5f * el : 0.f;
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(&a.energy[J.slot], (double)(((redf[0] + redf[1]) + redf[2]) + redf[3]));
+}
+
 // site-force output of the reciprocal-space-only path: out += sum of the k-chunk planes
 template <typename R>
 __global__ void k_sum_parts(EvalArgs a) {
@@ -2259,7 +2376,11 @@ int chunks_or(int tuned, long long base_blocks, int maxc) {
 }
 
 void launch_lj_dense(const EvalArgs &a, cudaStream_t s) {
-    if (a.lj_list) {  // large beads: the symmetric Verlet list instead of every pair
+    if (a.lj_list && a.lj_plane) {  // large beads: the symmetric Verlet list instead of every pair
+        k_lj_list_f32<<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
+        return;
+    }
+    if (a.lj_list) {
         k_lj<float, 1><<<dim3((a.max_mols + 3) / 4, a.n_jobs), 128, 0, s>>>(a);
         return;
     }
@@ -2293,7 +2414,7 @@ int list_chunks(const EvalArgs &a) {
 void launch_real_list(EvalArgs &a, cudaStream_t s) {
     a.n_rj = list_chunks(a);
     cudaMemsetAsync(a.rl_count, 0, sizeof(int), s);
-    k_rlist_test<<<a.n_jobs, 256, 0, s>>>(a);
+    k_rlist_test<<<dim3((3 * a.max_mols + RLT_SITES - 1) / RLT_SITES, a.n_jobs), 256, 0, s>>>(a);
     const int row_blocks = (a.max_mols + RL_ROWS - 1) / RL_ROWS;
     // eight resident blocks on each of the 152 SMs at most; a launch without
     // rebuilds costs each block one load of the count
@@ -2420,6 +2541,7 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
         else k_combine<double><<<gm, 128, 0, s>>>(a);
     } else if (n == "lj") {
         if (mixed) {
+            if (a.lj_full && a.ljf) a.lj_plane = 1;  // as the stepper's forked evaluation
             if (a.lj_full) launch_lj_dense(a, s);
             else k_lj<float, 0><<<gl, 128, 0, s>>>(a);
         } else {

@@ -518,6 +518,7 @@ struct EvalArgs {
     float4 *rl_ref;        // per slot site: the positions the list was built at (NaN: never built)
     int *rl_jobs, *rl_count;  // the launch's jobs whose list is rebuilt, and their number
     int *rl_wide;          // per slot: a site lies beyond RL_SPREAD of its M site (minimum image per site pair)
+    uint4 *rl_state;       // per slot: the displacement test's merge state (zero between launches)
     int tune_rj, tune_sc, tune_kc;  // chunk counts fixed by the autotuner (0: launcher heuristic)
     int sites_are_input;   // 1: positions are charge sites (M,H1,H2) -> reciprocal space only
     int sr_only;           // 1: only the short-range terms (LJ, intramolecular,

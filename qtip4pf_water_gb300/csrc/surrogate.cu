@@ -105,6 +105,7 @@ __global__ void __launch_bounds__(32 * DW) k_descriptors(DescArgs a) {
     __shared__ float4 nb[DW][NB_MAX];   // (dx, dy, dz, r) in A, minimum image
     __shared__ float nfc[DW][NB_MAX];   // f_c(r)
     __shared__ unsigned char sp[DW][NB_MAX];
+    __shared__ float red[DW][64];       // the warp's 64 totals of an atom
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int N = a.n_mols, na = 3 * N;
     const long long g = (long long)blockIdx.x * DW + warp;  // global molecule index over configurations
@@ -224,30 +225,51 @@ __global__ void __launch_bounds__(32 * DW) k_descriptors(DescArgs a) {
                     m[10] = fmaf(w, wv[e], m[10]);
                 }
         }
+        // warp sums of the 60 values by a reduce-scatter: at the step of offset o
+        // each lane keeps one half of its vector (the upper one if lane & o),
+        // sends the other half to lane ^ o and adds what it receives; after the
+        // five steps lane l holds the totals of values 2l and 2l + 1
+        float v[64];
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            g2a[k] = warp_sum(g2a[k]);
-            g2h[k] = warp_sum(g2h[k]);
+            v[k] = g2a[k];
+            v[8 + k] = g2h[k];
         }
 #pragma unroll
         for (int e = 0; e < 2; ++e)
 #pragma unroll
             for (int t = 0; t < 2; ++t)
 #pragma unroll
-                for (int k = 0; k < NM; ++k) mo[e][t][k] = warp_sum(mo[e][t][k]);
+                for (int k = 0; k < NM; ++k) v[16 + NM * (2 * e + t) + k] = mo[e][t][k];
+#pragma unroll
+        for (int k = 16 + 4 * NM; k < 64; ++k) v[k] = 0.f;
+#pragma unroll
+        for (int o = 16, len = 64; o > 0; o >>= 1, len >>= 1) {
+            const bool up = lane & o;
+#pragma unroll
+            for (int k = 0; k < len / 2; ++k) {
+                const float send = up ? v[k] : v[k + len / 2];
+                const float keep = up ? v[k + len / 2] : v[k];
+                v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+            }
+        }
+        red[warp][2 * lane] = v[0];
+        red[warp][2 * lane + 1] = v[1];
+        __syncwarp();
         if (lane == 0) {
+            const float *tot = red[warp];
             float *out = a.desc + ((size_t)conf * na + i) * ND;
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-                out[k] = g2a[k] - g2h[k];
-                out[8 + k] = g2h[k];
+                out[k] = tot[k] - tot[8 + k];
+                out[8 + k] = tot[8 + k];
             }
 #pragma unroll
             for (int e = 0; e < 2; ++e) {
                 float so[NM];  // the O moments: all minus H
+                const float *sa = tot + 16 + NM * (2 * e), *sh = tot + 16 + NM * (2 * e + 1);
 #pragma unroll
-                for (int k = 0; k < NM; ++k) so[k] = mo[e][0][k] - mo[e][1][k];
-                const float *sh = mo[e][1];
+                for (int k = 0; k < NM; ++k) so[k] = sa[k] - sh[k];
                 // same-species pair sums (OO + HH) and mixed ones (OH) of 1, cos, cos^2
                 auto frob = [](const float *x, const float *y) {
                     return x[4] * y[4] + x[5] * y[5] + x[6] * y[6] + 2.f * (x[7] * y[7] + x[8] * y[8] + x[9] * y[9]);
