@@ -28,6 +28,10 @@ reference names no dataset):
                 Trotter + PILE-G, mixed: all replicas in one context (one
                 CUDA-graph step for all, launch shapes autotuned) against the
                 same systems run one context at a time; aggregate bead-steps/s.
+  large4096     4096 waters (L = 49.7 A), P = 1, dt = 0.5 fs, mixed: NVE from
+                one Langevin-equilibrated state with the real space over the
+                pair list and over all pairs: drift and fluctuation of the
+                conserved quantity, ns/day, force difference of the two forms.
 
 Energies are in Hartree; drift is reported per ns and per molecule.
 """
@@ -179,6 +183,42 @@ def sc512(steps=40000, seed=13, fp64_steps=8000, equil=4000):
     rep["mixed_over_fp64_speed"] = rep["mixed"]["ns_day"] / rep["fp64"]["ns_day"]
     rep["force_rms_rel_err_mixed_vs_fp64"] = force_rms_error(eq["q"], st.box_bohr, n, P, 298.0, dt, SUZUKI_CHIN,
                                                              PILE_G)
+    return rep
+
+
+def large4096(steps=20000, seed=15, equil=4000, n=4096, beads=1, dt=0.5):
+    """Real space of large beads over the pair list against all pairs: n waters,
+    P = beads, mixed; equil Langevin (PILE-L) steps from the seeded lattice start,
+    then the same state advanced NVE with each real-space form. Reports the
+    conserved-quantity drift and fluctuation of both runs, their step times, and
+    the RMS difference of the two forms' forces on the list run's end state."""
+    st = seeded_start(n, beads, 298.0, seed=seed)
+    d = system_desc(n, beads, st.box_bohr, dt_fs=dt, propagator=TROTTER, thermostat=PILE_L, seed=seed)
+    ctx, _ = make_ctx([d], [st], MIXED)
+    run_records(ctx, 0, equil, True)
+    eq = ctx.systems[0].get_state()
+    ctx.close()
+    rep = {"workload": "large4096", "n_mols": n, "n_beads": beads, "dt_fs": dt, "nvt_equilibration_steps": equil,
+           "equilibration": "PILE-L, mixed form, pair-list real space, from the seeded lattice start"}
+    end = None
+    for form, tag in ((0, "pair_list"), (1, "all_pairs")):
+        ctx = Context([d], MIXED)
+        ctx.set_real_space(form)
+        ctx.systems[0].set_state(eq["q"], eq["p"])
+        ctx.init_forces()
+        rec, t = run_records(ctx, 0, steps, False)
+        rep[tag] = dict(_drift(rec, dt, n), ns_day=ns_per_day(t / steps, dt), ms_per_step=t / steps * 1e3,
+                        run_ps=steps * dt * 1e-3)
+        if form == 0:
+            end = ctx.systems[0].get_state()
+        else:  # the all-pairs forces at the list run's end state
+            ctx.systems[0].set_state(end["q"], end["p"])
+            ctx.init_forces()
+            fa = ctx.systems[0].get_state()["fphys"]
+            rep["force_rms_rel_diff_list_vs_all_pairs"] = float(
+                np.sqrt(np.mean((end["fphys"] - fa) ** 2) / np.mean(fa ** 2)))
+        ctx.close()
+    rep["list_over_all_pairs_speed"] = rep["pair_list"]["ns_day"] / rep["all_pairs"]["ns_day"]
     return rep
 
 
@@ -362,7 +402,7 @@ def headline(steps=200, seed=2024):
 
 
 WORKLOADS = {"headline": headline, "classical216": classical216, "trotter216": trotter216, "sc512": sc512,
-             "replicas48": replicas48, "cmd": cmd}
+             "replicas48": replicas48, "cmd": cmd, "large4096": large4096}
 
 
 def main(argv=None):

@@ -96,6 +96,32 @@ def test_list_forces_of_several_beads_match_the_oracle(gpu_lib):
     assert rel_rms(f_list, s.get_state()["fphys"]) < 1e-5
 
 
+def test_suzuki_chin_forces_of_large_beads_match_the_oracle(gpu_lib):
+    """Suzuki-Chin assembly of 1000 waters, P = 4, mixed: the physical forces
+    (real space over the pair list, Lennard-Jones over the list) and the
+    propagating Suzuki-Chin forces (with the FP64 finite-difference gradient
+    terms) against the oracle's restatement of force_eval_sc_nospline."""
+    from oracle.binding import Oracle
+
+    q = gpu_lib
+    P = 4
+    st = q.seeded_start(1000, P, 298.0, seed=47)
+    ctx = q.Context([q.system_desc(1000, P, st.box_bohr, dt_fs=0.25, propagator=q.SUZUKI_CHIN,
+                                   thermostat=q.PILE_G, seed=47)], q.MIXED)
+    assert ctx.real_space() == (0, True)
+    s = ctx.systems[0]
+    s.set_state(st.q, st.p)
+    ctx.init_forces()
+    out = s.get_state()
+    o = Oracle(1000, P, st.box_bohr, 298.0, 0.25)
+    qq = st.q.reshape(-1).copy()
+    point, lst, _ = o.build_lists(qq)
+    f, fp = np.zeros_like(qq), np.zeros_like(qq)
+    o.force_eval_sc(qq, f, point, lst, fp)
+    assert rel_rms(out["fphys"], fp) < 1e-4
+    assert rel_rms(out["f"], f) < 1e-4
+
+
 def test_list_stays_complete_while_the_system_moves(gpu_lib):
     """Also the Lennard-Jones term of large beads, which the stepper takes over
     its symmetric Verlet list (rebuilt beside the forces): the forces at the
