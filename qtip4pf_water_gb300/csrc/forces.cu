@@ -240,8 +240,8 @@ __global__ void __launch_bounds__(128) k_prep_f32(EvalArgs a) {
     const unsigned F = (unsigned)__double2ll_rn(x * S.fix_scale[d]);
     float *sv = reinterpret_cast<float *>(a.sites) + 4 * ((size_t)J.site_off + s);
     float xf = (float)F * S.fixf[d];
-    if (!a.sites_are_input && kind != 0) {
-        // an H site follows its molecule's wrapped M site across the box boundary
+    if (a.rl_on && !a.sites_are_input && kind != 0) {
+        // (pair-list real space) an H site follows its molecule's wrapped M site across the box boundary
         // (the wrapped fixed-point difference is the M-H minimum image), so the
         // FP32 positions of a molecule's sites stay together: one minimum image per
         // molecule pair serves all nine site pairs in k_real_list
@@ -2364,15 +2364,15 @@ void set_attrs() {
 }
 
 // Chunk counts so that each force kernel launches enough 4-warp blocks to keep
-// 12 blocks (48 warps) resident on each of the 152 SMs.
-int chunks_for(long long base_blocks, int maxc) {
-    const long long want = 12LL * 152;
+// per_sm blocks (12: 48 warps) resident on each of the 152 SMs.
+int chunks_for(long long base_blocks, int maxc, int per_sm = 12) {
+    const long long want = (long long)per_sm * 152;
     const int c = (int)((want + base_blocks - 1) / std::max(1LL, base_blocks));
     return std::max(1, std::min(c, maxc));
 }
 // a tuned count when the autotuner fixed one, else the heuristic
-int chunks_or(int tuned, long long base_blocks, int maxc) {
-    return tuned > 0 ? std::min(tuned, maxc) : chunks_for(base_blocks, maxc);
+int chunks_or(int tuned, long long base_blocks, int maxc, int per_sm = 12) {
+    return tuned > 0 ? std::min(tuned, maxc) : chunks_for(base_blocks, maxc, per_sm);
 }
 
 void launch_lj_dense(const EvalArgs &a, cudaStream_t s) {
@@ -2416,9 +2416,9 @@ void launch_real_list(EvalArgs &a, cudaStream_t s) {
     cudaMemsetAsync(a.rl_count, 0, sizeof(int), s);
     k_rlist_test<<<dim3((3 * a.max_mols + RLT_SITES - 1) / RLT_SITES, a.n_jobs), 256, 0, s>>>(a);
     const int row_blocks = (a.max_mols + RL_ROWS - 1) / RL_ROWS;
-    // eight resident blocks on each of the 152 SMs at most; a launch without
-    // rebuilds costs each block one load of the count
-    const int grid = (int)std::min<long long>((long long)row_blocks * a.n_jobs, 152LL * 8);
+    // one block an SM: a launch without rebuilds costs each block one load of the
+    // count, and a wider grid would hold thread slots the force kernels beside it need
+    const int grid = (int)std::min<long long>((long long)row_blocks * a.n_jobs, 152LL);
     k_rlist_rows<<<grid, 32 * RL_ROWS, 0, s>>>(a, row_blocks);
     k_real_list<<<dim3((a.max_mols + RLW - 1) / RLW, a.n_rj, a.n_jobs), 32 * RLW, 0, s>>>(a);
 }
@@ -2431,7 +2431,11 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
     a.n_sc = chunks_or(a.tune_sc, (long long)ktiles * a.n_jobs, MAX_SC);
     a.n_kc = chunks_or(a.tune_kc, (long long)tiles * a.n_jobs, MAX_KC);
     if (sizeof(R) == 4 && forks && a.mode == 0 && a.lj_full && a.ljf) {
-        // forked: prep; then real space | reciprocal chain | dense LJ; then combine
+        // forked: prep; then real space | reciprocal chain | dense LJ; then combine.
+        // The reciprocal chain runs beside the real-space kernel: its grids aim for
+        // half the blocks a kernel alone would (6 resident blocks an SM)
+        a.n_sc = chunks_or(a.tune_sc, (long long)ktiles * a.n_jobs, MAX_SC, 6);
+        a.n_kc = chunks_or(a.tune_kc, (long long)tiles * a.n_jobs, MAX_KC, 6);
         if (half_ok(a)) a.n_rj = half_chunks(a) + (3 * a.max_mols + 31) / 32 / 2;
         else if (list_ok(a)) a.n_rj = list_chunks(a);  // k_kforce_f32's planes follow the real-space ones
         a.lj_plane = 1;
@@ -2512,9 +2516,11 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
     EvalArgs a = a0;
     const int ns = 3 * a.max_mols;
     const int tiles = (ns + RT - 1) / RT, ktiles = (a.max_grp + KT - 1) / KT;
+    // the shapes of the stepper's evaluation (forked in the mixed form)
+    const int share = mixed ? 6 : 12;
     a.n_rj = chunks_or(a.tune_rj, (long long)tiles * a.n_jobs, MAX_RJ);
-    a.n_sc = chunks_or(a.tune_sc, (long long)ktiles * a.n_jobs, MAX_SC);
-    a.n_kc = chunks_or(a.tune_kc, (long long)tiles * a.n_jobs, MAX_KC);
+    a.n_sc = chunks_or(a.tune_sc, (long long)ktiles * a.n_jobs, MAX_SC, share);
+    a.n_kc = chunks_or(a.tune_kc, (long long)tiles * a.n_jobs, MAX_KC, share);
     const dim3 gs((ns + 127) / 128, a.n_jobs), gr(tiles, a.n_rj, a.n_jobs);
     const dim3 gk(ktiles, a.n_sc, a.n_jobs), gf(tiles, a.n_kc, a.n_jobs);
     const dim3 gm((a.max_mols + 127) / 128, a.n_jobs), gl((a.max_mols + 3) / 4, a.n_jobs);

@@ -374,8 +374,11 @@ void launch_skin_rebuild(const ListArgs &a, cudaStream_t s, unsigned long long *
     k_skin_test<<<a.n_jobs, 256, (size_t)LC_MAX_CELLS * sizeof(int), s>>>(a);
     const int row_blocks = (a.max_mols + ROWS - 1) / ROWS;
     const long long items = (long long)row_blocks * a.n_jobs;
-    // eight resident blocks on each of the 152 SMs at most
-    const int grid = (int)std::min<long long>(items, 152LL * 8);
+    // one block an SM: in a step without a rebuild the blocks only read the count
+    // and exit, and a wider grid would hold the thread slots of the force kernels
+    // running beside it (measured: 1216 blocks cost the step ~7 us); a rebuild of
+    // every bead loops over its items instead
+    const int grid = (int)std::min<long long>(items, 152LL);
     const size_t bm = (size_t)ROWS * W * sizeof(unsigned);
     k_list_rows<false><<<grid, 32 * ROWS, bm, s>>>(a, row_blocks);
     k_list_scan<<<a.n_jobs, 512, (size_t)a.max_mols * sizeof(int), s>>>(a);
