@@ -2416,9 +2416,11 @@ void launch_real_list(EvalArgs &a, cudaStream_t s) {
     cudaMemsetAsync(a.rl_count, 0, sizeof(int), s);
     k_rlist_test<<<dim3((3 * a.max_mols + RLT_SITES - 1) / RLT_SITES, a.n_jobs), 256, 0, s>>>(a);
     const int row_blocks = (a.max_mols + RL_ROWS - 1) / RL_ROWS;
-    // one block an SM: a launch without rebuilds costs each block one load of the
-    // count, and a wider grid would hold thread slots the force kernels beside it need
-    const int grid = (int)std::min<long long>((long long)row_blocks * a.n_jobs, 152LL);
+    // one block an SM, or one per 16 items of a rebuild of every configuration when
+    // that is more: a launch without rebuilds costs each block one load of the count,
+    // and a wide grid holds thread slots the force kernels beside it need
+    const long long items = (long long)row_blocks * a.n_jobs;
+    const int grid = (int)std::min<long long>(items, std::max<long long>(152LL, items / 16));
     k_rlist_rows<<<grid, 32 * RL_ROWS, 0, s>>>(a, row_blocks);
     k_real_list<<<dim3((a.max_mols + RLW - 1) / RLW, a.n_rj, a.n_jobs), 32 * RLW, 0, s>>>(a);
 }

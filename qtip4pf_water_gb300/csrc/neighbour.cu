@@ -248,7 +248,10 @@ __global__ void __launch_bounds__(32 * ROWS) k_list_rows(ListArgs a, int row_blo
         const SysDev &S = a.sys[a.job_sys[job]];
         const int i = rb * ROWS + w;
         if (i >= S.n_mols) continue;
-        list_row<FILL>(a, job, i, bms + (size_t)w * ((S.n_mols + 31) >> 5));
+        // each warp's bitmap at a fixed stride (the launch's largest bead): the warps
+        // of a block move on to the next item independently, and items of beads of
+        // different sizes must not shift one warp's bitmap onto another's
+        list_row<FILL>(a, job, i, bms + (size_t)w * ((a.max_mols + 31) >> 5));
         __syncwarp();
     }
 }
@@ -374,11 +377,11 @@ void launch_skin_rebuild(const ListArgs &a, cudaStream_t s, unsigned long long *
     k_skin_test<<<a.n_jobs, 256, (size_t)LC_MAX_CELLS * sizeof(int), s>>>(a);
     const int row_blocks = (a.max_mols + ROWS - 1) / ROWS;
     const long long items = (long long)row_blocks * a.n_jobs;
-    // one block an SM: in a step without a rebuild the blocks only read the count
-    // and exit, and a wider grid would hold the thread slots of the force kernels
-    // running beside it (measured: 1216 blocks cost the step ~7 us); a rebuild of
-    // every bead loops over its items instead
-    const int grid = (int)std::min<long long>(items, 152LL);
+    // one block an SM, or one per 16 items of a rebuild of every bead when that is
+    // more: in a step without a rebuild the blocks only read the count and exit,
+    // and a wide grid holds the thread slots of the force kernels running beside
+    // it (1216 blocks cost the 512-water P = 32 step ~7 us)
+    const int grid = (int)std::min<long long>(items, std::max<long long>(152LL, items / 16));
     const size_t bm = (size_t)ROWS * W * sizeof(unsigned);
     k_list_rows<false><<<grid, 32 * ROWS, bm, s>>>(a, row_blocks);
     k_list_scan<<<a.n_jobs, 512, (size_t)a.max_mols * sizeof(int), s>>>(a);
