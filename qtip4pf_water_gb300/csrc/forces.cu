@@ -2417,10 +2417,10 @@ void launch_real_list(EvalArgs &a, cudaStream_t s) {
     k_rlist_test<<<dim3((3 * a.max_mols + RLT_SITES - 1) / RLT_SITES, a.n_jobs), 256, 0, s>>>(a);
     const int row_blocks = (a.max_mols + RL_ROWS - 1) / RL_ROWS;
     // one block an SM, or one per 16 items of a rebuild of every configuration when
-    // that is more: a launch without rebuilds costs each block one load of the count,
+    // that is more (at most eight an SM): a launch without rebuilds costs each block one load of the count,
     // and a wide grid holds thread slots the force kernels beside it need
     const long long items = (long long)row_blocks * a.n_jobs;
-    const int grid = (int)std::min<long long>(items, std::max<long long>(152LL, items / 16));
+    const int grid = (int)std::min<long long>(items, std::max<long long>(152LL, std::min<long long>(items / 16, 152LL * 8)));
     k_rlist_rows<<<grid, 32 * RL_ROWS, 0, s>>>(a, row_blocks);
     k_real_list<<<dim3((a.max_mols + RLW - 1) / RLW, a.n_rj, a.n_jobs), 32 * RLW, 0, s>>>(a);
 }

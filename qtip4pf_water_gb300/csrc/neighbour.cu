@@ -378,10 +378,10 @@ void launch_skin_rebuild(const ListArgs &a, cudaStream_t s, unsigned long long *
     const int row_blocks = (a.max_mols + ROWS - 1) / ROWS;
     const long long items = (long long)row_blocks * a.n_jobs;
     // one block an SM, or one per 16 items of a rebuild of every bead when that is
-    // more: in a step without a rebuild the blocks only read the count and exit,
+    // more (at most eight an SM): in a step without a rebuild the blocks only read the count and exit,
     // and a wide grid holds the thread slots of the force kernels running beside
     // it (1216 blocks cost the 512-water P = 32 step ~7 us)
-    const int grid = (int)std::min<long long>(items, std::max<long long>(152LL, items / 16));
+    const int grid = (int)std::min<long long>(items, std::max<long long>(152LL, std::min<long long>(items / 16, 152LL * 8)));
     const size_t bm = (size_t)ROWS * W * sizeof(unsigned);
     k_list_rows<false><<<grid, 32 * ROWS, bm, s>>>(a, row_blocks);
     k_list_scan<<<a.n_jobs, 512, (size_t)a.max_mols * sizeof(int), s>>>(a);
