@@ -225,6 +225,7 @@ struct qtg_ctx {
     float4 *ljf = nullptr;    // dense LJ oxygen forces per molecule and slot
     float *intra = nullptr;   // intramolecular forces, 18 floats per molecule and slot
     int4 *sites_fix = nullptr;  // fixed-point site fractions per slot (half-interaction real space)
+    long long *rfix = nullptr;  // fixed-point real-space site forces per slot (half-interaction real space)
     // real-space pair list (mixed contexts with beads beyond the half-interaction
     // kernel in boxes with r_c + 2 RL_SPREAD <= L/2): rl_ok marks the context
     // eligible, rl_form 0 runs the real space over the list there, 1 over all pairs
@@ -393,6 +394,7 @@ EvalArgs eval_args(qtg_ctx *c, const Job *jobs, int n_jobs, const double *pos, d
     a.max_batch = c->max_batch;
     a.sites = c->sites;
     a.sites_fix = c->sites_fix;
+    a.rfix = c->rfix;
     a.opos = c->opos;
     a.ljf = c->ljf;
     a.intra = c->intra;
@@ -1311,6 +1313,7 @@ qtg_status qtg_create(const qtg_system_desc *systems, int n_systems, int precisi
     AL(ctx->ljf, ctx->total_sites / 3);
     AL(ctx->intra, 6 * ctx->total_sites);
     AL(ctx->sites_fix, ctx->total_sites);
+    if (ctx->mixed) AL(ctx->rfix, 3 * ctx->total_sites);
     {
         // real-space pair list: rows hold the molecules whose M sites lie within
         // r_c + RL_SKIN + 2 RL_SPREAD (the prefilter radius of k_rlist_rows), at the
@@ -1457,7 +1460,7 @@ void qtg_destroy(qtg_ctx *ctx) {
                     ctx->sc_bead, ctx->colwork, ctx->acc, ctx->run, ctx->est, ctx->step, ctx->records,
                     ctx->status, ctx->red_out, ctx->rebuilt, ctx->cw_part, ctx->cw_ticket, ctx->kpk, ctx->ljf, ctx->fin_ticket, ctx->sites_fix, ctx->intra, ctx->kfc, ctx->kfb, ctx->wpk,
                     ctx->wpos, ctx->cnt_half, ctx->cnt_full, ctx->cell_start, ctx->cell_mol,
-                    ctx->rb_jobs, ctx->rb_count, ctx->rl_list, ctx->rl_cnt, ctx->rl_ref, ctx->rl_jobs, ctx->rl_count, ctx->rl_wide, ctx->rl_state};
+                    ctx->rb_jobs, ctx->rb_count, ctx->rl_list, ctx->rl_cnt, ctx->rl_ref, ctx->rl_jobs, ctx->rl_count, ctx->rl_wide, ctx->rl_state, ctx->rfix};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (ctx->box) cudaFreeHost(ctx->box);

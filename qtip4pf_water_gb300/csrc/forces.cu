@@ -252,6 +252,7 @@ __global__ void __launch_bounds__(128) k_prep_f32(EvalArgs a) {
     sv[d] = xf;
     int *fx = reinterpret_cast<int *>(a.sites_fix + J.site_off + s);
     fx[d] = (int)F;
+    if (a.rfix) a.rfix[3 * ((size_t)J.site_off + s) + d] = 0;  // k_real_half adds into it
     float cf = 1.f;
     if (d == 0) {
         cf = (float)a.charge[S.chg_off + s];
@@ -765,6 +766,12 @@ __global__ void __launch_bounds__(32 * RLW) k_real_list(EvalArgs a) {
 // stationary-side sums of chunk ch of the distances, plane n_ch + d - 1 the
 // visited-side sums of distance d (zero where that visit is not made).
 constexpr int HW = 4;  // warps per block
+constexpr float RFIX_SCALE = 1099511627776.0f;  // 2^40: fixed-point units of the real-space site forces
+__device__ __forceinline__ void rfix_add(long long *p, float x, float y, float z) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(p), (unsigned long long)__float2ll_rn(x * RFIX_SCALE));
+    atomicAdd(reinterpret_cast<unsigned long long *>(p + 1), (unsigned long long)__float2ll_rn(y * RFIX_SCALE));
+    atomicAdd(reinterpret_cast<unsigned long long *>(p + 2), (unsigned long long)__float2ll_rn(z * RFIX_SCALE));
+}
 __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ch = blockIdx.y, jb = blockIdx.z;
@@ -823,7 +830,6 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
         return qq * A;
     };
     float Sx = 0.f, Sy = 0.f, Sz = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f, e = 0.f;
-    const size_t ts = (size_t)a.total_sites;
     for (int d = d0; d < d1; ++d) {
         float fx = 0.f, fy = 0.f, fz = 0.f;
         if (d == 0) {  // the tile's own pairs, from both sides
@@ -942,19 +948,13 @@ __global__ void __launch_bounds__(32 * HW) k_real_half(EvalArgs a, int n_ch) {
                     mz = __shfl_sync(0xffffffffu, mz, nx);
                 }
             }
-            if (m0 + lane < ns)
-                store_plane<float>(a.part, 3 * ((size_t)(n_ch + d - 1) * ts + J.site_off + m0 + lane), mx, my, mz);
+            if (m0 + lane < ns) rfix_add(a.rfix + 3 * ((size_t)J.site_off + m0 + lane), mx, my, mz);
         }
         kahan_add(Sx, Cx, fx);
         kahan_add(Sy, Cy, fy);
         kahan_add(Sz, Cz, fz);
     }
-    if (vs) store_plane<float>(a.part, 3 * ((size_t)ch * ts + J.site_off + s), Sx - Cx, Sy - Cy, Sz - Cz);
-    // a bead with fewer tiles than the largest of the batch: its sites get zero
-    // planes for the distances it does not have
-    if (ch == 0 && vs)
-        for (int d = maxd + 1; d <= a.n_rj - n_ch; ++d)
-            store_plane<float>(a.part, 3 * ((size_t)(n_ch + d - 1) * ts + J.site_off + s), 0.f, 0.f, 0.f);
+    if (vs) rfix_add(a.rfix + 3 * ((size_t)J.site_off + s), Sx - Cx, Sy - Cy, Sz - Cz);
     for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
     if (lane == 0) atomicAdd(&a.energy[J.slot], (double)e);
 }
@@ -1833,6 +1833,7 @@ __global__ void __launch_bounds__(128) k_combine_f32(EvalArgs a) {
         const int np = a.n_rj + a.n_kc;
         const size_t stride = 3 * (size_t)a.total_sites;
         const float *pl = reinterpret_cast<const float *>(a.part) + 3 * ((size_t)J.site_off + 3 * m0);
+        const long long *rf = a.real_fix ? a.rfix + 3 * ((size_t)J.site_off + 3 * m0) : nullptr;
         for (int o = threadIdx.x; o < 9 * nm; o += blockDim.x) {
             float sum = 0.f, comp = 0.f;
             int p = 0;
@@ -1844,6 +1845,8 @@ __global__ void __launch_bounds__(128) k_combine_f32(EvalArgs a) {
                 for (int u = 0; u < 16; ++u) kahan_add(sum, comp, v[u]);
             }
             for (; p < np; ++p) kahan_add(sum, comp, pl[p * stride + o]);
+            // the half-interaction real space's fixed-point sums (2^-40 units)
+            if (rf) kahan_add(sum, comp, (float)((double)rf[o] * 9.094947017729282e-13));
             fsum[o] = sum - comp;
         }
     }
@@ -2396,11 +2399,13 @@ bool half_ok(const EvalArgs &a) { return (3 * a.max_mols + 31) / 32 <= HALF_MAX_
 int half_chunks(const EvalArgs &a) {
     const int T = (3 * a.max_mols + 31) / 32;
     const long long blocks = (long long)((T + HW - 1) / HW) * a.n_jobs;
-    return chunks_or(a.tune_rj, blocks, HALF_MAX_CH);
+    // the autotuner's picks on the 512-water P = 32 step: the most chunks (20 blocks an SM)
+    return chunks_or(a.tune_rj, blocks, HALF_MAX_CH, 20);
 }
 void launch_real_half(EvalArgs &a, cudaStream_t s) {
     const int T = (3 * a.max_mols + 31) / 32, n_ch = half_chunks(a);
-    a.n_rj = n_ch + T / 2;  // the planes the combine sums
+    a.n_rj = 0;  // no real-space planes: the combine reads the fixed-point sums
+    a.real_fix = 1;
     k_real_half<<<dim3((T + HW - 1) / HW, n_ch, a.n_jobs), 32 * HW, 0, s>>>(a, n_ch);
 }
 
@@ -2435,10 +2440,14 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
     if (sizeof(R) == 4 && forks && a.mode == 0 && a.lj_full && a.ljf) {
         // forked: prep; then real space | reciprocal chain | dense LJ; then combine.
         // The reciprocal chain runs beside the real-space kernel: its grids aim for
-        // half the blocks a kernel alone would (6 resident blocks an SM)
-        a.n_sc = chunks_or(a.tune_sc, (long long)ktiles * a.n_jobs, MAX_SC, 6);
+        // a third (structure factors) and half (k-force) of the blocks a kernel alone
+        // would (the autotuner's picks on the 512-water P = 32 step)
+        a.n_sc = chunks_or(a.tune_sc, (long long)ktiles * a.n_jobs, MAX_SC, 4);
         a.n_kc = chunks_or(a.tune_kc, (long long)tiles * a.n_jobs, MAX_KC, 6);
-        if (half_ok(a)) a.n_rj = half_chunks(a) + (3 * a.max_mols + 31) / 32 / 2;
+        if (half_ok(a)) {  // k_kforce_f32's planes follow the real-space ones: none here
+            a.n_rj = 0;
+            a.real_fix = 1;
+        }
         else if (list_ok(a)) a.n_rj = list_chunks(a);  // k_kforce_f32's planes follow the real-space ones
         a.lj_plane = 1;
         launch_prep_f32(a, s);
@@ -2518,11 +2527,15 @@ void launch_ewald_kernel(const EvalArgs &a0, bool mixed, const char *name, cudaS
     EvalArgs a = a0;
     const int ns = 3 * a.max_mols;
     const int tiles = (ns + RT - 1) / RT, ktiles = (a.max_grp + KT - 1) / KT;
-    // the shapes of the stepper's evaluation (forked in the mixed form)
-    const int share = mixed ? 6 : 12;
+    // the shapes of the stepper's evaluation (forked in the mixed form; the
+    // half-interaction real space leaves fixed-point sums instead of planes)
     a.n_rj = chunks_or(a.tune_rj, (long long)tiles * a.n_jobs, MAX_RJ);
-    a.n_sc = chunks_or(a.tune_sc, (long long)ktiles * a.n_jobs, MAX_SC, share);
-    a.n_kc = chunks_or(a.tune_kc, (long long)tiles * a.n_jobs, MAX_KC, share);
+    if (mixed && half_ok(a)) {
+        a.n_rj = 0;
+        a.real_fix = 1;
+    }
+    a.n_sc = chunks_or(a.tune_sc, (long long)ktiles * a.n_jobs, MAX_SC, mixed ? 4 : 12);
+    a.n_kc = chunks_or(a.tune_kc, (long long)tiles * a.n_jobs, MAX_KC, mixed ? 6 : 12);
     const dim3 gs((ns + 127) / 128, a.n_jobs), gr(tiles, a.n_rj, a.n_jobs);
     const dim3 gk(ktiles, a.n_sc, a.n_jobs), gf(tiles, a.n_kc, a.n_jobs);
     const dim3 gm((a.max_mols + 127) / 128, a.n_jobs), gl((a.max_mols + 3) / 4, a.n_jobs);

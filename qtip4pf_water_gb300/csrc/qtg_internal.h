@@ -503,6 +503,12 @@ struct EvalArgs {
     void *phase;           // complex phase tables, per slot
     void *tan_sites;       // tangent of the site positions (mode 1), per slot
     double *part;          // partial site forces [MAX_PART][total_sites][3]
+    // mixed: the half-interaction real space's site forces as 64-bit fixed point
+    // (units of 2^-40 Hartree/bohr, [total_sites][3]; zeroed by k_prep_f32, summed by
+    // integer atomics, so the sum does not depend on their order), read by
+    // k_combine_f32 when real_fix is set
+    long long *rfix;
+    int real_fix;
     long long total_sites; // sites summed over all slots (plane stride of part)
     double2 *skp;          // partial S(k) [MAX_SC][total_k]
     double2 *dskp;         // partial dS(k) along the tangent direction
