@@ -1,7 +1,7 @@
 """The device-resident stepper against the oracle's restatement of it, step for
 step with the same counter-based thermostat noise (the oracle recomputes the
-Philox4x32-10 draws the device makes), and statistically with independent
-noise streams.
+Philox4x32-10 draws the device makes), and statistically over 2 ps chains
+that part by chaos.
 
 Paths covered (update.cpp:271-401 with the stepper's thermostats):
 * PILE-G, second-order and Suzuki-Chin assembly;
@@ -18,9 +18,10 @@ from FP64 by ~1e-7 relative; a step moves an atom ~1e-2 bohr); forces within
 the mixed-mode 1e-4 relative RMS, and 1e-6 in FP64 (forces at positions that
 differ by those 1e-8 bohr; the FP64 forces of one configuration are pinned
 at 1e-9 by the single-configuration tests); the mean centroid force within
-1e-6 (FP64) or 1e-4 (mixed) relative RMS. Statistics: mean potential and
-centroid-virial kinetic energy within two combined standard errors of block
-averages.
+1e-6 (FP64) or 1e-4 (mixed) relative RMS. Statistics: run averages of the
+potential and the centroid-virial kinetic energy over 32 paired chains
+(device and oracle from one equilibrated state with one noise stream), the
+mean paired difference within two standard errors.
 """
 import numpy as np
 import pytest
@@ -154,64 +155,69 @@ def test_headline_stepper_matches_the_oracle(gpu_lib):
     assert rel_rms(out["p"], pp) < 1e-4
 
 
-def _block_stats(x, nblocks):
-    n = len(x) // nblocks * nblocks
-    b = np.asarray(x[:n]).reshape(nblocks, -1).mean(axis=1)
-    return float(b.mean()), float(b.std(ddof=1) / np.sqrt(nblocks))
-
-
 def test_nvt_averages_match_the_oracle_within_two_standard_errors(gpu_lib):
-    """64 waters, P = 8, second order, PILE-G at 298 K, dt = 0.5 fs. Both sides
-    start from one state equilibrated on the device (20 ps from the lattice) and
-    sample with independent noise streams (different seeds): the device 20,000
-    steps, the oracle 8,200 steps (200 discarded). Mean potential energy per bead and
-    centroid-virial kinetic energy (the estimators simulation.cpp:936-961
-    averages) agree within two combined standard errors of block means, the
-    blocks 1000 steps (500 fs) long on both sides: longer than the potential
-    energy's correlation time, so that the block means are independent and the
-    standard errors not underestimated."""
+    """64 waters, P = 8, second order, PILE-G at 298 K, dt = 0.5 fs, as 32
+    paired replica chains. 32 systems start from 32 seeded lattices and
+    equilibrate 20 ps on the device (one context). From each equilibrated
+    state the device (a new context, mixed precision) and the oracle (spawned
+    worker processes, FP64) each run a 2 ps chain with the same thermostat
+    noise (seed and system index alike): the two trajectories stay together
+    for a few hundred fs and part by chaos within about 1 ps, so the pair's
+    run averages differ by far less than two independent chains' would. The
+    run averages are the potential energy per bead and the centroid-virial
+    kinetic energy (the estimators simulation.cpp:936-961 averages); their
+    mean paired difference lies within two standard errors of it (the paired
+    differences' spread over the 32 chains)."""
+    import multiprocessing as mp
+    import os
+
+    from oracle.nvt_chain import nvt_chain
+
     q = gpu_lib
     N, P, T, dt = 64, 8, 298.0, 0.5
-    st = q.seeded_start(N, P, T, seed=91)
-    ctx, s = _device(q, st, q.MIXED, q.TROTTER, q.PILE_G, 91, dt=dt)
+    n_chain, steps = 32, 4000
+
+    def desc(st, seed):
+        return q.system_desc(N, P, st.box_bohr, temp_K=T, dt_fs=dt, propagator=q.TROTTER,
+                             thermostat=q.PILE_G, tau0_fs=100.0, seed=seed)
+
+    starts = [q.seeded_start(N, P, T, seed=9100 + i) for i in range(n_chain)]
+    ctx = q.Context([desc(st, 9100 + i) for i, st in enumerate(starts)], q.MIXED)
+    for s, st in zip(ctx.systems, starts):
+        s.set_state(st.q, st.p)
+    ctx.init_forces()
     ctx.run_steps(40000, is_nvt=True)
     ctx.sync()
-    eq = s.get_state()
+    eq = [s.get_state() for s in ctx.systems]
 
-    class Eq:
-        n_mols, n_beads, box_bohr = N, P, st.box_bohr
-        q = eq["q"].copy()
-        p = eq["p"].copy()
+    jobs = [(N, P, starts[i].box_bohr, e["q"], e["p"], T, dt, 9300 + i, steps, 0, i) for i, e in enumerate(eq)]
+    pool = mp.get_context("spawn").Pool(max(1, min(n_chain, os.cpu_count() or 1)))
+    orc_async = pool.map_async(nvt_chain, jobs)
 
-    ctx2, s2 = _device(q, Eq, q.MIXED, q.TROTTER, q.PILE_G, 92, dt=dt)
-    pot_g, kcv_g = [], []
-    for _ in range(5):  # the device keeps the last 4096 records: read them every 4000 steps
-        ctx2.reset_estimators()
-        ctx2.run_steps(4000, is_nvt=True)
-        ctx2.sync()
-        est = s2.estimators()
-        assert len(est["pot"]) == 4000
-        pot_g.extend(est["pot"])
-        kcv_g.extend(est["kcv"])
+    ctx2 = q.Context([desc(st, 9300 + i) for i, st in enumerate(starts)], q.MIXED)
+    for s, e in zip(ctx2.systems, eq):
+        s.set_state(e["q"], e["p"])
+    ctx2.init_forces()
+    ctx2.reset_estimators()
+    ctx2.run_steps(steps, is_nvt=True)
+    ctx2.sync()
+    dev = []
+    for s in ctx2.systems:
+        est = s.estimators()
+        assert len(est["pot"]) == steps
+        dev.append((float(np.mean(est["pot"])), float(np.mean(est["kcv"]))))
+    try:
+        orc = orc_async.get()
+    finally:
+        pool.close()
+        pool.join()
 
-    o, stp, (qq, pp, f, fp, point, lst, disp) = _oracle(Eq, True, 1, 93, dt=dt)
-    beta = 1.0 / (T * o.constants()[2])
-    nd = 9 * N
-    pot_o, kcv_o = [], []
-    for k in range(8200):
-        _, pot = o.stepper_step(stp, qq, pp, f, fp, point, lst, disp, is_nvt=True)
-        if k < 200:
-            continue
-        x = qq.reshape(P, nd)
-        tq = -np.sum((x - x.mean(axis=0)) * fp.reshape(P, nd))
-        pot_o.append(pot)
-        kcv_o.append(0.5 * nd / beta + 0.5 * tq / P)
     report, ok = [], True
-    for name, g, c in (("potential", pot_g, pot_o), ("kinetic (centroid virial)", kcv_g, kcv_o)):
-        mg, sg = _block_stats(g, 20)  # blocks of 1000 steps (500 fs) on both sides
-        mo, so = _block_stats(c, 8)
-        se = float(np.hypot(sg, so))
-        ok = ok and abs(mg - mo) < 2.0 * se
-        report.append(f"{name}: device {mg:.6f} +- {sg:.1e}, oracle {mo:.6f} +- {so:.1e}, "
-                      f"difference {abs(mg - mo) / se:.2f} SE")
+    for k, name in ((0, "potential"), (1, "kinetic (centroid virial)")):
+        d = np.array([a[k] - b[k] for a, b in zip(dev, orc)])
+        se = float(d.std(ddof=1) / np.sqrt(len(d)))
+        ok = ok and abs(d.mean()) < 2.0 * se
+        report.append(f"{name}: device {np.mean([a[k] for a in dev]):.6f}, oracle {np.mean([b[k] for b in orc]):.6f}, "
+                      f"mean paired difference {d.mean():.2e} = {abs(d.mean()) / se:.2f} SE (SE {se:.1e})")
+    print("; ".join(report))
     assert ok, "; ".join(report)

@@ -92,3 +92,19 @@ def test_same_seed_same_trajectory_different_seed_differs():
             o.stepper_step(stp, *a, is_nvt=True)
         outs.append(a[0].copy())
     assert np.array_equal(outs[0], outs[1]) and not np.array_equal(outs[0], outs[2])
+
+
+def test_nvt_chains_in_spawned_workers_are_seeded_and_distinct():
+    """The replica chains the statistical comparison runs in spawned worker
+    processes: one seed gives one run average, another seed another."""
+    import multiprocessing as mp
+
+    from oracle.nvt_chain import nvt_chain
+    from qtip4pf_water_gb300.start import seeded_start
+
+    st = seeded_start(64, 2, 298.0, seed=5)
+    jobs = [(64, 2, st.box_bohr, st.q, st.p, 298.0, 0.5, s, 12, 2) for s in (7, 7, 8)]
+    with mp.get_context("spawn").Pool(2) as pool:
+        a, b, c = pool.map(nvt_chain, jobs)
+    assert a == b and a != c
+    assert all(np.isfinite(x) for x in a + c)
