@@ -10,11 +10,13 @@ import numpy as np
 
 
 def nvt_chain(args):
-    """args: (n_mols, n_beads, box_bohr, q, p, temp_K, dt_fs, seed, steps, discard[, sys]).
+    """args: (n_mols, n_beads, box_bohr, q, p, temp_K, dt_fs, seed, steps, discard[, sys[, head]]).
     The noise is the device's for system index sys (default 0) of a context
-    with that seed."""
+    with that seed. Returns the two run averages and the per-step values of
+    the first `head` steps (default none)."""
     n_mols, n_beads, box, q, p, temp, dt, seed, steps, discard = args[:10]
     sys = args[10] if len(args) > 10 else 0
+    head = args[11] if len(args) > 11 else 0
     from oracle.binding import Oracle
 
     o = Oracle(n_mols, n_beads, np.asarray(box), temp, dt)
@@ -27,13 +29,17 @@ def nvt_chain(args):
     stp = o.stepper(seed, sys=sys, thermostat=1, trotter=True)
     beta = 1.0 / (temp * o.constants()[2])
     nd = 9 * n_mols
-    pots, kcvs = [], []
+    pots, kcvs, head_pot, head_kcv = [], [], [], []
     for k in range(steps):
         _, pot = o.stepper_step(stp, qq, pp, f, fp, point, lst, disp, is_nvt=True)
-        if k < discard:
-            continue
         x = qq.reshape(n_beads, nd)
         tq = -np.sum((x - x.mean(axis=0)) * fp.reshape(n_beads, nd))
+        kcv = 0.5 * nd / beta + 0.5 * tq / n_beads
+        if k < head:
+            head_pot.append(pot)
+            head_kcv.append(kcv)
+        if k < discard:
+            continue
         pots.append(pot)
-        kcvs.append(0.5 * nd / beta + 0.5 * tq / n_beads)
-    return float(np.mean(pots)), float(np.mean(kcvs))
+        kcvs.append(kcv)
+    return float(np.mean(pots)), float(np.mean(kcvs)), head_pot, head_kcv

@@ -18,10 +18,11 @@ from FP64 by ~1e-7 relative; a step moves an atom ~1e-2 bohr); forces within
 the mixed-mode 1e-4 relative RMS, and 1e-6 in FP64 (forces at positions that
 differ by those 1e-8 bohr; the FP64 forces of one configuration are pinned
 at 1e-9 by the single-configuration tests); the mean centroid force within
-1e-6 (FP64) or 1e-4 (mixed) relative RMS. Statistics: run averages of the
-potential and the centroid-virial kinetic energy over 32 paired chains
-(device and oracle from one equilibrated state with one noise stream), the
-mean paired difference within two standard errors.
+1e-6 (FP64) or 1e-4 (mixed) relative RMS. Statistics: 32 chains a side
+(device and oracle from one equilibrated state with one noise stream): the
+per-step estimator records while the trajectories stay together, then the
+run averages of the potential and the centroid-virial kinetic energy within
+two standard errors of the two sides' means.
 """
 import numpy as np
 import pytest
@@ -156,18 +157,24 @@ def test_headline_stepper_matches_the_oracle(gpu_lib):
 
 
 def test_nvt_averages_match_the_oracle_within_two_standard_errors(gpu_lib):
-    """64 waters, P = 8, second order, PILE-G at 298 K, dt = 0.5 fs, as 32
-    paired replica chains. 32 systems start from 32 seeded lattices and
-    equilibrate 20 ps on the device (one context). From each equilibrated
-    state the device (a new context, mixed precision) and the oracle (spawned
-    worker processes, FP64) each run a 2 ps chain with the same thermostat
-    noise (seed and system index alike): the two trajectories stay together
-    for a few hundred fs and part by chaos within about 1 ps, so the pair's
-    run averages differ by far less than two independent chains' would. The
-    run averages are the potential energy per bead and the centroid-virial
-    kinetic energy (the estimators simulation.cpp:936-961 averages); their
-    mean paired difference lies within two standard errors of it (the paired
-    differences' spread over the 32 chains)."""
+    """64 waters, P = 8, second order, PILE-G at 298 K, dt = 0.5 fs, 32 replica
+    chains a side. 32 systems start from 32 seeded lattices and equilibrate
+    20 ps on the device (one context). From each equilibrated state the device
+    (a new context, mixed precision) and the oracle (spawned worker processes,
+    FP64) each run a 2 ps chain with the same thermostat noise (seed and system
+    index alike). The run averages are the potential energy per bead and the
+    centroid-virial kinetic energy (the estimators simulation.cpp:936-961
+    averages).
+
+    * The two trajectories stay together for the first few hundred fs: over the
+      first 100 steps the device's per-step estimator records equal the oracle's
+      values (kinetic within 1e-6 relative; potential within 2e-5 relative, the
+      FP32 Ewald energy sums of the mixed form).
+    * They part by chaos within about 1 ps; the two sides' means of the chain
+      averages agree within two standard errors, each side's the spread of its
+      32 chain averages / sqrt(32), combined in quadrature (the chains of a pair
+      share a start and a noise stream, so the difference's own spread is
+      smaller and this bound conservative)."""
     import multiprocessing as mp
     import os
 
@@ -175,7 +182,7 @@ def test_nvt_averages_match_the_oracle_within_two_standard_errors(gpu_lib):
 
     q = gpu_lib
     N, P, T, dt = 64, 8, 298.0, 0.5
-    n_chain, steps = 32, 4000
+    n_chain, steps, head = 32, 4000, 100
 
     def desc(st, seed):
         return q.system_desc(N, P, st.box_bohr, temp_K=T, dt_fs=dt, propagator=q.TROTTER,
@@ -190,7 +197,8 @@ def test_nvt_averages_match_the_oracle_within_two_standard_errors(gpu_lib):
     ctx.sync()
     eq = [s.get_state() for s in ctx.systems]
 
-    jobs = [(N, P, starts[i].box_bohr, e["q"], e["p"], T, dt, 9300 + i, steps, 0, i) for i, e in enumerate(eq)]
+    jobs = [(N, P, starts[i].box_bohr, e["q"], e["p"], T, dt, 9300 + i, steps, 0, i, head)
+            for i, e in enumerate(eq)]
     pool = mp.get_context("spawn").Pool(max(1, min(n_chain, os.cpu_count() or 1)))
     orc_async = pool.map_async(nvt_chain, jobs)
 
@@ -201,23 +209,28 @@ def test_nvt_averages_match_the_oracle_within_two_standard_errors(gpu_lib):
     ctx2.reset_estimators()
     ctx2.run_steps(steps, is_nvt=True)
     ctx2.sync()
-    dev = []
-    for s in ctx2.systems:
-        est = s.estimators()
-        assert len(est["pot"]) == steps
-        dev.append((float(np.mean(est["pot"])), float(np.mean(est["kcv"]))))
+    ests = [s.estimators() for s in ctx2.systems]
     try:
         orc = orc_async.get()
     finally:
         pool.close()
         pool.join()
 
+    for est, o in zip(ests, orc):
+        assert len(est["pot"]) == steps
+        dk = np.abs(est["kcv"][:head] - np.asarray(o[3])) / np.abs(np.asarray(o[3]))
+        dp = np.abs(est["pot"][:head] - np.asarray(o[2])) / np.abs(np.asarray(o[2]))
+        assert dk.max() < 1e-6, f"per-step kinetic estimator differs by {dk.max():.1e} relative"
+        assert dp.max() < 2e-5, f"per-step potential differs by {dp.max():.1e} relative"
+
     report, ok = [], True
-    for k, name in ((0, "potential"), (1, "kinetic (centroid virial)")):
-        d = np.array([a[k] - b[k] for a, b in zip(dev, orc)])
-        se = float(d.std(ddof=1) / np.sqrt(len(d)))
+    for k, key, name in ((0, "pot", "potential"), (1, "kcv", "kinetic (centroid virial)")):
+        g = np.array([float(np.mean(e[key])) for e in ests])
+        c = np.array([r[k] for r in orc])
+        se = float(np.hypot(g.std(ddof=1), c.std(ddof=1)) / np.sqrt(n_chain))
+        d = g - c
         ok = ok and abs(d.mean()) < 2.0 * se
-        report.append(f"{name}: device {np.mean([a[k] for a in dev]):.6f}, oracle {np.mean([b[k] for b in orc]):.6f}, "
-                      f"mean paired difference {d.mean():.2e} = {abs(d.mean()) / se:.2f} SE (SE {se:.1e})")
+        report.append(f"{name}: device {g.mean():.6f}, oracle {c.mean():.6f}, difference {d.mean():.2e} = "
+                      f"{abs(d.mean()) / se:.2f} SE (SE {se:.1e}; paired {abs(d.mean()) / (d.std(ddof=1) / np.sqrt(n_chain)):.2f})")
     print("; ".join(report))
     assert ok, "; ".join(report)

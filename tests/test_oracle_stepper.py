@@ -103,8 +103,9 @@ def test_nvt_chains_in_spawned_workers_are_seeded_and_distinct():
     from qtip4pf_water_gb300.start import seeded_start
 
     st = seeded_start(64, 2, 298.0, seed=5)
-    jobs = [(64, 2, st.box_bohr, st.q, st.p, 298.0, 0.5, s, 12, 2) for s in (7, 7, 8)]
+    jobs = [(64, 2, st.box_bohr, st.q, st.p, 298.0, 0.5, s, 12, 2, 0, 4) for s in (7, 7, 8)]
     with mp.get_context("spawn").Pool(2) as pool:
         a, b, c = pool.map(nvt_chain, jobs)
-    assert a == b and a != c
-    assert all(np.isfinite(x) for x in a + c)
+    assert a == b and a[:2] != c[:2]
+    assert all(np.isfinite(x) for x in a[:2] + c[:2])
+    assert len(a[2]) == len(a[3]) == 4 and a[2] != c[2]
