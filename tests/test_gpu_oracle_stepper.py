@@ -18,11 +18,12 @@ from FP64 by ~1e-7 relative; a step moves an atom ~1e-2 bohr); forces within
 the mixed-mode 1e-4 relative RMS, and 1e-6 in FP64 (forces at positions that
 differ by those 1e-8 bohr; the FP64 forces of one configuration are pinned
 at 1e-9 by the single-configuration tests); the mean centroid force within
-1e-6 (FP64) or 1e-4 (mixed) relative RMS. Statistics: 32 chains a side
-(device and oracle from one equilibrated state with one noise stream): the
-per-step estimator records while the trajectories stay together, then the
-run averages of the potential and the centroid-virial kinetic energy within
-two standard errors of the two sides' means.
+1e-6 (FP64) or 1e-4 (mixed) relative RMS. Statistics: 32 oracle chains and
+32 device chains from the same equilibrated states with the same noise
+streams (the per-step estimator records while the trajectories stay
+together, then the run averages), and 32 device chains with independent
+noise streams: the run averages of the potential and the centroid-virial
+kinetic energy within two standard errors of the two sides' means.
 """
 import numpy as np
 import pytest
@@ -174,7 +175,9 @@ def test_nvt_averages_match_the_oracle_within_two_standard_errors(gpu_lib):
       averages agree within two standard errors, each side's the spread of its
       32 chain averages / sqrt(32), combined in quadrature (the chains of a pair
       share a start and a noise stream, so the difference's own spread is
-      smaller and this bound conservative)."""
+      smaller and this bound conservative).
+    * The same holds for 32 more device chains from the same states with
+      independent noise streams (other seeds)."""
     import multiprocessing as mp
     import os
 
@@ -202,14 +205,20 @@ def test_nvt_averages_match_the_oracle_within_two_standard_errors(gpu_lib):
     pool = mp.get_context("spawn").Pool(max(1, min(n_chain, os.cpu_count() or 1)))
     orc_async = pool.map_async(nvt_chain, jobs)
 
-    ctx2 = q.Context([desc(st, 9300 + i) for i, st in enumerate(starts)], q.MIXED)
-    for s, e in zip(ctx2.systems, eq):
-        s.set_state(e["q"], e["p"])
-    ctx2.init_forces()
-    ctx2.reset_estimators()
-    ctx2.run_steps(steps, is_nvt=True)
-    ctx2.sync()
-    ests = [s.estimators() for s in ctx2.systems]
+    def device_chains(seed0):
+        c = q.Context([desc(st, seed0 + i) for i, st in enumerate(starts)], q.MIXED)
+        for s, e in zip(c.systems, eq):
+            s.set_state(e["q"], e["p"])
+        c.init_forces()
+        c.reset_estimators()
+        c.run_steps(steps, is_nvt=True)
+        c.sync()
+        out = [s.estimators() for s in c.systems]
+        c.close()
+        return out
+
+    ests = device_chains(9300)  # the oracle's noise streams
+    ests_ind = device_chains(9500)  # independent noise streams
     try:
         orc = orc_async.get()
     finally:
@@ -225,12 +234,14 @@ def test_nvt_averages_match_the_oracle_within_two_standard_errors(gpu_lib):
 
     report, ok = [], True
     for k, key, name in ((0, "pot", "potential"), (1, "kcv", "kinetic (centroid virial)")):
-        g = np.array([float(np.mean(e[key])) for e in ests])
         c = np.array([r[k] for r in orc])
-        se = float(np.hypot(g.std(ddof=1), c.std(ddof=1)) / np.sqrt(n_chain))
-        d = g - c
-        ok = ok and abs(d.mean()) < 2.0 * se
-        report.append(f"{name}: device {g.mean():.6f}, oracle {c.mean():.6f}, difference {d.mean():.2e} = "
-                      f"{abs(d.mean()) / se:.2f} SE (SE {se:.1e}; paired {abs(d.mean()) / (d.std(ddof=1) / np.sqrt(n_chain)):.2f})")
+        for label, chains in (("same noise", ests), ("independent noise", ests_ind)):
+            g = np.array([float(np.mean(e[key])) for e in chains])
+            se = float(np.hypot(g.std(ddof=1), c.std(ddof=1)) / np.sqrt(n_chain))
+            d = g - c
+            ok = ok and abs(d.mean()) < 2.0 * se
+            report.append(f"{name}, {label}: device {g.mean():.6f}, oracle {c.mean():.6f}, difference "
+                          f"{d.mean():.2e} = {abs(d.mean()) / se:.2f} SE (SE {se:.1e}; paired "
+                          f"{abs(d.mean()) / (d.std(ddof=1) / np.sqrt(n_chain)):.2f})")
     print("; ".join(report))
     assert ok, "; ".join(report)
