@@ -1836,17 +1836,18 @@ __global__ void __launch_bounds__(128) k_combine_f32(EvalArgs a) {
         const long long *rf = a.real_fix ? a.rfix + 3 * ((size_t)J.site_off + 3 * m0) : nullptr;
         for (int o = threadIdx.x; o < 9 * nm; o += blockDim.x) {
             float sum = 0.f, comp = 0.f;
-            int p = 0;
-            for (; p + 16 <= np; p += 16) {  // sixteen planes' loads in flight, then their sums in order
+            // the half-interaction real space's fixed-point sums (2^-40 units), loaded
+            // beside the planes
+            const long long rv = rf ? rf[o] : 0ll;
+            for (int p = 0; p < np; p += 16) {  // up to sixteen planes' loads in flight, then their sums in order
                 float v[16];
 #pragma unroll
-                for (int u = 0; u < 16; ++u) v[u] = pl[(p + u) * stride + o];
+                for (int u = 0; u < 16; ++u) v[u] = p + u < np ? pl[(p + u) * stride + o] : 0.f;
 #pragma unroll
-                for (int u = 0; u < 16; ++u) kahan_add(sum, comp, v[u]);
+                for (int u = 0; u < 16; ++u)
+                    if (p + u < np) kahan_add(sum, comp, v[u]);
             }
-            for (; p < np; ++p) kahan_add(sum, comp, pl[p * stride + o]);
-            // the half-interaction real space's fixed-point sums (2^-40 units)
-            if (rf) kahan_add(sum, comp, (float)((double)rf[o] * 9.094947017729282e-13));
+            if (rf) kahan_add(sum, comp, (float)((double)rv * 9.094947017729282e-13));
             fsum[o] = sum - comp;
         }
     }
