@@ -762,9 +762,12 @@ __global__ void __launch_bounds__(32 * RLW) k_real_list(EvalArgs a) {
 // back home. The stationary tile's own pairs (d = 0) are taken from both sides.
 // Sites are read as 32-bit fixed-point box fractions (k_prep), whose wrapped
 // integer differences are minimum-image separations to 2^-32 of the box.
-// Forces are written as partial planes, deterministic: plane `ch` holds the
-// stationary-side sums of chunk ch of the distances, plane n_ch + d - 1 the
-// visited-side sums of distance d (zero where that visit is not made).
+// Both sides' site forces are added into one array a configuration (a.rfix,
+// zeroed by k_prep_f32) as 64-bit fixed point (2^-40 Hartree/bohr) by integer
+// atomics: the visited sites' sums after each visit, the stationary sites' Kahan
+// sums over the block's distance chunk ch at the end. Integer addition is
+// associative, so the totals are the same bits whatever order the warps finish
+// in; k_combine_f32 reads the array after the float planes of the other terms.
 constexpr int HW = 4;  // warps per block
 constexpr float RFIX_SCALE = 1099511627776.0f;  // 2^40: fixed-point units of the real-space site forces
 __device__ __forceinline__ void rfix_add(long long *p, float x, float y, float z) {
