@@ -96,16 +96,18 @@ def test_same_seed_same_trajectory_different_seed_differs():
 
 def test_nvt_chains_in_spawned_workers_are_seeded_and_distinct():
     """The replica chains the statistical comparison runs in spawned worker
-    processes: one seed gives one run average, another seed another."""
+    processes: one (seed, system index) gives one run average, another seed or
+    another system index another."""
     import multiprocessing as mp
 
     from oracle.nvt_chain import nvt_chain
     from qtip4pf_water_gb300.start import seeded_start
 
     st = seeded_start(64, 2, 298.0, seed=5)
-    jobs = [(64, 2, st.box_bohr, st.q, st.p, 298.0, 0.5, s, 12, 2, 0, 4) for s in (7, 7, 8)]
+    jobs = [(64, 2, st.box_bohr, st.q, st.p, 298.0, 0.5, s, 12, 2, k, 4) for s, k in ((7, 0), (7, 0), (8, 0), (7, 1))]
     with mp.get_context("spawn").Pool(2) as pool:
-        a, b, c = pool.map(nvt_chain, jobs)
+        a, b, c, d = pool.map(nvt_chain, jobs)
     assert a == b and a[:2] != c[:2]
+    assert a[:2] != d[:2]  # the system index keys the noise too
     assert all(np.isfinite(x) for x in a[:2] + c[:2])
     assert len(a[2]) == len(a[3]) == 4 and a[2] != c[2]
