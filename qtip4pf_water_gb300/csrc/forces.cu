@@ -2457,7 +2457,7 @@ void launch_ewald(EvalArgs a, cudaStream_t s, unsigned long long *n, const Forks
         launch_prep_f32(a, s);
         // capture order: the reciprocal chain (the critical path: three dependent
         // kernels) first, then the Lennard-Jones branch, the real-space kernel last
-        // (it fills the SMs the others leave; captured first, the step took 11-13 %
+        // (it fills the SMs the others leave; captured first, the step took 11-14 %
         // longer)
         cudaEventRecord(forks->fork, s);
         cudaStreamWaitEvent(forks->side[0], forks->fork, 0);
