@@ -43,17 +43,12 @@ template <typename R> struct V2;
 template <> struct __align__(8) V2<float> { float x, y; };
 template <> struct __align__(16) V2<double> { double x, y; };
 
-__device__ __forceinline__ float f_erfc(float x) { return erfcf(x); }
 __device__ __forceinline__ double f_erfc(double x) { return erfc(x); }
-__device__ __forceinline__ float f_exp(float x) { return expf(x); }
 __device__ __forceinline__ double f_exp(double x) { return exp(x); }
 __device__ __forceinline__ float f_rint(float x) { return rintf(x); }
 __device__ __forceinline__ double f_rint(double x) { return rint(x); }
-__device__ __forceinline__ float f_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double f_sqrt(double x) { return sqrt(x); }
-__device__ __forceinline__ float f_acos(float x) { return acosf(x); }
 __device__ __forceinline__ double f_acos(double x) { return acos(x); }
-__device__ __forceinline__ void f_sincospi(float t, float *s, float *c) { sincospif(t, s, c); }
 __device__ __forceinline__ void f_sincospi(double t, double *s, double *c) { sincospi(t, s, c); }
 
 template <typename R> __device__ __forceinline__ R sys_box(const SysDev &S, int d);
